@@ -1,0 +1,408 @@
+// FP64-accurate Ozaki split GEMM on tcgen05 BF16 tensor cores.
+//
+// C += A * B (the semantics of the reference's GEMM, src/phpc_gemm.cu:55 and
+// the beta = 1 cuBLASXt call, src/phpc_gemm.cu:161-170) computed as:
+//
+//  1. Exponent scans (HBM-bound, integer work on the FP64 bit patterns):
+//     ea[i] = max_k e(A[i][k]), eb[j] = max_k e(B[k][j]) where e(x) is the
+//     integer with 2^(e-1) <= |x| < 2^e.
+//  2. Digit split (HBM-bound, integer only): every element is rounded to the
+//     P = 8s - 1 bit fixed-point grid of its row (A) or column (B),
+//     X = round(|x| * 2^(P - e)) < = 2^P, and X is cut into s balanced base-256
+//     digits d_1..d_s in [-128, 128] (sign applied to every digit), so that
+//     x ~= sum_p d_p * 2^(e + 1 - 8p). Each digit is an integer of at most 8
+//     significant bits and therefore exact in BF16. A's planes are stored
+//     [s][M][ldp] (K contiguous); B's are stored transposed, [s][N][ldp], so
+//     both MMA operands are K-major.
+//  3. The slice GEMM (tc_gemm.cuh, kOzaki): for every digit diagonal
+//     g = p + q <= s + 1 (the triangular truncation drops pairs whose weight is
+//     below 2^-8s of the leading one), S_g = sum_{p+q=g} A_p * B_q^T exactly
+//     (f32 chunks of 1024 products, int32 accumulation), then
+//     C += S_g * 2^(ea[i] + eb[j] + 2 - 8g) in FP64.
+//
+// FP64 arithmetic is used only in the fold (one int32->f64 conversion and one
+// multiply-add per element per diagonal): this GPU's FP64 rate is ~1 TFLOP/s,
+// ~2000x below its BF16 tensor rate.
+#include <algorithm>
+#include <cstdlib>
+
+#include <cuda_bf16.h>
+
+#include "phpc_host.hpp"
+#include "tc_gemm.cuh"
+
+namespace phpc {
+
+namespace {
+
+constexpr int kExpZero = -20000;     // exponent recorded for an all-zero row/column
+constexpr int kExpNonFinite = 20000; // exponent recorded when an inf/NaN is present
+
+__device__ __forceinline__ int exponent_of(double x, bool& nonfinite) {
+  const uint64_t b = static_cast<uint64_t>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
+  const int E = static_cast<int>(b >> 52);
+  if (E == 0x7FF) { nonfinite = true; return kExpNonFinite; }
+  if (E != 0) return E - 1022;
+  if (b == 0) return kExpZero;
+  return (64 - __clzll(static_cast<long long>(b))) - 1074;
+}
+
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// One warp per row of A: ea[i] = max_k e(A[i][k]).
+__global__ void scan_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K, int* __restrict__ ea,
+                                 int* status) {
+  const int warps = blockDim.x >> 5;
+  const int64_t row = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+  if (row >= M) return;
+  const double* a = A + row * lda;
+  int e = kExpZero;
+  bool nf = false;
+  for (int k = threadIdx.x & 31; k < K; k += 32) e = max(e, exponent_of(a[k], nf));
+  e = warp_max(e);
+  if ((threadIdx.x & 31) == 0) ea[row] = e;
+  if (__any_sync(0xffffffffu, nf) && (threadIdx.x & 31) == 0) record_error(status, PHPC_ERR_NONFINITE);
+}
+
+// eb[j] = max_k e(B[k][j]); eb is pre-filled with kExpZero, blockIdx.y splits K.
+__global__ void scan_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N, int krows,
+                                 int* __restrict__ eb, int* status) {
+  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= N) return;
+  const int k0 = blockIdx.y * krows, k1 = min(K, k0 + krows);
+  int e = kExpZero;
+  bool nf = false;
+  for (int k = k0; k < k1; ++k) e = max(e, exponent_of(B[(int64_t)k * ldb + col], nf));
+  if (e > kExpZero) atomicMax(&eb[col], e);
+  if (nf) record_error(status, PHPC_ERR_NONFINITE);
+}
+
+__global__ void fill_int_kernel(int* p, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+// Balanced base-256 digits of round(|x| * 2^(P - e)), P = 8s - 1, most
+// significant first, with the sign of x applied. Non-finite and zero inputs
+// give all-zero digits.
+__device__ __forceinline__ void split_digits(double x, int e, int s, int (&d)[8]) {
+  uint64_t b = static_cast<uint64_t>(__double_as_longlong(x));
+  const bool neg = (b >> 63) != 0;
+  b &= 0x7FFFFFFFFFFFFFFFull;
+  const int E = static_cast<int>(b >> 52);
+  uint64_t m = b & 0x000FFFFFFFFFFFFFull;
+  int elsb;
+  if (E == 0x7FF || e <= kExpZero || e >= kExpNonFinite) {
+    m = 0;
+    elsb = 0;
+  } else if (E != 0) {
+    m |= 1ull << 52;
+    elsb = E - 1075;
+  } else {
+    elsb = -1074;
+  }
+  const int P = 8 * s - 1;
+  const int sh = elsb + P - e;
+  uint64_t X;
+  if (m == 0) X = 0;
+  else if (sh >= 0) X = m << sh;  // |x| < 2^e  =>  X < 2^P <= 2^63
+  else if (sh > -64) X = (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
+  else X = 0;
+#pragma unroll
+  for (int p = 7; p >= 1; --p) {
+    if (p < s) {
+      const int r = static_cast<int>(X & 255u);
+      const int carry = r >= 128;
+      d[p] = r - (carry << 8);
+      X = (X >> 8) + carry;
+    } else {
+      d[p] = 0;
+    }
+  }
+  d[0] = static_cast<int>(X);  // <= 128
+  if (neg) {
+#pragma unroll
+    for (int p = 0; p < 8; ++p) d[p] = -d[p];
+  }
+}
+
+__device__ __forceinline__ uint16_t bf16_bits_of_int(int v) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(static_cast<float>(v)));
+}
+
+// A planes: plane p holds digit p of A[i][k] at [p][i][k] (row stride ldp).
+// Each thread converts 8 consecutive k and writes one 16-byte vector per plane.
+__global__ void split_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K, const int* __restrict__ ea,
+                                  int s, uint16_t* __restrict__ planes, int64_t ldp, int64_t plane_stride) {
+  const int64_t row = blockIdx.x;
+  const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
+  if (row >= M || k0 >= ldp) return;
+  const int e = ea[row];
+  const double* a = A + row * lda;
+  uint32_t packed[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; j += 2) {
+    int d0[8], d1[8];
+    const double x0 = (k0 + j < K) ? a[k0 + j] : 0.0;
+    const double x1 = (k0 + j + 1 < K) ? a[k0 + j + 1] : 0.0;
+    split_digits(x0, e, s, d0);
+    split_digits(x1, e, s, d1);
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+      packed[p][j >> 1] = static_cast<uint32_t>(bf16_bits_of_int(d0[p])) |
+                          (static_cast<uint32_t>(bf16_bits_of_int(d1[p])) << 16);
+  }
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    if (p < s) {
+      uint4 v = make_uint4(packed[p][0], packed[p][1], packed[p][2], packed[p][3]);
+      *reinterpret_cast<uint4*>(planes + p * plane_stride + row * ldp + k0) = v;
+    }
+  }
+}
+
+// B planes, transposed: plane p holds digit p of B[k][j] at [p][j][k].
+// A CTA converts a 32 (k) x 64 (j) block: reads are coalesced along j, the
+// digits are staged in shared memory as packed k-pairs, writes are 16-byte
+// vectors along k.
+__global__ void __launch_bounds__(256) split_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
+                                                         const int* __restrict__ eb, int s,
+                                                         uint16_t* __restrict__ planes, int64_t ldp,
+                                                         int64_t plane_stride) {
+  __shared__ uint32_t st[8][64][17];  // [plane][j][k pair], padded row
+  const int j = threadIdx.x & 63;
+  const int kp0 = threadIdx.x >> 6;   // 0..3
+  const int64_t k0 = (int64_t)blockIdx.y * 32;
+  const int64_t j0 = (int64_t)blockIdx.x * 64;
+  const int64_t col = j0 + j;
+  const int e = col < N ? eb[col] : kExpZero;
+  for (int kp = kp0; kp < 16; kp += 4) {
+    const int64_t k = k0 + 2 * kp;
+    const double x0 = (col < N && k < K) ? B[k * ldb + col] : 0.0;
+    const double x1 = (col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0;
+    int d0[8], d1[8];
+    split_digits(x0, e, s, d0);
+    split_digits(x1, e, s, d1);
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+      if (p < s)
+        st[p][j][kp] = static_cast<uint32_t>(bf16_bits_of_int(d0[p])) |
+                       (static_cast<uint32_t>(bf16_bits_of_int(d1[p])) << 16);
+  }
+  __syncthreads();
+  const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;  // row j of the tile, 16-byte quarter of its 64-byte run
+  const int64_t gj = j0 + wj;
+  const int64_t gk = k0 + 8 * q;
+  if (gj >= N || gk >= ldp) return;
+  for (int p = 0; p < s; ++p) {
+    uint4 v = make_uint4(st[p][wj][4 * q], st[p][wj][4 * q + 1], st[p][wj][4 * q + 2], st[p][wj][4 * q + 3]);
+    *reinterpret_cast<uint4*>(planes + p * plane_stride + gj * ldp + gk) = v;
+  }
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct OzakiLayout {
+  int64_t ldp;
+  size_t off_ea, off_eb, off_pa, off_pb, total;
+};
+
+OzakiLayout ozaki_layout(int m, int k, int n, int s) {
+  OzakiLayout L;
+  L.ldp = ((int64_t)k + 7) / 8 * 8;
+  L.off_ea = 0;
+  L.off_eb = align256(L.off_ea + sizeof(int) * (size_t)m);
+  L.off_pa = align256(L.off_eb + sizeof(int) * (size_t)n);
+  L.off_pb = align256(L.off_pa + (size_t)s * m * L.ldp * 2);
+  L.total = align256(L.off_pb + (size_t)s * n * L.ldp * 2);
+  return L;
+}
+
+// Pairs (p, q) with p + q <= s + 1, grouped by diagonal g = p + q (1-based digits).
+PairList ozaki_pairs(int s) {
+  PairList pl{};
+  pl.n = 0;
+  for (int g = 2; g <= s + 1; ++g)
+    for (int p = 1; p < g; ++p) {
+      const int q = g - p;
+      if (p > s || q > s) continue;
+      pl.a[pl.n] = static_cast<uint8_t>(p - 1);
+      pl.b[pl.n] = static_cast<uint8_t>(q - 1);
+      pl.g[pl.n] = static_cast<uint8_t>(g);
+      ++pl.n;
+    }
+  return pl;
+}
+
+}  // namespace
+
+// Launches the tcgen05 slice GEMM over bf16 planes (shared with the 3xBF16 path).
+template <int BN, int MODE>
+int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
+                         int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
+                         cudaStream_t stream) {
+  using Cfg = TcCfg<BN>;
+  const DeviceInfo* dev = current_device();
+  if (!dev) return PHPC_ERR_CUDA;
+  CUtensorMap tmA, tmB;
+  const uint64_t dA[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)nplanesA};
+  const uint64_t sA[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * m};
+  const uint32_t bA[3] = {kTcBK, kTcBM, 1};
+  const uint64_t dB[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)nplanesB};
+  const uint64_t sB[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * n};
+  const uint32_t bB[3] = {kTcBK, (uint32_t)BN, 1};
+  if (!encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesA, dA, sA, bA, CU_TENSOR_MAP_SWIZZLE_128B) ||
+      !encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesB, dB, sB, bB, CU_TENSOR_MAP_SWIZZLE_128B))
+    return PHPC_ERR_CUDA;
+  TcArgs a{};
+  a.M = m;
+  a.N = n;
+  a.K = k;
+  a.tm = ceil_div(m, kTcBM);
+  a.tn = ceil_div(n, BN);
+  a.group_rows = 8;
+  a.C = C;
+  a.ldc = ldc;
+  a.ea = ea;
+  a.eb = eb;
+  a.status = device_status_ptr();
+  const char* gr = getenv("PHPC_GROUP_ROWS");
+  if (gr && atoi(gr) > 0) a.group_rows = atoi(gr);
+  auto kern = tc_slice_gemm_kernel<BN, MODE>;
+  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
+  const int ntiles = a.tm * a.tn;
+  const int grid = std::min(ntiles, dev->sm_count);
+  kern<<<grid, kTcThreads, Cfg::kSmem, stream>>>(tmA, tmB, pairs, a);
+  PHPC_CUDA_TRY(cudaGetLastError());
+  return PHPC_OK;
+}
+
+template int launch_tc_slice_gemm<256, kF32>(const void*, const void*, int, int, int64_t, int, int, int,
+                                              const PairList&, void*, int64_t, const int*, const int*, cudaStream_t);
+template int launch_tc_slice_gemm<128, kF32>(const void*, const void*, int, int, int64_t, int, int, int,
+                                              const PairList&, void*, int64_t, const int*, const int*, cudaStream_t);
+
+size_t ozaki_workspace_bytes(int m, int k, int n, int s) { return ozaki_layout(m, k, n, s).total; }
+
+int ozaki_prepare(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
+                  size_t ws_bytes, cudaStream_t stream) {
+  const DeviceInfo* dev = current_device();
+  if (!dev) return PHPC_ERR_CUDA;
+  if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
+  const OzakiLayout L = ozaki_layout(m, k, n, s);
+  if (!ws || ws_bytes < L.total || !aligned16(ws)) return PHPC_ERR_WORKSPACE;
+  uint8_t* base = static_cast<uint8_t*>(ws);
+  int* ea = reinterpret_cast<int*>(base + L.off_ea);
+  int* eb = reinterpret_cast<int*>(base + L.off_eb);
+  uint16_t* pa = reinterpret_cast<uint16_t*>(base + L.off_pa);
+  uint16_t* pb = reinterpret_cast<uint16_t*>(base + L.off_pb);
+  int* status = device_status_ptr();
+
+  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream>>>(dA, lda, m, k, ea, status);
+  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(eb, n, kExpZero);
+  {
+    const int krows = 256;
+    dim3 g(ceil_div(n, 256), ceil_div(k, krows));
+    scan_cols_kernel<<<g, 256, 0, stream>>>(dB, ldb, k, n, krows, eb, status);
+  }
+  {
+    dim3 g(m, ceil_div(L.ldp / 8, 128));
+    split_rows_kernel<<<g, 128, 0, stream>>>(dA, lda, m, k, ea, s, pa, L.ldp, (int64_t)m * L.ldp);
+  }
+  {
+    dim3 g(ceil_div(n, 64), ceil_div(k, 32));
+    split_cols_kernel<<<g, 256, 0, stream>>>(dB, ldb, k, n, eb, s, pb, L.ldp, (int64_t)n * L.ldp);
+  }
+  PHPC_CUDA_TRY(cudaGetLastError());
+  return PHPC_OK;
+}
+
+int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const void* ws, size_t ws_bytes,
+                   cudaStream_t stream, int bn) {
+  const OzakiLayout L = ozaki_layout(m, k, n, s);
+  if (!ws || ws_bytes < L.total || !aligned16(ws)) return PHPC_ERR_WORKSPACE;
+  const uint8_t* base = static_cast<const uint8_t*>(ws);
+  const int* ea = reinterpret_cast<const int*>(base + L.off_ea);
+  const int* eb = reinterpret_cast<const int*>(base + L.off_eb);
+  const void* pa = base + L.off_pa;
+  const void* pb = base + L.off_pb;
+  const PairList pl = ozaki_pairs(s);
+  if (bn == 128)
+    return launch_tc_slice_gemm<128, kOzaki>(pa, pb, s, s, L.ldp, m, n, k, pl, dC, ldc, ea, eb, stream);
+  return launch_tc_slice_gemm<256, kOzaki>(pa, pb, s, s, L.ldp, m, n, k, pl, dC, ldc, ea, eb, stream);
+}
+
+int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
+                int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
+  const int rc = ozaki_prepare(m, k, n, dA, lda, dB, ldb, s, ws, ws_bytes, stream);
+  if (rc != PHPC_OK) return rc;
+  return ozaki_multiply(m, k, n, dC, ldc, s, ws, ws_bytes, stream, bn);
+}
+
+}  // namespace phpc
+
+extern "C" size_t phpc_ozaki_workspace_bytes(int m, int k, int n, int slices) {
+  if (m <= 0 || k <= 0 || n <= 0 || slices < 2 || slices > 8) return 0;
+  return phpc::ozaki_workspace_bytes(m, k, n, slices);
+}
+
+namespace {
+int check_ozaki_args(int m, int k, int n, int slices) {
+  if (m < 0 || k < 0 || n < 0 || slices < 2 || slices > 8) return PHPC_ERR_ARG;
+  return PHPC_OK;
+}
+}  // namespace
+
+extern "C" int phpc_ozaki_prepare_dev(int m, int k, int n, const double* dA, int64_t lda, const double* dB,
+                                      int64_t ldb, int slices, void* workspace, size_t workspace_bytes,
+                                      void* stream) {
+  using namespace phpc;
+  int rc = check_ozaki_args(m, k, n, slices);
+  if (rc == PHPC_OK && m > 0 && n > 0 && k > 0) {
+    if (!dA || !dB || lda < k || ldb < n)
+      rc = PHPC_ERR_ARG;
+    else
+      rc = ozaki_prepare(m, k, n, dA, lda, dB, ldb, slices, workspace, workspace_bytes,
+                         static_cast<cudaStream_t>(stream));
+  }
+  set_last_error(rc);
+  return rc;
+}
+
+extern "C" int phpc_ozaki_multiply_dev(int m, int k, int n, double* dC, int64_t ldc, int slices,
+                                       const void* workspace, size_t workspace_bytes, void* stream) {
+  using namespace phpc;
+  int rc = check_ozaki_args(m, k, n, slices);
+  if (rc == PHPC_OK && m > 0 && n > 0 && k > 0) {
+    if (!dC || ldc < n)
+      rc = PHPC_ERR_ARG;
+    else
+      rc = ozaki_multiply(m, k, n, dC, ldc, slices, workspace, workspace_bytes, static_cast<cudaStream_t>(stream),
+                          default_bn(m, k, n));
+  }
+  set_last_error(rc);
+  return rc;
+}
+
+extern "C" int phpc_dgemm_ozaki_dev(int m, int k, int n, const double* dA, int64_t lda, const double* dB,
+                                    int64_t ldb, double* dC, int64_t ldc, int slices, void* workspace,
+                                    size_t workspace_bytes, void* stream) {
+  using namespace phpc;
+  int rc;
+  if (m < 0 || k < 0 || n < 0 || slices < 2 || slices > 8) {
+    rc = PHPC_ERR_ARG;
+  } else if (m == 0 || n == 0 || k == 0) {
+    rc = PHPC_OK;
+  } else if (!dA || !dB || !dC || lda < k || ldb < n || ldc < n) {
+    rc = PHPC_ERR_ARG;
+  } else {
+    rc = dgemm_ozaki(m, k, n, dA, lda, dB, ldb, dC, ldc, slices, workspace, workspace_bytes,
+                     static_cast<cudaStream_t>(stream), default_bn(m, k, n));
+  }
+  set_last_error(rc);
+  return rc;
+}

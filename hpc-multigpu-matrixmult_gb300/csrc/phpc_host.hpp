@@ -1,0 +1,60 @@
+// Host-side internals shared by the library's translation units: the
+// per-thread status, the device status word, device properties and TMA
+// tensor-map encoding through the driver entry point (no link-time libcuda).
+#pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+
+#include "phpc_gemm.h"
+
+namespace phpc {
+
+// Per-thread status of the last public call.
+void set_last_error(int code);
+int get_last_error();
+
+// Device status word (a file-scope __device__ int, one per device). Kernels
+// receive its device address and record timeouts there.
+int* device_status_ptr();
+
+// Properties of the current device, cached per device ordinal.
+struct DeviceInfo {
+  int ordinal;
+  int sm_count;
+  int cc_major, cc_minor;
+  size_t smem_optin;
+};
+const DeviceInfo* current_device();
+
+// cuTensorMapEncodeTiled, resolved once through cudaGetDriverEntryPointByVersion.
+bool encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
+                  const uint64_t* strides_bytes /* rank-1 entries */, const uint32_t* box, CUtensorMapSwizzle swz);
+
+#define PHPC_CUDA_TRY(expr)                                                                        \
+  do {                                                                                             \
+    cudaError_t _e = (expr);                                                                       \
+    if (_e != cudaSuccess) {                                                                       \
+      if (getenv("PHPC_VERBOSE"))                                                                  \
+        fprintf(stderr, "phpc: %s failed at %s:%d: %s\n", #expr, __FILE__, __LINE__, cudaGetErrorString(_e)); \
+      return PHPC_ERR_CUDA;                                                                        \
+    }                                                                                              \
+  } while (0)
+
+// Library-internal launchers (device pointers, asynchronous on `stream`).
+int dgemm_dmma(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
+               int64_t ldc, int gw, int gh, int kpanel, cudaStream_t stream);
+int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
+                int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
+size_t ozaki_workspace_bytes(int m, int k, int n, int s);
+int default_slices(int m, int k, int n);
+int default_bn(int m, int k, int n);
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+inline int ceil_div(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }
+
+}  // namespace phpc

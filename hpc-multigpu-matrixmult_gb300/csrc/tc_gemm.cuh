@@ -1,0 +1,324 @@
+// Persistent tcgen05 slice GEMM: C (+)= sum over a list of (A plane, B plane)
+// pairs of A_p[M x K] * B_q[N x K]^T, with bf16 digit/slice planes streamed by
+// TMA and products accumulated by tcgen05.mma (kind::f16, f32 accumulators in
+// TMEM). Two epilogues:
+//
+//  kOzaki  Exact-integer Ozaki accumulation. The pair list is grouped by digit
+//          diagonal g = p + q; every pair of a group has the same power-of-two
+//          weight. MMAs accumulate at most 16 K-steps of 64 (1024 products of
+//          |d| <= 128, |sum| <= 2^24, exact in f32) into one TMEM buffer; the
+//          epilogue converts each chunk to int32 (exact) and adds it into
+//          per-thread int32 registers. At the end of a group (or after 127
+//          chunks, before int32 could overflow) it folds the integer sums into
+//          the FP64 output: C[i][j] += S * 2^(ea[i] + eb[j] + 2 - 8g).
+//  kF32    One f32 accumulation over all pairs and K (3xBF16 split GEMM);
+//          at the end of the tile C[i][j] += acc (float).
+//
+// Warp roles (320 threads): warp 0 = TMA producer, warp 1 = TMEM allocator and
+// single-thread MMA issuer, warps 2..9 = epilogue. Epilogue warp w reads TMEM
+// lanes 32*(w%4) .. +31 (the lane quadrant tcgen05.ld allows it) and column
+// half (w-2)/4 of the BN-wide accumulator. Two TMEM accumulator buffers let
+// the MMA of chunk c+1 overlap the epilogue of chunk c.
+#pragma once
+#include "phpc_dev.cuh"
+
+namespace phpc {
+
+enum TcMode { kOzaki = 0, kF32 = 1 };
+
+constexpr int kTcBM = 128;
+constexpr int kTcBK = 64;              // bf16 elements of K per stage (one 128-byte swizzle row)
+constexpr int kTcMaxPairs = 64;
+constexpr int kTcChunkSteps = 16;      // 16 x 64 = 1024 products per exact f32 chunk
+constexpr int kTcFoldChunks = 127;     // 127 chunks of |v| <= 2^24 keep |int32 sum| < 2^31
+constexpr int kTcEpiWarps = 8;
+constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
+
+struct PairList {
+  int n;                      // number of (A plane, B plane) pairs
+  uint8_t a[kTcMaxPairs];     // A plane index (0-based)
+  uint8_t b[kTcMaxPairs];     // B plane index (0-based)
+  uint8_t g[kTcMaxPairs];     // group id (Ozaki: diagonal p + q, 1-based digits); pairs of a group are contiguous
+};
+
+struct TcArgs {
+  int M, N, K;
+  int tm, tn;                 // tiles along M (128) and N (BN)
+  int group_rows;             // tile rows per L2 raster group
+  void* C;                    // double* (kOzaki) or float* (kF32)
+  int64_t ldc;
+  const int* ea;              // kOzaki: per-row exponent of A
+  const int* eb;              // kOzaki: per-column exponent of B
+  int* status;
+};
+
+template <int BN>
+struct TcCfg {
+  static constexpr int kStages = BN == 256 ? 4 : 6;
+  static constexpr int kStageA = kTcBM * kTcBK * 2;
+  static constexpr int kStageB = BN * kTcBK * 2;
+  static constexpr int kStageBytes = kStageA + kStageB;
+  static constexpr int kScratchPerWarp = 32 * 33 * 4;       // 32x32 transpose tile, padded
+  static constexpr int kTmemCols = 2 * BN;                  // two accumulator buffers
+  static constexpr size_t kSmem =
+      (size_t)kStages * kStageBytes + kTcEpiWarps * kScratchPerWarp + 256 /*barriers*/ + 1024 /*align*/;
+};
+
+__device__ __forceinline__ void tc_tile_coords(const TcArgs& a, int t, int& rm, int& rn) {
+  const int per_group = a.group_rows * a.tn;
+  const int grp = t / per_group;
+  const int r0 = grp * a.group_rows;
+  const int rows = min(a.group_rows, a.tm - r0);
+  const int w = t - grp * per_group;
+  rn = w / rows;
+  rm = r0 + w % rows;
+}
+
+// 2^x as a double for any int x (0 below the subnormal range, inf above).
+__device__ __forceinline__ double fold_term(int32_t s, int x) {
+  const double v = static_cast<double>(s);
+  if (x >= -1022 && x <= 1023) return v * __longlong_as_double(static_cast<long long>(x + 1023) << 52);
+  if (s == 0) return 0.0;
+  return ldexp(v, x);
+}
+
+template <int BN, int MODE>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    tc_slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                         const __grid_constant__ PairList pairs, const __grid_constant__ TcArgs args) {
+  using Cfg = TcCfg<BN>;
+  constexpr int S = Cfg::kStages;
+  constexpr int HALF = BN / 2;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* scratch = smem + S * Cfg::kStageBytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(scratch + kTcEpiWarps * Cfg::kScratchPerWarp);
+  uint64_t* empty = full + S;
+  uint64_t* tfull = empty + S;      // [2] MMA -> epilogue
+  uint64_t* tempty = tfull + 2;     // [2] epilogue -> MMA
+  uint64_t* drain = tempty + 2;     // MMA issuer waits here for its last MMAs before teardown
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = args.tm * args.tn;
+  const int nk = (args.K + kTcBK - 1) / kTcBK;
+  int* status = args.status;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kTcEpiWarps);
+    }
+    mbar_init(drain, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------------ TMA
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int rm, rn;
+        tc_tile_coords(args, t, rm, rn);
+        for (int pi = 0; pi < pairs.n && ok; ++pi) {
+          const int pa = pairs.a[pi], pb = pairs.b[pi];
+          for (int kb = 0; kb < nk; ++kb) {
+            if (!wait_parity(&empty[stage], phase ^ 1, status, 11)) { ok = false; break; }
+            mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
+            uint8_t* sa = smem + stage * Cfg::kStageBytes;
+            tma_load_3d(sa, &tmA, kb * kTcBK, rm * kTcBM, pa, &full[stage]);
+            tma_load_3d(sa + Cfg::kStageA, &tmB, kb * kTcBK, rn * BN, pb, &full[stage]);
+            ++issued;
+            if (++stage == S) { stage = 0; phase ^= 1; }
+          }
+        }
+      }
+      if (!ok) {
+        int s = stage;
+        uint32_t ph = phase;
+        for (int i = 0; i < min(issued, S); ++i) {
+          if (--s < 0) { s = S - 1; ph ^= 1; }
+          const uint32_t addr = smem_u32(&full[s]);
+          const uint64_t t0 = globaltimer_ns();
+          while (!mbar_try_wait(addr, ph) && globaltimer_ns() - t0 < PHPC_WAIT_LIMIT_NS) {}
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------------ MMA
+    if (lane == 0) {
+      constexpr uint32_t idesc = idesc_bf16_f32(kTcBM, BN);
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t tphase[2] = {0, 0};
+      int buf = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int gstart = 0;
+        while (gstart < pairs.n && ok) {
+          int gend = gstart + 1;
+          if (MODE == kOzaki)
+            while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
+          else
+            gend = pairs.n;
+          const int total = (gend - gstart) * nk;
+          const int chunk = MODE == kOzaki ? kTcChunkSteps : total;
+          for (int done = 0; done < total && ok; done += chunk) {
+            const int len = min(chunk, total - done);
+            if (!wait_parity(&tempty[buf], tphase[buf] ^ 1, status, 12)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t dt = tmem_base + buf * BN;
+            for (int s = 0; s < len; ++s) {
+              if (!wait_parity(&full[stage], phase, status, 13)) { ok = false; break; }
+              tc_fence_after();
+              const uint32_t sa = smem_u32(smem + stage * Cfg::kStageBytes);
+              const uint64_t adesc = sdesc_kmajor_sw128(sa);
+              const uint64_t bdesc = sdesc_kmajor_sw128(sa + Cfg::kStageA);
+#pragma unroll
+              for (int kk = 0; kk < kTcBK / 16; ++kk)
+                tc_mma_bf16(dt, adesc + 2 * kk, bdesc + 2 * kk, idesc, (s > 0 || kk > 0) ? 1u : 0u);
+              tc_commit(&empty[stage]);
+              if (++stage == S) { stage = 0; phase ^= 1; }
+            }
+            if (!ok) break;
+            tc_commit(&tfull[buf]);
+            tphase[buf] ^= 1;
+            buf ^= 1;
+          }
+          gstart = gend;
+        }
+      }
+      // Every MMA this thread issued has completed once the drain barrier
+      // flips, so TMEM can be released safely even on the error path.
+      tc_commit(drain);
+      const uint32_t daddr = smem_u32(drain);
+      const uint64_t t0 = globaltimer_ns();
+      while (!mbar_try_wait(daddr, 0) && globaltimer_ns() - t0 < PHPC_WAIT_LIMIT_NS) {}
+    }
+  } else {
+    // ------------------------------------------------------------- epilogue
+    const int ew = warp - 2;
+    const int quad = warp & 3;              // TMEM lane quadrant of this warp
+    const int half = ew >> 2;               // column half of the accumulator
+    uint32_t* tr = reinterpret_cast<uint32_t*>(scratch + ew * Cfg::kScratchPerWarp);  // [32][33]
+    uint32_t tphase[2] = {0, 0};
+    int buf = 0;
+    bool ok = true;
+    int32_t acc[HALF];  // kOzaki: exact int32 sums; kF32: raw f32 bits of the accumulator
+#pragma unroll
+    for (int j = 0; j < HALF; ++j) acc[j] = 0;
+
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int rm, rn;
+      tc_tile_coords(args, t, rm, rn);
+      const int64_t row0 = (int64_t)rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
+      const int col0 = rn * BN + half * HALF;                 // first global column of this warp's half
+      int my_ea = 0;
+      if (MODE == kOzaki) {
+        const int64_t r = row0 + lane;
+        my_ea = r < args.M ? max(args.ea[r], -20000) : -20000;
+      }
+      int gstart = 0;
+      while (gstart < pairs.n && ok) {
+        int gend = gstart + 1;
+        if (MODE == kOzaki)
+          while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
+        else
+          gend = pairs.n;
+        const int total = (gend - gstart) * nk;
+        const int chunk = MODE == kOzaki ? kTcChunkSteps : total;
+        const int nchunks = (total + chunk - 1) / chunk;
+        for (int c = 0; c < nchunks && ok; ++c) {
+          // all lanes must agree before the warp-collective tcgen05.ld below
+          ok = __all_sync(0xffffffffu, wait_parity(&tfull[buf], tphase[buf], status, 14));
+          if (!ok) break;
+          tc_fence_after();
+          const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + buf * BN + half * HALF;
+          if (MODE == kOzaki) {
+#pragma unroll
+            for (int cb = 0; cb < HALF; cb += 32) {
+              uint32_t r[32];
+              tmem_ld_32x32b_x32(taddr + cb, r);
+              tc_wait_ld();
+#pragma unroll
+              for (int j = 0; j < 32; ++j) acc[cb + j] += __float2int_rn(__uint_as_float(r[j]));
+            }
+          } else {
+#pragma unroll
+            for (int cb = 0; cb < HALF; cb += 32) {
+              uint32_t r[32];
+              tmem_ld_32x32b_x32(taddr + cb, r);
+              tc_wait_ld();
+#pragma unroll
+              for (int j = 0; j < 32; ++j) acc[cb + j] = (int32_t)r[j];  // raw f32 bits
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&tempty[buf]);
+          tphase[buf] ^= 1;
+          buf ^= 1;
+
+          const bool group_end = (c == nchunks - 1);
+          const bool fold = MODE == kOzaki ? (group_end || ((c + 1) % kTcFoldChunks) == 0) : group_end;
+          if (!fold) continue;
+          // Write the warp's 32 rows x HALF columns out, 32 columns at a time,
+          // transposed through shared memory so that a warp touches one
+          // contiguous 32-element run of a row per access.
+          const int gexp = MODE == kOzaki ? 2 - 8 * (int)pairs.g[gstart] : 0;
+#pragma unroll
+          for (int cb = 0; cb < HALF; cb += 32) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) tr[lane * 33 + j] = (uint32_t)acc[cb + j];
+            __syncwarp();
+            const int col = col0 + cb + lane;
+            const bool col_ok = col < args.N;
+            int col_e = 0;
+            if (MODE == kOzaki) col_e = col_ok ? max(args.eb[col], -20000) : -20000;
+            for (int r = 0; r < 32; ++r) {
+              const int64_t grow = row0 + r;
+              const int row_e = __shfl_sync(0xffffffffu, my_ea, r);
+              if (grow < args.M && col_ok) {
+                const uint32_t v = tr[r * 33 + lane];
+                if (MODE == kOzaki) {
+                  double* cp = static_cast<double*>(args.C) + grow * args.ldc + col;
+                  *cp += fold_term((int32_t)v, row_e + col_e + gexp);
+                } else {
+                  float* cp = static_cast<float*>(args.C) + grow * args.ldc + col;
+                  *cp += __uint_as_float(v);
+                }
+              }
+            }
+            __syncwarp();
+          }
+#pragma unroll
+          for (int j = 0; j < HALF; ++j) acc[j] = 0;
+        }
+        gstart = gend;
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem_base, Cfg::kTmemCols);
+  }
+}
+
+}  // namespace phpc

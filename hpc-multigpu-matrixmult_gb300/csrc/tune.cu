@@ -1,0 +1,90 @@
+// Slice-count selection for the Ozaki GEMM.
+//
+// Order of precedence: the PHPC_SLICES environment variable (2..8), then the
+// tuning table written by the autotuner (PHPC_TUNE_TABLE, or tune_table.txt
+// next to the library), then the built-in default of 7 slices (55-bit digit
+// grids: Frobenius error well below 1e-14 even for inputs whose exponents
+// spread over 2^+-20 inside a row).
+#include <dlfcn.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "phpc_host.hpp"
+
+namespace phpc {
+namespace {
+
+struct TuneEntry {
+  long long max_mnk;  // entry applies to problems with m*n*k <= max_mnk (first match wins)
+  int slices;
+  int bn;
+};
+
+std::once_flag g_once;
+std::vector<TuneEntry> g_table;
+
+std::string library_dir() {
+  Dl_info info;
+  if (dladdr(reinterpret_cast<void*>(&library_dir), &info) && info.dli_fname) {
+    std::string p(info.dli_fname);
+    const size_t s = p.rfind('/');
+    if (s != std::string::npos) return p.substr(0, s);
+  }
+  return ".";
+}
+
+// Table format (text): one entry per line, "max_mnk slices bn", '#' comments.
+void load_table() {
+  const char* env = getenv("PHPC_TUNE_TABLE");
+  const std::string path = env ? std::string(env) : library_dir() + "/tune_table.txt";
+  FILE* f = fopen(path.c_str(), "r");
+  if (!f) return;
+  char line[256];
+  while (fgets(line, sizeof line, f)) {
+    if (line[0] == '#') continue;
+    TuneEntry e{};
+    if (sscanf(line, "%lld %d %d", &e.max_mnk, &e.slices, &e.bn) == 3 && e.slices >= 2 && e.slices <= 8 &&
+        (e.bn == 128 || e.bn == 256))
+      g_table.push_back(e);
+  }
+  fclose(f);
+}
+
+const TuneEntry* lookup(int m, int k, int n) {
+  std::call_once(g_once, load_table);
+  const long long mnk = (long long)m * n * k;
+  for (const TuneEntry& e : g_table)
+    if (mnk <= e.max_mnk) return &e;
+  return nullptr;
+}
+
+}  // namespace
+
+int default_slices(int m, int k, int n) {
+  const char* env = getenv("PHPC_SLICES");
+  if (env) {
+    const int s = atoi(env);
+    if (s >= 2 && s <= 8) return s;
+  }
+  if (const TuneEntry* e = lookup(m, k, n)) return e->slices;
+  return 7;
+}
+
+int default_bn(int m, int k, int n) {
+  const char* env = getenv("PHPC_OZAKI_BN");
+  if (env) {
+    const int b = atoi(env);
+    if (b == 128 || b == 256) return b;
+  }
+  if (const TuneEntry* e = lookup(m, k, n)) return e->bn;
+  return 256;
+}
+
+}  // namespace phpc
+
+extern "C" int phpc_default_slices(int m, int k, int n) { return phpc::default_slices(m, k, n); }

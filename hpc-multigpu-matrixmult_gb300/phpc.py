@@ -1,0 +1,186 @@
+"""Python view of the C ABI in include/phpc_gemm.h (ctypes over lib/libphpc_gemm.so).
+
+Mirrors the reference's local-GEMM interface (src/phpc_gemm.cuh:4-14):
+``gemm_cuda`` / ``gemm_cublas`` take host row-major float64 arrays with
+leading dimensions in elements, compute C += A @ B in place and return the
+device time in seconds, as the reference's ``*compute_time`` out-argument
+does. The reference has no error returns; here a non-zero status raises
+``PhpcError``. The ``*_dev`` functions take device pointers (torch tensors or
+integers) and a CUDA stream.
+
+There is no CPU fallback: importing this module fails if the CUDA library has
+not been built, and every call fails if no sm_103 device is present.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "lib" / "libphpc_gemm.so"
+SUMMA_PATH = PKG / "lib" / "libphpc_summa.so"
+MAIN_OUT = PKG / "bin" / "main.out"
+
+if not LIB_PATH.exists():
+    raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (nvcc, sm_103a) first")
+
+_dp = ct.POINTER(ct.c_double)
+_fp = ct.POINTER(ct.c_float)
+_lib = ct.CDLL(str(LIB_PATH))
+
+_REF_SIG = [_dp, ct.c_int, _dp, ct.c_int, _dp, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+            ct.c_int, _fp]
+_lib.phpc_gemm_cuda.argtypes = _REF_SIG
+_lib.phpc_gemm_cuda.restype = None
+_lib.phpc_gemm_cublas.argtypes = _REF_SIG
+_lib.phpc_gemm_cublas.restype = None
+_lib.phpc_last_error.restype = ct.c_int
+_lib.phpc_error_string.argtypes = [ct.c_int]
+_lib.phpc_error_string.restype = ct.c_char_p
+_lib.phpc_device_status.restype = ct.c_int
+_lib.phpc_dgemm_dmma_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_int64,
+                                     ct.c_void_p, ct.c_int64, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p]
+_lib.phpc_dgemm_dmma_dev.restype = ct.c_int
+_lib.phpc_ozaki_workspace_bytes.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+_lib.phpc_ozaki_workspace_bytes.restype = ct.c_size_t
+_lib.phpc_dgemm_ozaki_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p,
+                                      ct.c_int64, ct.c_void_p, ct.c_int64, ct.c_int, ct.c_void_p, ct.c_size_t,
+                                      ct.c_void_p]
+_lib.phpc_dgemm_ozaki_dev.restype = ct.c_int
+_lib.phpc_default_slices.argtypes = [ct.c_int, ct.c_int, ct.c_int]
+_lib.phpc_default_slices.restype = ct.c_int
+_lib.phpc_ozaki_prepare_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p,
+                                        ct.c_int64, ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_ozaki_prepare_dev.restype = ct.c_int
+_lib.phpc_ozaki_multiply_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_int,
+                                         ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_ozaki_multiply_dev.restype = ct.c_int
+_lib.phpc_dgemm_dd_rows_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p,
+                                        ct.c_int64, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_int, ct.c_void_p,
+                                        ct.c_int64, ct.c_void_p]
+_lib.phpc_dgemm_dd_rows_dev.restype = ct.c_int
+_lib.phpc_fill_uniform_dev.argtypes = [ct.c_void_p, ct.c_size_t, ct.c_uint64, ct.c_uint64, ct.c_void_p]
+_lib.phpc_fill_uniform_dev.restype = ct.c_int
+_lib.phpc_fill_wide_dev.argtypes = [ct.c_void_p, ct.c_size_t, ct.c_uint64, ct.c_uint64, ct.c_int, ct.c_int,
+                                    ct.c_void_p]
+_lib.phpc_fill_wide_dev.restype = ct.c_int
+
+
+class PhpcError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"{what}: status {code} ({error_string(code)})")
+
+
+def lib() -> ct.CDLL:
+    return _lib
+
+
+def error_string(code: int) -> str:
+    return _lib.phpc_error_string(code).decode()
+
+
+def _check(code: int, what: str) -> None:
+    if code != 0:
+        raise PhpcError(code, what)
+
+
+def _host_ptr(a: np.ndarray):
+    if a.dtype != np.float64:
+        raise TypeError("float64 arrays required")
+    return a.ctypes.data_as(_dp)
+
+
+# ---------------------------------------------------------------- reference API
+def gemm_cuda(a, lda, b, ldb, c, ldc, m, k, n, gpu_count=1, grid_width=1, grid_height=1, block_width=32) -> float:
+    """phpc_gemm_cuda: plain FP64 DMMA GEMM, C += A @ B on host arrays; returns seconds."""
+    t = ct.c_float(0.0)
+    _lib.phpc_gemm_cuda(_host_ptr(a), lda, _host_ptr(b), ldb, _host_ptr(c), ldc, m, k, n, gpu_count, grid_width,
+                        grid_height, block_width, ct.byref(t))
+    _check(_lib.phpc_last_error(), "phpc_gemm_cuda")
+    return t.value
+
+
+def gemm_cublas(a, lda, b, ldb, c, ldc, m, k, n, gpu_count=1, grid_width=0, grid_height=0, block_width=0) -> float:
+    """phpc_gemm_cublas: FP64-accurate Ozaki split GEMM, C += A @ B on host arrays; returns seconds."""
+    t = ct.c_float(0.0)
+    _lib.phpc_gemm_cublas(_host_ptr(a), lda, _host_ptr(b), ldb, _host_ptr(c), ldc, m, k, n, gpu_count, grid_width,
+                          grid_height, block_width, ct.byref(t))
+    _check(_lib.phpc_last_error(), "phpc_gemm_cublas")
+    return t.value
+
+
+def gemm_host(method: str, a: np.ndarray, b: np.ndarray, c: np.ndarray, grid_width=1, grid_height=1,
+              block_width=32) -> float:
+    """C += A @ B for C-contiguous float64 host matrices ('dmma' or 'ozaki')."""
+    m, k = a.shape
+    n = b.shape[1]
+    assert b.shape[0] == k and c.shape == (m, n)
+    for x in (a, b, c):
+        assert x.flags.c_contiguous
+    if method == "dmma":
+        return gemm_cuda(a, k, b, n, c, n, m, k, n, 1, grid_width, grid_height, block_width)
+    if method == "ozaki":
+        return gemm_cublas(a, k, b, n, c, n, m, k, n, 1)
+    raise ValueError(method)
+
+
+# --------------------------------------------------------------- device API
+def _dptr(x) -> int:
+    return int(x.data_ptr()) if hasattr(x, "data_ptr") else int(x)
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    return int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def dgemm_dmma_dev(m, k, n, A, lda, B, ldb, C, ldc, grid_width=1, grid_height=1, kpanel=256, stream=None) -> None:
+    _check(_lib.phpc_dgemm_dmma_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, grid_width, grid_height,
+                                    kpanel, _stream(stream)), "phpc_dgemm_dmma_dev")
+
+
+def ozaki_workspace_bytes(m, k, n, slices) -> int:
+    return int(_lib.phpc_ozaki_workspace_bytes(m, k, n, slices))
+
+
+def default_slices(m, k, n) -> int:
+    return int(_lib.phpc_default_slices(m, k, n))
+
+
+def dgemm_ozaki_dev(m, k, n, A, lda, B, ldb, C, ldc, slices, workspace, workspace_bytes, stream=None) -> None:
+    _check(_lib.phpc_dgemm_ozaki_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, slices,
+                                     _dptr(workspace), workspace_bytes, _stream(stream)), "phpc_dgemm_ozaki_dev")
+
+
+def ozaki_prepare_dev(m, k, n, A, lda, B, ldb, slices, workspace, workspace_bytes, stream=None) -> None:
+    _check(_lib.phpc_ozaki_prepare_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, slices, _dptr(workspace),
+                                       workspace_bytes, _stream(stream)), "phpc_ozaki_prepare_dev")
+
+
+def ozaki_multiply_dev(m, k, n, C, ldc, slices, workspace, workspace_bytes, stream=None) -> None:
+    _check(_lib.phpc_ozaki_multiply_dev(m, k, n, _dptr(C), ldc, slices, _dptr(workspace), workspace_bytes,
+                                        _stream(stream)), "phpc_ozaki_multiply_dev")
+
+
+def dgemm_dd_rows_dev(m, k, n, A, lda, B, ldb, C0, ldc, rows, nrows, R, ldr, stream=None) -> None:
+    """Double-double reference rows R[r] = C0[rows[r]] + A[rows[r]] @ B (device pointers)."""
+    _check(_lib.phpc_dgemm_dd_rows_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, None if C0 is None else _dptr(C0),
+                                       ldc, _dptr(rows), nrows, _dptr(R), ldr, _stream(stream)),
+           "phpc_dgemm_dd_rows_dev")
+
+
+def fill_uniform_dev(x, n, seed, offset=0, stream=None) -> None:
+    _check(_lib.phpc_fill_uniform_dev(_dptr(x), n, seed, offset, _stream(stream)), "phpc_fill_uniform_dev")
+
+
+def fill_wide_dev(x, n, seed, offset=0, emin=-20, emax=20, stream=None) -> None:
+    _check(_lib.phpc_fill_wide_dev(_dptr(x), n, seed, offset, emin, emax, _stream(stream)), "phpc_fill_wide_dev")
+
+
+def device_status() -> int:
+    """Reads and clears the device status word (synchronises the device)."""
+    return int(_lib.phpc_device_status())

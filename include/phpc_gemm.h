@@ -1,0 +1,121 @@
+/*
+ * phpc_gemm.h - C ABI of the GB300 (sm_103a) GEMM library.
+ *
+ * Two groups of entry points:
+ *
+ *  1. The reference-compatible local GEMM, same names, argument order and
+ *     meaning as the HPC-MultiGPU-MatrixMult project (src/phpc_gemm.cuh:4-14):
+ *     host pointers, row-major doubles, leading dimensions in elements,
+ *     C += A * B, synchronous on return, kernel-only time in seconds through
+ *     the last argument, void return. The reference gives no error reporting;
+ *     here the outcome of the last call is available through phpc_last_error().
+ *
+ *  2. Device-pointer entry points used by tests, the benchmark and callers that
+ *     keep matrices resident in HBM. They return a status code (PHPC_OK = 0),
+ *     take a CUDA stream as `void *` (NULL = legacy default stream) and are
+ *     asynchronous with respect to the host. Sizes follow the reference's
+ *     (m, k, n) order: A is m x k, B is k x n, C is m x n.
+ */
+#ifndef PHPC_GEMM_H
+#define PHPC_GEMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define PHPC_OK 0
+#define PHPC_ERR_ARG 1         /* invalid size, pointer or option             */
+#define PHPC_ERR_CUDA 2        /* a CUDA runtime or driver call failed        */
+#define PHPC_ERR_ALIGN 3       /* device pointer / leading dim not 16-B aligned */
+#define PHPC_ERR_TIMEOUT 4     /* a bounded device wait expired (site << 8)    */
+#define PHPC_ERR_NONFINITE 5   /* reserved: non-finite input seen by a scan    */
+#define PHPC_ERR_WORKSPACE 6   /* workspace missing or too small              */
+#define PHPC_ERR_UNSUPPORTED 7 /* no device of compute capability 10.3        */
+#define PHPC_ERR_NOMEM 8       /* device or pinned host allocation failed     */
+
+/* Status of the most recent call made by this host thread (0 = success). */
+int phpc_last_error(void);
+/* Human-readable text for a status code. */
+const char *phpc_error_string(int code);
+
+/* ------------------------------------------- reference-compatible entry points */
+
+/*
+ * Replaces phpc_gemm_cuda (reference src/phpc_gemm.cu:59-156).
+ * C[m x n] += A[m x k] * B[k x n] in plain FP64 on the tensor cores (DMMA).
+ * grid_width x grid_height is the logical SUMMA block decomposition of C that
+ * the persistent CTAs walk; block_width (the reference's thread-block edge,
+ * 1..32) is validated and otherwise only reported. gpu_count is accepted for
+ * signature compatibility; one device (the current one) is used.
+ * *compute_time receives the device time of the GEMM kernel in seconds.
+ */
+void phpc_gemm_cuda(const double *a, int lda, const double *b, int ldb, double *c, int ldc, int m, int k, int n,
+                    int gpu_count, int grid_width, int grid_height, int block_width, float *compute_time);
+
+/*
+ * Replaces phpc_gemm_cublas (reference src/phpc_gemm.cu:158-174), which called
+ * cuBLASXt Dgemm with alpha = beta = 1. Here the same C += A * B is computed
+ * by the FP64-accurate split-precision (Ozaki) GEMM on BF16 tensor cores; the
+ * slice count comes from the tuning table or PHPC_SLICES. Unlike the
+ * reference, *gpu_time receives the real device time (scan + split + GEMM).
+ */
+void phpc_gemm_cublas(const double *a, int lda, const double *b, int ldb, double *c, int ldc, int m, int k, int n,
+                      int gpu_count, int grid_width, int grid_height, int block_width, float *gpu_time);
+
+/* ---------------------------------------------- device-pointer entry points */
+
+/* Plain FP64 DMMA GEMM: C += A * B. Requires 16-byte aligned pointers and even
+ * leading dimensions (TMA). kpanel (multiple of 16, 0 = 256) is the SUMMA
+ * k-panel width; grid_width/grid_height (>= 1) the logical block grid. */
+int phpc_dgemm_dmma_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb, double *dC,
+                        int64_t ldc, int grid_width, int grid_height, int kpanel, void *stream);
+
+/* Bytes of device workspace the Ozaki GEMM needs for these sizes. */
+size_t phpc_ozaki_workspace_bytes(int m, int k, int n, int slices);
+
+/* FP64-accurate Ozaki GEMM: C += A * B computed from `slices` (2..8) balanced
+ * 8-bit digit planes per operand, exact slice products on tcgen05 BF16 tensor
+ * cores, int32 accumulation and one FP64 fold per digit diagonal. */
+int phpc_dgemm_ozaki_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
+                         double *dC, int64_t ldc, int slices, void *workspace, size_t workspace_bytes, void *stream);
+
+/* The two phases of phpc_dgemm_ozaki_dev, for callers that reuse the digit
+ * planes of A and B or time the phases separately:
+ * prepare = exponent scans + digit split of A and B into the workspace;
+ * multiply = slice GEMM + FP64 fold into C (reads only the workspace). */
+int phpc_ozaki_prepare_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
+                           int slices, void *workspace, size_t workspace_bytes, void *stream);
+int phpc_ozaki_multiply_dev(int m, int k, int n, double *dC, int64_t ldc, int slices, const void *workspace,
+                            size_t workspace_bytes, void *stream);
+
+/* Slice count the host entry points use for an m x k x n problem
+ * (PHPC_SLICES, else the autotuner's table, else 7). */
+int phpc_default_slices(int m, int k, int n);
+
+/* ------------------------------------------------------------------ utils */
+
+/* Higher-precision reference for stating errors: R[r][j] = C0[i][j] +
+ * sum_k A[i][k] B[k][j] for i = d_rows[r] (device int array), accumulated in
+ * double-double and rounded once. C0 may be NULL. nrows <= 65535. */
+int phpc_dgemm_dd_rows_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
+                           const double *dC0, int64_t ldc, const int *d_rows, int nrows, double *dR, int64_t ldr,
+                           void *stream);
+
+/* Seeded inputs on the device, bit-identical to phpc_fill_uniform /
+ * phpc_fill_wide of phpc_utils.h. */
+int phpc_fill_uniform_dev(double *dx, size_t n, uint64_t seed, uint64_t offset, void *stream);
+int phpc_fill_wide_dev(double *dx, size_t n, uint64_t seed, uint64_t offset, int emin, int emax, void *stream);
+
+/* Last kernel status of the calling thread's device (reads and clears the
+ * device status word; synchronises the device). */
+int phpc_device_status(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHPC_GEMM_H */

@@ -1,0 +1,140 @@
+"""Host-side logic that needs no GPU: the single-rank MPI layer, the SUMMA
+driver's argument handling, the seeded generators, the known answer, and the
+error properties of the Ozaki digit algorithm (numpy model)."""
+import ctypes as ct
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import ozaki_model
+
+ROOT = Path(__file__).resolve().parent.parent
+PKG = ROOT / "hpc-multigpu-matrixmult_gb300"
+
+
+@pytest.fixture(scope="module")
+def summa_lib(built):
+    L = ct.CDLL(str(PKG / "lib" / "libphpc_summa.so"))
+    ip = ct.POINTER(ct.c_int)
+    L.MPI_Dims_create.argtypes = [ct.c_int, ct.c_int, ip]
+    L.MPI_Cart_create.argtypes = [ct.c_int, ct.c_int, ip, ip, ct.c_int, ip]
+    L.MPI_Bcast.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+    L.MPI_Send.argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+    L.phpc_mix64.argtypes = [ct.c_uint64]
+    L.phpc_mix64.restype = ct.c_uint64
+    L.phpc_fill_uniform.argtypes = [ct.POINTER(ct.c_double), ct.c_size_t, ct.c_uint64, ct.c_uint64]
+    L.phpc_fill_wide.argtypes = [ct.POINTER(ct.c_double), ct.c_size_t, ct.c_uint64, ct.c_uint64, ct.c_int, ct.c_int]
+    L.phpc_kat_index_entry.argtypes = [ct.c_int, ct.c_int, ct.c_int]
+    L.phpc_kat_index_entry.restype = ct.c_double
+    return L
+
+
+def _ints(*v):
+    return (ct.c_int * len(v))(*v)
+
+
+def test_dims_create(summa_lib):
+    for nodes, expect in [(1, (1, 1)), (4, (2, 2)), (6, (3, 2)), (16, (4, 4)), (12, (4, 3)), (7, (7, 1))]:
+        d = _ints(0, 0)
+        assert summa_lib.MPI_Dims_create(nodes, 2, d) == 0
+        assert tuple(d) == expect
+    d = _ints(2, 0)
+    assert summa_lib.MPI_Dims_create(6, 2, d) == 0 and tuple(d) == (2, 3)
+    d = _ints(4, 0)
+    assert summa_lib.MPI_Dims_create(6, 2, d) != 0
+
+
+def test_single_rank_cartesian_and_collectives(summa_lib):
+    comm = ct.c_int(0)
+    assert summa_lib.MPI_Cart_create(1, 2, _ints(1, 1), _ints(1, 1), 0, ct.byref(comm)) == 0
+    assert comm.value > 1
+    # a 2 x 2 grid does not exist in a one-process job
+    bad = ct.c_int(0)
+    assert summa_lib.MPI_Cart_create(1, 2, _ints(2, 2), _ints(1, 1), 0, ct.byref(bad)) != 0
+    buf = (ct.c_double * 4)(1, 2, 3, 4)
+    assert summa_lib.MPI_Bcast(buf, 4, 2, 0, comm.value) == 0  # self-broadcast keeps the data
+    assert list(buf) == [1, 2, 3, 4]
+    assert summa_lib.MPI_Bcast(buf, 4, 2, 1, comm.value) != 0  # root 1 does not exist
+    assert summa_lib.MPI_Send(buf, 4, 2, 1, 0, comm.value) != 0
+
+
+def test_generators_deterministic_and_in_range(summa_lib):
+    n = 100000
+    x = np.empty(n)
+    y = np.empty(n)
+    dp = ct.POINTER(ct.c_double)
+    summa_lib.phpc_fill_uniform(x.ctypes.data_as(dp), n, 7, 0)
+    summa_lib.phpc_fill_uniform(y.ctypes.data_as(dp), n, 7, 0)
+    np.testing.assert_array_equal(x, y)
+    assert x.min() >= -1.0 and x.max() < 1.0 and abs(x.mean()) < 0.01
+    # offsets continue the same stream
+    z = np.empty(10)
+    summa_lib.phpc_fill_uniform(z.ctypes.data_as(dp), 10, 7, 500)
+    np.testing.assert_array_equal(z, x[500:510])
+    w = np.empty(n)
+    summa_lib.phpc_fill_wide(w.ctypes.data_as(dp), n, 9, 0, -20, 20)
+    _, e = np.frexp(w[w != 0])
+    assert e.min() >= -20 - 52 and e.max() <= 20
+    assert len(np.unique(np.clip(e, -20, 20))) == 41
+
+
+def test_index_known_answer(summa_lib):
+    for n in (1, 7, 64, 1024, 16384):
+        for i, j in [(0, 0), (n - 1, n - 1), (n // 3, n // 2)]:
+            s1 = n * (n - 1) // 2
+            s2 = (n - 1) * n * (2 * n - 1) // 6
+            exact = i * n * n * s1 + i * j * n * n + n * s2 + j * s1
+            assert summa_lib.phpc_kat_index_entry(n, i, j) == float(exact)
+
+
+def test_main_out_usage_and_divisibility(built):
+    exe = str(PKG / "bin" / "main.out")
+    r = subprocess.run([exe, "64", "32"], capture_output=True, text=True)
+    assert r.returncode != 0 and "Usage" in r.stderr
+    r = subprocess.run([exe, "64", "33", "1", "1", "x"], capture_output=True, text=True)
+    assert r.returncode != 0 and "tile_width" in r.stderr
+
+
+# ----------------------------------------------------- Ozaki digit algorithm
+@pytest.mark.parametrize("s", [2, 3, 4, 5, 6, 7, 8])
+def test_digit_split_reconstructs_to_grid(s):
+    rng = np.random.default_rng(s)
+    x = rng.uniform(-1, 1, (64, 64)) * np.exp2(rng.integers(-20, 21, (64, 64)))
+    x[3, :] = 0.0
+    e = ozaki_model.exponents(x, axis=1)
+    d = ozaki_model.split(x, e[:, None], s)
+    assert np.abs(d).max() <= 128
+    # sum_p d_p 2^(e + 1 - 8p) reproduces x to the P = 8s - 1 bit grid of its row
+    rec = sum(np.ldexp(d[p], (e[:, None] + 1 - 8 * (p + 1))) for p in range(s))
+    err = np.abs(rec - x) / np.ldexp(1.0, e[:, None].clip(-1000, 1000))
+    assert np.all(err[np.isfinite(err)] <= 2.0 ** -(8 * s - 1) * 0.5 * (1 + 1e-12))
+    assert np.all(d[:, 3, :] == 0)
+
+
+def test_digit_split_exact_for_short_mantissas():
+    # values with <= 8s-1 significant bits below the row maximum are represented exactly
+    rng = np.random.default_rng(1)
+    a = rng.integers(-2**20, 2**20, (32, 32)).astype(np.float64)
+    e = ozaki_model.exponents(a, axis=1)
+    d = ozaki_model.split(a, e[:, None], 3)
+    rec = sum(np.ldexp(d[p], (e[:, None] + 1 - 8 * (p + 1))) for p in range(3))
+    np.testing.assert_array_equal(rec, a)
+
+
+@pytest.mark.parametrize("dist,s,bound", [("uniform", 6, 2e-14), ("uniform", 7, 1e-16), ("wide", 7, 1e-15),
+                                          ("wide", 6, 3e-13), ("uniform", 4, 1e-9)])
+def test_model_error_vs_dd_oracle(oracle, dist, s, bound):
+    rng = np.random.default_rng(11)
+    n = 256
+    if dist == "uniform":
+        a = rng.uniform(-1, 1, (n, n))
+        b = rng.uniform(-1, 1, (n, n))
+    else:
+        a = rng.uniform(-1, 1, (n, n)) * np.exp2(rng.integers(-20, 21, (n, n)))
+        b = rng.uniform(-1, 1, (n, n)) * np.exp2(rng.integers(-20, 21, (n, n)))
+    c = ozaki_model.gemm(a, b, None, s)
+    ref = oracle.gemm_dd(a, b)
+    err = oracle.rel_errors(c, ref)
+    assert err["frob"] <= bound, err
