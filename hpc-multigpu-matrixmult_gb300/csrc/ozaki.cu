@@ -25,6 +25,7 @@
 // ~2000x below its BF16 tensor rate.
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 
 #include <cuda_bf16.h>
 
@@ -402,6 +403,77 @@ extern "C" int phpc_dgemm_ozaki_dev(int m, int k, int n, const double* dA, int64
   } else {
     rc = dgemm_ozaki(m, k, n, dA, lda, dB, ldb, dC, ldc, slices, workspace, workspace_bytes,
                      static_cast<cudaStream_t>(stream), default_bn(m, k, n));
+  }
+  set_last_error(rc);
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Ozaki GEMM for callers that cannot allocate device memory.
+//
+// Some callers must not call cudaMalloc (or any allocating routine) while they
+// run a GEMM: a host application whose device memory is entirely owned by its
+// own pool allocator and that forbids allocations outside it, code running
+// under a fixed memory plan near the capacity of the device, or latency-bound
+// loops that cannot afford the device-wide synchronisation cudaMalloc may
+// cause. phpc_dgemm_ozaki_noalloc_dev serves them: the digit planes and the
+// row/column exponents live in the fixed array below instead of a
+// caller-provided or freshly allocated workspace.
+//
+// The array is part of this library's Ozaki module: every GPU on which the
+// module is loaded holds its PHPC_NOALLOC_SCRATCH_BYTES until the process
+// exits. All calls share it; it keeps the previous call's contents, none of
+// which is read before the current call writes it (the column exponents are
+// reset by the call itself). Calls whose work overlaps on the GPU (different
+// streams, or different host threads) race on the array and must be ordered
+// by the caller.
+namespace phpc {
+namespace {
+
+static __device__ __align__(256) uint8_t g_noalloc_scratch[PHPC_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noalloc_ptr[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
+
+// Device address of g_noalloc_scratch on the current device. The name of the
+// array in host code is only a host-side handle, not a device address, so it
+// is resolved once per device with cudaGetSymbolAddress (the set-up done by
+// the first call on each device).
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return PHPC_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PHPC_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return PHPC_OK;
+}
+
+}  // namespace
+}  // namespace phpc
+
+extern "C" int phpc_dgemm_ozaki_noalloc_dev(int m, int k, int n, const double* dA, int64_t lda, const double* dB,
+                                            int64_t ldb, double* dC, int64_t ldc, int slices, void* stream) {
+  using namespace phpc;
+  int rc;
+  if (m < 0 || k < 0 || n < 0 || slices < 2 || slices > 8) {
+    rc = PHPC_ERR_ARG;
+  } else if (m == 0 || n == 0 || k == 0) {
+    rc = PHPC_OK;
+  } else if (!dA || !dB || !dC || lda < k || ldb < n || ldc < n) {
+    rc = PHPC_ERR_ARG;
+  } else if (ozaki_workspace_bytes(m, k, n, slices) > (size_t)PHPC_NOALLOC_SCRATCH_BYTES) {
+    rc = PHPC_ERR_WORKSPACE;  // the problem needs more scratch than the fixed array holds
+  } else {
+    void* ws = nullptr;
+    rc = noalloc_scratch(&ws);
+    if (rc == PHPC_OK)
+      rc = dgemm_ozaki(m, k, n, dA, lda, dB, ldb, dC, ldc, slices, ws, (size_t)PHPC_NOALLOC_SCRATCH_BYTES,
+                       static_cast<cudaStream_t>(stream), default_bn(m, k, n));
   }
   set_last_error(rc);
   return rc;

@@ -92,6 +92,24 @@ int phpc_ozaki_prepare_dev(int m, int k, int n, const double *dA, int64_t lda, c
 int phpc_ozaki_multiply_dev(int m, int k, int n, double *dC, int64_t ldc, int slices, const void *workspace,
                             size_t workspace_bytes, void *stream);
 
+/*
+ * Ozaki GEMM that allocates nothing (no counterpart in the reference).
+ * For callers that must not allocate device memory during the call, e.g. a
+ * host application whose device memory belongs to its own pool allocator, or
+ * code running under a fixed memory plan near the device's capacity. Same
+ * computation as phpc_dgemm_ozaki_dev; the scratch (digit planes, exponents)
+ * is a fixed array of PHPC_NOALLOC_SCRATCH_BYTES inside the library that every
+ * GPU loading the library's Ozaki module holds until the process exits.
+ * Returns PHPC_ERR_WORKSPACE when phpc_ozaki_workspace_bytes(m, k, n, slices)
+ * exceeds that size (e.g. m = n = k = 1024 needs 28 MiB at 7 slices).
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture. All calls share the array:
+ * calls whose GPU work overlaps race and must be ordered by the caller.
+ */
+#define PHPC_NOALLOC_SCRATCH_BYTES (64u << 20)
+int phpc_dgemm_ozaki_noalloc_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
+                                 double *dC, int64_t ldc, int slices, void *stream);
+
 /* Slice count the host entry points use for an m x k x n problem
  * (PHPC_SLICES, else the autotuner's table, else 7). */
 int phpc_default_slices(int m, int k, int n);
