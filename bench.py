@@ -46,6 +46,11 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "hpc-multigpu-matrixmult_gb300"))
 
 METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel err≤1e-14"
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
+# dominant kernel, from a one-pass ncu capture of this workload
+# (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by (N, slices).
+NCU_TRAFFIC_BYTES = {(16384, 7): 501.57e9 + 15.98e9}
 UNIT = "TFLOP/s"
 
 
@@ -293,7 +298,8 @@ def run_ours(args, world, rank, local):
         "phase_ms": {"scan_split": round(prep_ms, 3), "slice_gemm": round(gemm_ms, 3)},
         "roofline": {"bound": "tensor", "kernel": "tc_slice_gemm_kernel<256,kOzaki>",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "TFLOP/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get((n, s)),
+                     "traffic_unit": "DRAM bytes per launch (ncu)",
                      "peak_source": peak_src,
                      "work_per_launch": f"{ozaki_pairs(s)} slice pairs x 2 N^3 = {ozaki_pairs(s) * flops:.4e} bf16 flop"},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * n * n * 8,

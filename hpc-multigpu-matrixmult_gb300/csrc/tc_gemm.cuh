@@ -11,8 +11,12 @@
 //          per-thread int32 registers. At the end of a group (or after 127
 //          chunks, before int32 could overflow) it folds the integer sums into
 //          the FP64 output: C[i][j] += S * 2^(ea[i] + eb[j] + 2 - 8g).
-//  kF32    One f32 accumulation over all pairs and K (3xBF16 split GEMM);
-//          at the end of the tile C[i][j] += acc (float).
+//  kF32    3xBF16 split GEMM: all pairs accumulate into one f32 result. The
+//          tensor cores' f32 accumulation does not round to nearest, so its
+//          error grows with the number of MMAs summed; the accumulator is
+//          therefore flushed every 8 K-steps of 64 (512 products per output)
+//          into per-thread f32 registers with round-to-nearest adds, and at
+//          the end of the tile C[i][j] += acc (float).
 //
 // Warp roles (320 threads): warp 0 = TMA producer, warp 1 = TMEM allocator and
 // single-thread MMA issuer, warps 2..9 = epilogue. Epilogue warp w reads TMEM
@@ -30,6 +34,7 @@ constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;              // bf16 elements of K per stage (one 128-byte swizzle row)
 constexpr int kTcMaxPairs = 64;
 constexpr int kTcChunkSteps = 16;      // 16 x 64 = 1024 products per exact f32 chunk
+constexpr int kTcF32ChunkSteps = 8;    // kF32: flush to round-to-nearest registers every 512 products
 constexpr int kTcFoldChunks = 127;     // 127 chunks of |v| <= 2^24 keep |int32 sum| < 2^31
 constexpr int kTcEpiWarps = 8;
 constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
@@ -176,7 +181,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           else
             gend = pairs.n;
           const int total = (gend - gstart) * nk;
-          const int chunk = MODE == kOzaki ? kTcChunkSteps : total;
+          const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
             const int len = min(chunk, total - done);
             if (!wait_parity(&tempty[buf], tphase[buf] ^ 1, status, 12)) { ok = false; break; }
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint32_t tphase[2] = {0, 0};
     int buf = 0;
     bool ok = true;
-    int32_t acc[HALF];  // kOzaki: exact int32 sums; kF32: raw f32 bits of the accumulator
+    int32_t acc[HALF];  // kOzaki: exact int32 sums; kF32: bits of the f32 running sums
 #pragma unroll
     for (int j = 0; j < HALF; ++j) acc[j] = 0;
 
@@ -240,7 +245,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         else
           gend = pairs.n;
         const int total = (gend - gstart) * nk;
-        const int chunk = MODE == kOzaki ? kTcChunkSteps : total;
+        const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
         const int nchunks = (total + chunk - 1) / chunk;
         for (int c = 0; c < nchunks && ok; ++c) {
           // all lanes must agree before the warp-collective tcgen05.ld below
@@ -264,7 +269,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               tmem_ld_32x32b_x32(taddr + cb, r);
               tc_wait_ld();
 #pragma unroll
-              for (int j = 0; j < 32; ++j) acc[cb + j] = (int32_t)r[j];  // raw f32 bits
+              for (int j = 0; j < 32; ++j)
+                acc[cb + j] = __float_as_int(__int_as_float(acc[cb + j]) + __uint_as_float(r[j]));
             }
           }
           tc_fence_before();

@@ -66,6 +66,14 @@ _lib.phpc_fill_uniform_dev.restype = ct.c_int
 _lib.phpc_fill_wide_dev.argtypes = [ct.c_void_p, ct.c_size_t, ct.c_uint64, ct.c_uint64, ct.c_int, ct.c_int,
                                     ct.c_void_p]
 _lib.phpc_fill_wide_dev.restype = ct.c_int
+_lib.phpc_bf16x3_workspace_bytes.argtypes = [ct.c_int, ct.c_int, ct.c_int]
+_lib.phpc_bf16x3_workspace_bytes.restype = ct.c_size_t
+_lib.phpc_sgemm_bf16x3_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p,
+                                       ct.c_int64, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_sgemm_bf16x3_dev.restype = ct.c_int
+_lib.phpc_sgemm_ffma_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_int64,
+                                     ct.c_void_p, ct.c_int64, ct.c_void_p]
+_lib.phpc_sgemm_ffma_dev.restype = ct.c_int
 
 
 class PhpcError(RuntimeError):
@@ -179,6 +187,22 @@ def fill_uniform_dev(x, n, seed, offset=0, stream=None) -> None:
 
 def fill_wide_dev(x, n, seed, offset=0, emin=-20, emax=20, stream=None) -> None:
     _check(_lib.phpc_fill_wide_dev(_dptr(x), n, seed, offset, emin, emax, _stream(stream)), "phpc_fill_wide_dev")
+
+
+def bf16x3_workspace_bytes(m, k, n) -> int:
+    return int(_lib.phpc_bf16x3_workspace_bytes(m, k, n))
+
+
+def sgemm_bf16x3_dev(m, k, n, A, lda, B, ldb, C, ldc, workspace, workspace_bytes, stream=None) -> None:
+    """FP32-accurate C += A @ B (float32 device matrices) from 3 BF16 slices per operand."""
+    _check(_lib.phpc_sgemm_bf16x3_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, _dptr(workspace),
+                                      workspace_bytes, _stream(stream)), "phpc_sgemm_bf16x3_dev")
+
+
+def sgemm_ffma_dev(m, k, n, A, lda, B, ldb, C, ldc, stream=None) -> None:
+    """Plain FP32 C += A @ B on the CUDA cores."""
+    _check(_lib.phpc_sgemm_ffma_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, _stream(stream)),
+           "phpc_sgemm_ffma_dev")
 
 
 def device_status() -> int:

@@ -110,6 +110,18 @@ int phpc_ozaki_multiply_dev(int m, int k, int n, double *dC, int64_t ldc, int sl
 int phpc_dgemm_ozaki_noalloc_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
                                  double *dC, int64_t ldc, int slices, void *stream);
 
+/* FP32-accurate GEMM from three BF16 slices per operand (six slice products,
+ * tcgen05 BF16 tensor cores, f32 accumulation): C += A * B on row-major FP32
+ * device matrices. Finite inputs only. Workspace: phpc_bf16x3_workspace_bytes. */
+size_t phpc_bf16x3_workspace_bytes(int m, int k, int n);
+int phpc_sgemm_bf16x3_dev(int m, int k, int n, const float *dA, int64_t lda, const float *dB, int64_t ldb, float *dC,
+                          int64_t ldc, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Plain FP32 GEMM on the CUDA cores (FFMA), C += A * B: the baseline of the
+ * 3xBF16 path. */
+int phpc_sgemm_ffma_dev(int m, int k, int n, const float *dA, int64_t lda, const float *dB, int64_t ldb, float *dC,
+                        int64_t ldc, void *stream);
+
 /* Slice count the host entry points use for an m x k x n problem
  * (PHPC_SLICES, else the autotuner's table, else 7). */
 int phpc_default_slices(int m, int k, int n);
