@@ -1,0 +1,384 @@
+// Grouped FP64-accurate GEMM: many independent C_i += A_i * B_i of uneven
+// sizes in one persistent launch per phase, replayable as one CUDA graph.
+//
+// The reference runs one GEMM per call (src/phpc_gemm.cu:59-156), one kernel
+// per panel (src/phpc_summa.c:93); a batch of small GEMMs there is a batch of
+// launches that each leave most of the GPU idle. Here a plan describes the
+// whole batch once:
+//  - a device table with one record per problem and the prefix sums of its
+//    rows, columns, split blocks and output tiles, plus two TMA descriptors
+//    per problem (A digit planes, B digit planes), written into the head of
+//    the caller's workspace;
+//  - five launches cover the batch: exponent scans of all rows, of all
+//    columns, digit splits of all rows, of all column blocks, and the
+//    persistent tcgen05 slice GEMM over the union of all output tiles
+//    (tc_gemm.cuh, grouped mode: a tile finds its problem by binary search);
+//  - phpc_grouped_graph_launch captures those five launches once into a CUDA
+//    graph and replays it.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "ozaki_digits.cuh"
+#include "phpc_host.hpp"
+#include "tc_gemm.cuh"
+
+namespace phpc {
+namespace {
+
+// Split-phase record of one problem (device copy in the workspace).
+struct GSplitProb {
+  int m, k, n;
+  int row_start, col_start, sblock_start;  // prefix sums over the problems
+  int nblk_j;                              // 64-column blocks of B
+  int64_t lda, ldb, ldp;
+  const double* A;
+  const double* B;
+  int* ea;
+  int* eb;
+  uint16_t* pa;
+  uint16_t* pb;
+};
+
+// Last problem p with start(p) <= x, over a field of the records.
+template <typename F>
+__device__ __forceinline__ int locate(const GSplitProb* P, int count, int x, F start) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start(P[mid]) <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void g_scan_rows_kernel(const GSplitProb* __restrict__ P, int count, int total_rows, int* status) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= total_rows) return;
+  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
+  const int64_t row = r - p.row_start;
+  scan_row_warp(p.A + row * p.lda, p.k, p.ea + row, status);
+}
+
+// One thread per column over the whole K of its problem (no atomics).
+__global__ void g_scan_cols_kernel(const GSplitProb* __restrict__ P, int count, int total_cols, int* status) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= total_cols) return;
+  const GSplitProb& p = P[locate(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
+  const int64_t col = c - p.col_start;
+  int e = kExpZero;
+  bool nf = false;
+  for (int k = 0; k < p.k; ++k) e = max(e, exponent_of(p.B[(int64_t)k * p.ldb + col], nf));
+  p.eb[col] = e;
+  if (nf) record_error(status, PHPC_ERR_NONFINITE);
+}
+
+__global__ void g_split_rows_kernel(const GSplitProb* __restrict__ P, int count, int total_rows, int s) {
+  const int r = blockIdx.x;
+  if (r >= total_rows) return;
+  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
+  const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
+  if (k0 >= p.ldp) return;
+  const int64_t row = r - p.row_start;
+  split_row_piece(p.A + row * p.lda, p.k, p.ea[row], s, p.pa + row * p.ldp, (int64_t)p.m * p.ldp, k0);
+}
+
+__global__ void __launch_bounds__(256) g_split_cols_kernel(const GSplitProb* __restrict__ P, int count,
+                                                           int total_blocks, int s) {
+  __shared__ uint32_t st[8][64][17];
+  const int b = blockIdx.x;
+  if (b >= total_blocks) return;  // uniform over the CTA
+  const GSplitProb& p = P[locate(P, count, b, [](const GSplitProb& q) { return q.sblock_start; })];
+  const int lb = b - p.sblock_start;
+  const int64_t j0 = (int64_t)(lb % p.nblk_j) * 64, k0 = (int64_t)(lb / p.nblk_j) * 32;
+  split_col_block(p.B, p.ldb, p.k, p.n, p.eb, s, p.pb, p.ldp, (int64_t)p.n * p.ldp, k0, j0, st);
+}
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct ProbLayout {
+  int64_t ldp;
+  size_t ea, eb, pa, pb, end;  // offsets relative to the problem's base
+};
+
+ProbLayout prob_layout(const phpc_gemm_problem& q, int s) {
+  ProbLayout L;
+  L.ldp = ((int64_t)q.k + 7) / 8 * 8;
+  L.ea = 0;
+  L.eb = align_up(sizeof(int) * (size_t)q.m, 256);
+  L.pa = align_up(L.eb + sizeof(int) * (size_t)q.n, 256);
+  L.pb = align_up(L.pa + (size_t)s * q.m * L.ldp * 2, 256);
+  L.end = align_up(L.pb + (size_t)s * q.n * L.ldp * 2, 256);
+  return L;
+}
+
+struct TableLayout {
+  size_t split, tprob, maps, end;
+};
+
+TableLayout table_layout(int count) {
+  TableLayout T;
+  T.split = 0;
+  T.tprob = align_up(sizeof(GSplitProb) * (size_t)count, 256);
+  T.maps = align_up(T.tprob + sizeof(TcGroupProblem) * (size_t)count, 256);
+  T.end = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
+  return T;
+}
+
+bool valid_problem(const phpc_gemm_problem& q) {
+  return q.m > 0 && q.k > 0 && q.n > 0 && q.A && q.B && q.C && q.lda >= q.k && q.ldb >= q.n && q.ldc >= q.n;
+}
+
+PairList grouped_pairs(int s) {
+  PairList pl{};
+  for (int g = 2; g <= s + 1; ++g)
+    for (int p = 1; p < g; ++p) {
+      const int q = g - p;
+      if (p > s || q > s) continue;
+      pl.a[pl.n] = static_cast<uint8_t>(p - 1);
+      pl.b[pl.n] = static_cast<uint8_t>(q - 1);
+      pl.g[pl.n] = static_cast<uint8_t>(g);
+      ++pl.n;
+    }
+  return pl;
+}
+
+}  // namespace
+}  // namespace phpc
+
+struct phpc_grouped_plan {
+  int device;
+  int count, s, bn;
+  int total_rows, total_cols, total_sblocks, total_tiles, max_kgroups;
+  phpc::GSplitProb* d_split;
+  phpc::TcGroupTable table;
+  phpc::PairList pairs;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+};
+
+namespace phpc {
+namespace {
+
+template <int BN>
+int launch_grouped_gemm(const phpc_grouped_plan* pl, cudaStream_t stream) {
+  using Cfg = TcCfg<BN>;
+  const DeviceInfo* dev = current_device();
+  if (!dev) return PHPC_ERR_CUDA;
+  TcArgs a{};
+  a.status = device_status_ptr();
+  CUtensorMap dummy;
+  std::memset(&dummy, 0, sizeof dummy);
+  const int grid = std::min(pl->total_tiles, dev->sm_count);
+  tc_slice_gemm_kernel<BN, kOzaki, true><<<grid, kTcThreads, Cfg::kSmem, stream>>>(dummy, dummy, pl->pairs, a,
+                                                                                   pl->table);
+  return cudaGetLastError() == cudaSuccess ? PHPC_OK : PHPC_ERR_CUDA;
+}
+
+template <int BN>
+int prepare_grouped_gemm() {
+  using Cfg = TcCfg<BN>;
+  auto kern = tc_slice_gemm_kernel<BN, kOzaki, true>;
+  if (!tc_regs_ok(reinterpret_cast<const void*>(kern))) return PHPC_ERR_UNSUPPORTED;
+  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
+  return PHPC_OK;
+}
+
+int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
+  int* status = device_status_ptr();
+  if (pl->total_rows > 0) {
+    g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
+                                                                        status);
+    g_scan_cols_kernel<<<ceil_div(pl->total_cols, 128), 128, 0, stream>>>(pl->d_split, pl->count, pl->total_cols,
+                                                                          status);
+    g_split_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                                   pl->total_rows, pl->s);
+    g_split_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks, pl->s);
+    if (cudaGetLastError() != cudaSuccess) return PHPC_ERR_CUDA;
+  }
+  if (pl->total_tiles == 0) return PHPC_OK;
+  return pl->bn == 128 ? launch_grouped_gemm<128>(pl, stream) : launch_grouped_gemm<256>(pl, stream);
+}
+
+}  // namespace
+}  // namespace phpc
+
+extern "C" size_t phpc_grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int slices) {
+  using namespace phpc;
+  if (!problems || count <= 0 || slices < 2 || slices > 8) return 0;
+  size_t total = table_layout(count).end;
+  for (int i = 0; i < count; ++i) {
+    if (!valid_problem(problems[i])) return 0;
+    total += prob_layout(problems[i], slices).end;
+  }
+  return total;
+}
+
+extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* problems, int count,
+                                        int slices, void* workspace, size_t workspace_bytes, void* stream) {
+  using namespace phpc;
+  int rc = PHPC_OK;
+  if (out) *out = nullptr;
+  if (!out || !problems || count <= 0 || count > (1 << 20) || slices < 2 || slices > 8) {
+    set_last_error(PHPC_ERR_ARG);
+    return PHPC_ERR_ARG;
+  }
+  for (int i = 0; i < count; ++i)
+    if (!valid_problem(problems[i])) {
+      set_last_error(PHPC_ERR_ARG);
+      return PHPC_ERR_ARG;
+    }
+  const DeviceInfo* dev = current_device();
+  if (!dev) rc = PHPC_ERR_CUDA;
+  else if (dev->cc_major != 10 || dev->cc_minor != 3) rc = PHPC_ERR_UNSUPPORTED;
+  const size_t need = phpc_grouped_workspace_bytes(problems, count, slices);
+  if (rc == PHPC_OK && (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255)))
+    rc = PHPC_ERR_WORKSPACE;
+  if (rc != PHPC_OK) {
+    set_last_error(rc);
+    return rc;
+  }
+
+  phpc_grouped_plan* pl = new phpc_grouped_plan();
+  pl->device = dev->ordinal;
+  pl->count = count;
+  pl->s = slices;
+  pl->bn = default_grouped_bn(problems, count);
+  pl->pairs = grouped_pairs(slices);
+
+  const TableLayout T = table_layout(count);
+  uint8_t* base = static_cast<uint8_t*>(workspace);
+  std::vector<GSplitProb> hs(count);
+  std::vector<TcGroupProblem> ht(count);
+  std::vector<CUtensorMap> hm(2 * (size_t)count);
+  size_t off = T.end;
+  int rows = 0, cols = 0, sblocks = 0, tiles = 0, maxkg = 1;
+  for (int i = 0; i < count && rc == PHPC_OK; ++i) {
+    const phpc_gemm_problem& q = problems[i];
+    const ProbLayout L = prob_layout(q, slices);
+    uint8_t* pb = base + off;
+    GSplitProb& g = hs[i];
+    g.m = q.m;
+    g.k = q.k;
+    g.n = q.n;
+    g.row_start = rows;
+    g.col_start = cols;
+    g.sblock_start = sblocks;
+    g.nblk_j = ceil_div(q.n, 64);
+    g.lda = q.lda;
+    g.ldb = q.ldb;
+    g.ldp = L.ldp;
+    g.A = q.A;
+    g.B = q.B;
+    g.ea = reinterpret_cast<int*>(pb + L.ea);
+    g.eb = reinterpret_cast<int*>(pb + L.eb);
+    g.pa = reinterpret_cast<uint16_t*>(pb + L.pa);
+    g.pb = reinterpret_cast<uint16_t*>(pb + L.pb);
+    rows += q.m;
+    cols += q.n;
+    sblocks += g.nblk_j * ceil_div(q.k, 32);
+    maxkg = std::max(maxkg, ceil_div(L.ldp / 8, 128));
+
+    TcGroupProblem& t = ht[i];
+    t.M = q.m;
+    t.N = q.n;
+    t.K = q.k;
+    t.tm = ceil_div(q.m, kTcBM);
+    t.tn = ceil_div(q.n, pl->bn);
+    t.tile_start = tiles;
+    t.C = q.C;
+    t.ldc = q.ldc;
+    t.ea = g.ea;
+    t.eb = g.eb;
+    tiles += t.tm * t.tn;
+
+    const uint64_t dA[3] = {(uint64_t)q.k, (uint64_t)q.m, (uint64_t)slices};
+    const uint64_t sA[2] = {(uint64_t)L.ldp * 2, (uint64_t)L.ldp * 2 * q.m};
+    const uint32_t bA[3] = {kTcBK, kTcBM, 1};
+    const uint64_t dB[3] = {(uint64_t)q.k, (uint64_t)q.n, (uint64_t)slices};
+    const uint64_t sB[2] = {(uint64_t)L.ldp * 2, (uint64_t)L.ldp * 2 * q.n};
+    const uint32_t bB[3] = {kTcBK, (uint32_t)pl->bn, 1};
+    if (!encode_tiled(&hm[2 * i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, g.pa, dA, sA, bA, CU_TENSOR_MAP_SWIZZLE_128B) ||
+        !encode_tiled(&hm[2 * i + 1], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, g.pb, dB, sB, bB,
+                      CU_TENSOR_MAP_SWIZZLE_128B))
+      rc = PHPC_ERR_CUDA;
+    off += L.end;
+  }
+  pl->total_rows = rows;
+  pl->total_cols = cols;
+  pl->total_sblocks = sblocks;
+  pl->total_tiles = tiles;
+  pl->max_kgroups = maxkg;
+  pl->d_split = reinterpret_cast<GSplitProb*>(base + T.split);
+  pl->table.count = count;
+  pl->table.ntiles = tiles;
+  pl->table.group_rows = 8;
+  pl->table.probs = reinterpret_cast<const TcGroupProblem*>(base + T.tprob);
+  pl->table.maps = reinterpret_cast<const CUtensorMap*>(base + T.maps);
+  if (rc == PHPC_OK) rc = pl->bn == 128 ? prepare_grouped_gemm<128>() : prepare_grouped_gemm<256>();
+  if (rc == PHPC_OK && !device_status_ptr()) rc = PHPC_ERR_CUDA;  // resolved now, not during a graph capture
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (rc == PHPC_OK &&
+      (cudaMemcpyAsync(base + T.split, hs.data(), sizeof(GSplitProb) * count, cudaMemcpyHostToDevice, st) !=
+           cudaSuccess ||
+       cudaMemcpyAsync(base + T.tprob, ht.data(), sizeof(TcGroupProblem) * count, cudaMemcpyHostToDevice, st) !=
+           cudaSuccess ||
+       cudaMemcpyAsync(base + T.maps, hm.data(), sizeof(CUtensorMap) * 2 * count, cudaMemcpyHostToDevice, st) !=
+           cudaSuccess ||
+       cudaStreamSynchronize(st) != cudaSuccess))
+    rc = PHPC_ERR_CUDA;
+  if (rc != PHPC_OK) {
+    delete pl;
+    set_last_error(rc);
+    return rc;
+  }
+  *out = pl;
+  set_last_error(PHPC_OK);
+  return PHPC_OK;
+}
+
+extern "C" int phpc_grouped_run(const phpc_grouped_plan* plan, void* stream) {
+  int rc = plan ? phpc::run_grouped(plan, static_cast<cudaStream_t>(stream)) : PHPC_ERR_ARG;
+  phpc::set_last_error(rc);
+  return rc;
+}
+
+extern "C" int phpc_grouped_graph_launch(phpc_grouped_plan* plan, void* stream) {
+  using namespace phpc;
+  int rc = PHPC_OK;
+  if (!plan) {
+    rc = PHPC_ERR_ARG;
+  } else {
+    if (!plan->exec) {
+      cudaStream_t cs = nullptr;
+      if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
+      if (rc == PHPC_OK && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        rc = PHPC_ERR_CUDA;
+      if (rc == PHPC_OK) {
+        const int run_rc = run_grouped(plan, cs);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(cs, &g);
+        if (run_rc != PHPC_OK) rc = run_rc;
+        else if (e != cudaSuccess) rc = PHPC_ERR_CUDA;
+        if (rc == PHPC_OK && cudaGraphInstantiate(&plan->exec, g, 0) != cudaSuccess) rc = PHPC_ERR_CUDA;
+        if (rc == PHPC_OK) plan->graph = g;
+        else if (g) cudaGraphDestroy(g);
+      }
+      if (cs) cudaStreamDestroy(cs);
+      cudaGetLastError();
+    }
+    if (rc == PHPC_OK && cudaGraphLaunch(plan->exec, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+      rc = PHPC_ERR_CUDA;
+  }
+  set_last_error(rc);
+  return rc;
+}
+
+extern "C" void phpc_grouped_plan_destroy(phpc_grouped_plan* plan) {
+  if (!plan) return;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  delete plan;
+}

@@ -52,6 +52,7 @@ int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double
 size_t ozaki_workspace_bytes(int m, int k, int n, int s);
 int default_slices(int m, int k, int n);
 int default_bn(int m, int k, int n);
+int default_grouped_bn(const phpc_gemm_problem* problems, int count);
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 

@@ -18,11 +18,16 @@
 //          into per-thread f32 registers with round-to-nearest adds, and at
 //          the end of the tile C[i][j] += acc (float).
 //
-// Warp roles (320 threads): warp 0 = TMA producer, warp 1 = TMEM allocator and
-// single-thread MMA issuer, warps 2..9 = epilogue. Epilogue warp w reads TMEM
-// lanes 32*(w%4) .. +31 (the lane quadrant tcgen05.ld allows it) and column
-// half (w-2)/4 of the BN-wide accumulator. Two TMEM accumulator buffers let
-// the MMA of chunk c+1 overlap the epilogue of chunk c.
+// Warp roles (384 threads, three warpgroups): warp 0 = TMA producer, warp 1 =
+// TMEM allocator and single-thread MMA issuer, warps 2-3 idle; warps 4..11 =
+// epilogue. Epilogue warp w reads TMEM lanes 32*(w%4) .. +31 (the lane
+// quadrant tcgen05.ld allows it) and column half (w-4)/4 of the BN-wide
+// accumulator. Two TMEM accumulator buffers let the MMA of chunk c+1 overlap
+// the epilogue of chunk c. The kernel is compiled for 168 registers per
+// thread; the first warpgroup gives registers back (setmaxnreg.dec to 40) and
+// the two epilogue warpgroups take them (setmaxnreg.inc to 232):
+// 128 x 40 + 256 x 232 = 384 x 168. The host launches the kernel only after
+// checking that its compiled register count is 168 (tc_regs_ok).
 #pragma once
 #include "phpc_dev.cuh"
 
@@ -37,7 +42,12 @@ constexpr int kTcChunkSteps = 16;      // 16 x 64 = 1024 products per exact f32 
 constexpr int kTcF32ChunkSteps = 8;    // kF32: flush to round-to-nearest registers every 512 products
 constexpr int kTcFoldChunks = 127;     // 127 chunks of |v| <= 2^24 keep |int32 sum| < 2^31
 constexpr int kTcEpiWarps = 8;
-constexpr int kTcThreads = (2 + kTcEpiWarps) * 32;
+constexpr int kTcFirstEpiWarp = 4;
+constexpr int kTcThreads = (kTcFirstEpiWarp + kTcEpiWarps) * 32;
+constexpr int kTcLaunchRegs = 168;   // per-thread registers the kernel must be compiled with
+constexpr int kTcRegsLow = 40;       // warpgroup 0 after setmaxnreg.dec
+constexpr int kTcRegsHigh = 232;     // epilogue warpgroups after setmaxnreg.inc
+static_assert(128 * kTcRegsLow + 256 * kTcRegsHigh <= kTcThreads * kTcLaunchRegs, "register split exceeds the pool");
 
 struct PairList {
   int n;                      // number of (A plane, B plane) pairs
@@ -57,6 +67,39 @@ struct TcArgs {
   int* status;
 };
 
+// Grouped mode: many independent problems in one persistent launch. The
+// host writes this table (and two tensor maps per problem: A planes, B planes)
+// into device memory; a global tile index is mapped to its problem by binary
+// search over tile_start.
+struct TcGroupProblem {
+  int M, N, K;
+  int tm, tn;
+  int tile_start;             // first global tile index of this problem
+  void* C;
+  int64_t ldc;
+  const int* ea;
+  const int* eb;
+};
+
+struct TcGroupTable {
+  int count;
+  int ntiles;
+  int group_rows;
+  const TcGroupProblem* probs;  // [count]
+  const CUtensorMap* maps;      // [2 * count], 64-byte aligned
+};
+
+// What one output tile needs: its problem's sizes, operands and position.
+struct TcJob {
+  int M, N, nk, rm, rn;
+  const CUtensorMap* tmA;
+  const CUtensorMap* tmB;
+  void* C;
+  int64_t ldc;
+  const int* ea;
+  const int* eb;
+};
+
 template <int BN>
 struct TcCfg {
   static constexpr int kStages = BN == 256 ? 4 : 6;
@@ -69,14 +112,50 @@ struct TcCfg {
       (size_t)kStages * kStageBytes + kTcEpiWarps * kScratchPerWarp + 256 /*barriers*/ + 1024 /*align*/;
 };
 
-__device__ __forceinline__ void tc_tile_coords(const TcArgs& a, int t, int& rm, int& rn) {
-  const int per_group = a.group_rows * a.tn;
+// Tile t of a tm x tn tile grid in L2 raster order: groups of group_rows tile
+// rows, column-major inside a group, so consecutive tiles share a B panel.
+__device__ __forceinline__ void tc_tile_coords(int tm, int tn, int group_rows, int t, int& rm, int& rn) {
+  const int per_group = group_rows * tn;
   const int grp = t / per_group;
-  const int r0 = grp * a.group_rows;
-  const int rows = min(a.group_rows, a.tm - r0);
+  const int r0 = grp * group_rows;
+  const int rows = min(group_rows, tm - r0);
   const int w = t - grp * per_group;
   rn = w / rows;
   rm = r0 + w % rows;
+}
+
+template <bool GROUPED>
+__device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap* tmA, const CUtensorMap* tmB,
+                                       const TcGroupTable& g, TcJob& j) {
+  if (!GROUPED) {
+    j.M = a.M;
+    j.N = a.N;
+    j.nk = (a.K + kTcBK - 1) / kTcBK;
+    tc_tile_coords(a.tm, a.tn, a.group_rows, t, j.rm, j.rn);
+    j.tmA = tmA;
+    j.tmB = tmB;
+    j.C = a.C;
+    j.ldc = a.ldc;
+    j.ea = a.ea;
+    j.eb = a.eb;
+  } else {
+    int lo = 0, hi = g.count - 1;
+    while (lo < hi) {  // last problem with tile_start <= t
+      const int mid = (lo + hi + 1) >> 1;
+      if (g.probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
+    }
+    const TcGroupProblem& p = g.probs[lo];
+    j.M = p.M;
+    j.N = p.N;
+    j.nk = (p.K + kTcBK - 1) / kTcBK;
+    tc_tile_coords(p.tm, p.tn, g.group_rows, t - p.tile_start, j.rm, j.rn);
+    j.tmA = g.maps + 2 * lo;
+    j.tmB = g.maps + 2 * lo + 1;
+    j.C = p.C;
+    j.ldc = p.ldc;
+    j.ea = p.ea;
+    j.eb = p.eb;
+  }
 }
 
 // 2^x as a double for any int x (0 below the subnormal range, inf above).
@@ -87,10 +166,11 @@ __device__ __forceinline__ double fold_term(int32_t s, int x) {
   return ldexp(v, x);
 }
 
-template <int BN, int MODE>
+template <int BN, int MODE, bool GROUPED = false>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                         const __grid_constant__ PairList pairs, const __grid_constant__ TcArgs args) {
+                         const __grid_constant__ PairList pairs, const __grid_constant__ TcArgs args,
+                         const __grid_constant__ TcGroupTable gt) {
   using Cfg = TcCfg<BN>;
   constexpr int S = Cfg::kStages;
   constexpr int HALF = BN / 2;
@@ -105,8 +185,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = args.tm * args.tn;
-  const int nk = (args.K + kTcBK - 1) / kTcBK;
+  const int ntiles = GROUPED ? gt.ntiles : args.tm * args.tn;
   int* status = args.status;
 
   if (threadIdx.x == 0) {
@@ -126,27 +205,32 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
-
+  // Each role's code is dominated by its own setmaxnreg, so the compiler can
+  // allocate up to kTcRegsHigh registers in the epilogue branch.
+  if (warp < kTcFirstEpiWarp) {
+  asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kTcRegsLow));
   if (warp == 0) {
     // ------------------------------------------------------------------ TMA
     if (lane == 0) {
-      tma_prefetch_desc(&tmA);
-      tma_prefetch_desc(&tmB);
+      if (!GROUPED) {
+        tma_prefetch_desc(&tmA);
+        tma_prefetch_desc(&tmB);
+      }
       int stage = 0;
       uint32_t phase = 0;
       int issued = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        int rm, rn;
-        tc_tile_coords(args, t, rm, rn);
+        TcJob j;
+        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, j);
         for (int pi = 0; pi < pairs.n && ok; ++pi) {
           const int pa = pairs.a[pi], pb = pairs.b[pi];
-          for (int kb = 0; kb < nk; ++kb) {
+          for (int kb = 0; kb < j.nk; ++kb) {
             if (!wait_parity(&empty[stage], phase ^ 1, status, 11)) { ok = false; break; }
             mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
             uint8_t* sa = smem + stage * Cfg::kStageBytes;
-            tma_load_3d(sa, &tmA, kb * kTcBK, rm * kTcBM, pa, &full[stage]);
-            tma_load_3d(sa + Cfg::kStageA, &tmB, kb * kTcBK, rn * BN, pb, &full[stage]);
+            tma_load_3d(sa, j.tmA, kb * kTcBK, j.rm * kTcBM, pa, &full[stage]);
+            tma_load_3d(sa + Cfg::kStageA, j.tmB, kb * kTcBK, j.rn * BN, pb, &full[stage]);
             ++issued;
             if (++stage == S) { stage = 0; phase ^= 1; }
           }
@@ -173,6 +257,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       int buf = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        TcJob j;
+        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, j);
         int gstart = 0;
         while (gstart < pairs.n && ok) {
           int gend = gstart + 1;
@@ -180,7 +266,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
           else
             gend = pairs.n;
-          const int total = (gend - gstart) * nk;
+          const int total = (gend - gstart) * j.nk;
           const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
             const int len = min(chunk, total - done);
@@ -214,9 +300,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(daddr, 0) && globaltimer_ns() - t0 < PHPC_WAIT_LIMIT_NS) {}
     }
+  }
   } else {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kTcRegsHigh));
     // ------------------------------------------------------------- epilogue
-    const int ew = warp - 2;
+    const int ew = warp - kTcFirstEpiWarp;
     const int quad = warp & 3;              // TMEM lane quadrant of this warp
     const int half = ew >> 2;               // column half of the accumulator
     uint32_t* tr = reinterpret_cast<uint32_t*>(scratch + ew * Cfg::kScratchPerWarp);  // [32][33]
@@ -228,14 +316,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int j = 0; j < HALF; ++j) acc[j] = 0;
 
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      int rm, rn;
-      tc_tile_coords(args, t, rm, rn);
-      const int64_t row0 = (int64_t)rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
-      const int col0 = rn * BN + half * HALF;                 // first global column of this warp's half
+      TcJob j;
+      tc_job<GROUPED>(t, args, &tmA, &tmB, gt, j);
+      const int64_t row0 = (int64_t)j.rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
+      const int col0 = j.rn * BN + half * HALF;                 // first global column of this warp's half
       int my_ea = 0;
       if (MODE == kOzaki) {
         const int64_t r = row0 + lane;
-        my_ea = r < args.M ? max(args.ea[r], -20000) : -20000;
+        my_ea = r < j.M ? max(j.ea[r], -20000) : -20000;
       }
       int gstart = 0;
       while (gstart < pairs.n && ok) {
@@ -244,7 +332,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
         else
           gend = pairs.n;
-        const int total = (gend - gstart) * nk;
+        const int total = (gend - gstart) * j.nk;
         const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
         const int nchunks = (total + chunk - 1) / chunk;
         for (int c = 0; c < nchunks && ok; ++c) {
@@ -292,19 +380,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (int j = 0; j < 32; ++j) tr[lane * 33 + j] = (uint32_t)acc[cb + j];
             __syncwarp();
             const int col = col0 + cb + lane;
-            const bool col_ok = col < args.N;
+            const bool col_ok = col < j.N;
             int col_e = 0;
-            if (MODE == kOzaki) col_e = col_ok ? max(args.eb[col], -20000) : -20000;
+            if (MODE == kOzaki) col_e = col_ok ? max(j.eb[col], -20000) : -20000;
             for (int r = 0; r < 32; ++r) {
               const int64_t grow = row0 + r;
               const int row_e = __shfl_sync(0xffffffffu, my_ea, r);
-              if (grow < args.M && col_ok) {
+              if (grow < j.M && col_ok) {
                 const uint32_t v = tr[r * 33 + lane];
                 if (MODE == kOzaki) {
-                  double* cp = static_cast<double*>(args.C) + grow * args.ldc + col;
+                  double* cp = static_cast<double*>(j.C) + grow * j.ldc + col;
                   *cp += fold_term((int32_t)v, row_e + col_e + gexp);
                 } else {
-                  float* cp = static_cast<float*>(args.C) + grow * args.ldc + col;
+                  float* cp = static_cast<float*>(j.C) + grow * j.ldc + col;
                   *cp += __uint_as_float(v);
                 }
               }
@@ -325,6 +413,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc_fence_after();
     tmem_dealloc(tmem_base, Cfg::kTmemCols);
   }
+}
+
+// The setmaxnreg split above redistributes exactly the registers the CTA was
+// launched with; it is only sound if the kernel was compiled with
+// kTcLaunchRegs registers per thread. Checked on the host before every launch
+// (a smaller count would make setmaxnreg.inc wait for registers that never
+// become free).
+inline bool tc_regs_ok(const void* kernel) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return false;
+  return fa.numRegs == kTcLaunchRegs && fa.maxThreadsPerBlock >= kTcThreads;
 }
 
 }  // namespace phpc

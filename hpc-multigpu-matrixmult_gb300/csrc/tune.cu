@@ -26,7 +26,8 @@ struct TuneEntry {
 };
 
 std::once_flag g_once;
-std::vector<TuneEntry> g_table;
+std::vector<TuneEntry> g_table;    // single-problem entries
+std::vector<TuneEntry> g_grouped;  // grouped-call entries (lines starting with "grouped")
 
 std::string library_dir() {
   Dl_info info;
@@ -38,7 +39,9 @@ std::string library_dir() {
   return ".";
 }
 
-// Table format (text): one entry per line, "max_mnk slices bn", '#' comments.
+// Table format (text): one entry per line, "max_mnk slices bn" for single
+// problems or "grouped max_mean_mnk slices bn" for grouped calls; '#' starts a
+// comment line.
 void load_table() {
   const char* env = getenv("PHPC_TUNE_TABLE");
   const std::string path = env ? std::string(env) : library_dir() + "/tune_table.txt";
@@ -48,6 +51,12 @@ void load_table() {
   while (fgets(line, sizeof line, f)) {
     if (line[0] == '#') continue;
     TuneEntry e{};
+    if (strncmp(line, "grouped", 7) == 0) {
+      if (sscanf(line + 7, "%lld %d %d", &e.max_mnk, &e.slices, &e.bn) == 3 && e.slices >= 2 && e.slices <= 8 &&
+          (e.bn == 128 || e.bn == 256))
+        g_grouped.push_back(e);
+      continue;
+    }
     if (sscanf(line, "%lld %d %d", &e.max_mnk, &e.slices, &e.bn) == 3 && e.slices >= 2 && e.slices <= 8 &&
         (e.bn == 128 || e.bn == 256))
       g_table.push_back(e);
@@ -83,6 +92,26 @@ int default_bn(int m, int k, int n) {
   }
   if (const TuneEntry* e = lookup(m, k, n)) return e->bn;
   return 256;
+}
+
+// Tile width of the grouped slice GEMM: PHPC_GROUPED_BN, else the tuning
+// table's entry for the batch's mean problem size, else 128 (small problems
+// waste less of a 128-wide tile).
+int default_grouped_bn(const phpc_gemm_problem* problems, int count) {
+  const char* env = getenv("PHPC_GROUPED_BN");
+  if (env) {
+    const int b = atoi(env);
+    if (b == 128 || b == 256) return b;
+  }
+  double mnk = 0;
+  for (int i = 0; i < count; ++i) mnk += (double)problems[i].m * problems[i].n * problems[i].k;
+  if (count > 0) {
+    std::call_once(g_once, load_table);
+    const long long mean = (long long)(mnk / count);
+    for (const TuneEntry& e : g_grouped)
+      if (mean <= e.max_mnk) return e.bn;
+  }
+  return 128;
 }
 
 }  // namespace phpc

@@ -76,6 +76,25 @@ _lib.phpc_sgemm_ffma_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, 
 _lib.phpc_sgemm_ffma_dev.restype = ct.c_int
 
 
+class GemmProblem(ct.Structure):
+    """phpc_gemm_problem: C += A @ B with device pointers and leading dimensions."""
+    _fields_ = [("m", ct.c_int), ("k", ct.c_int), ("n", ct.c_int), ("A", ct.c_void_p), ("lda", ct.c_int64),
+                ("B", ct.c_void_p), ("ldb", ct.c_int64), ("C", ct.c_void_p), ("ldc", ct.c_int64)]
+
+
+_lib.phpc_grouped_workspace_bytes.argtypes = [ct.POINTER(GemmProblem), ct.c_int, ct.c_int]
+_lib.phpc_grouped_workspace_bytes.restype = ct.c_size_t
+_lib.phpc_grouped_plan_create.argtypes = [ct.POINTER(ct.c_void_p), ct.POINTER(GemmProblem), ct.c_int, ct.c_int,
+                                          ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_grouped_plan_create.restype = ct.c_int
+_lib.phpc_grouped_run.argtypes = [ct.c_void_p, ct.c_void_p]
+_lib.phpc_grouped_run.restype = ct.c_int
+_lib.phpc_grouped_graph_launch.argtypes = [ct.c_void_p, ct.c_void_p]
+_lib.phpc_grouped_graph_launch.restype = ct.c_int
+_lib.phpc_grouped_plan_destroy.argtypes = [ct.c_void_p]
+_lib.phpc_grouped_plan_destroy.restype = None
+
+
 class PhpcError(RuntimeError):
     def __init__(self, code: int, what: str = ""):
         self.code = code
@@ -203,6 +222,52 @@ def sgemm_ffma_dev(m, k, n, A, lda, B, ldb, C, ldc, stream=None) -> None:
     """Plain FP32 C += A @ B on the CUDA cores."""
     _check(_lib.phpc_sgemm_ffma_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, _stream(stream)),
            "phpc_sgemm_ffma_dev")
+
+
+class GroupedPlan:
+    """A planned grouped FP64-accurate GEMM over device-resident problems.
+
+    problems: list of (m, k, n, A, lda, B, ldb, C, ldc) with device pointers or
+    torch tensors. The caller keeps the matrices and the workspace alive."""
+
+    def __init__(self, problems, slices, workspace, workspace_bytes, stream=None):
+        arr = (GemmProblem * len(problems))()
+        for i, (m, k, n, A, lda, B, ldb, C, ldc) in enumerate(problems):
+            arr[i] = GemmProblem(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc)
+        self._arr = arr
+        self._plan = ct.c_void_p()
+        _check(_lib.phpc_grouped_plan_create(ct.byref(self._plan), arr, len(problems), slices, _dptr(workspace),
+                                             workspace_bytes, _stream(stream)), "phpc_grouped_plan_create")
+
+    @staticmethod
+    def workspace_bytes(problems, slices) -> int:
+        arr = (GemmProblem * len(problems))()
+        for i, (m, k, n, A, lda, B, ldb, C, ldc) in enumerate(problems):
+            arr[i] = GemmProblem(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc)
+        return int(_lib.phpc_grouped_workspace_bytes(arr, len(problems), slices))
+
+    def run(self, stream=None) -> None:
+        _check(_lib.phpc_grouped_run(self._plan, _stream(stream)), "phpc_grouped_run")
+
+    def graph_launch(self, stream=None) -> None:
+        _check(_lib.phpc_grouped_graph_launch(self._plan, _stream(stream)), "phpc_grouped_graph_launch")
+
+    def close(self) -> None:
+        if self._plan:
+            _lib.phpc_grouped_plan_destroy(self._plan)
+            self._plan = ct.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+
+def grouped_shapes(count=512, seed=5, lo=64, hi=2048, multiple=16):
+    """Seeded problem shapes of the batching workload: m, k, n each log-uniform
+    in [lo, hi], rounded to a multiple of `multiple` (at least `multiple`)."""
+    rng = np.random.default_rng(seed)
+    x = np.exp(rng.uniform(np.log(lo), np.log(hi), (count, 3)))
+    x = np.maximum(multiple, np.rint(x / multiple) * multiple).astype(int)
+    return [tuple(int(v) for v in row) for row in x]
 
 
 def device_status() -> int:

@@ -122,6 +122,41 @@ int phpc_sgemm_bf16x3_dev(int m, int k, int n, const float *dA, int64_t lda, con
 int phpc_sgemm_ffma_dev(int m, int k, int n, const float *dA, int64_t lda, const float *dB, int64_t ldb, float *dC,
                         int64_t ldc, void *stream);
 
+/* ------------------------------------------------------- grouped GEMM */
+
+/* One independent problem of a grouped call: C += A * B, FP64 row-major
+ * device matrices. */
+typedef struct phpc_gemm_problem {
+  int m, k, n;
+  const double *A;
+  int64_t lda;
+  const double *B;
+  int64_t ldb;
+  double *C;
+  int64_t ldc;
+} phpc_gemm_problem;
+
+typedef struct phpc_grouped_plan phpc_grouped_plan; /* opaque */
+
+/* Workspace for a grouped FP64-accurate (Ozaki) call over `count` problems:
+ * the device problem table plus every problem's digit planes. 0 on invalid
+ * input. */
+size_t phpc_grouped_workspace_bytes(const phpc_gemm_problem *problems, int count, int slices);
+
+/* Builds the plan of a grouped call: writes the problem table and the TMA
+ * descriptors into the workspace (256-byte aligned, at least
+ * phpc_grouped_workspace_bytes) and returns when they are on the device. The
+ * problems' matrices are read only when the plan runs. No reference
+ * counterpart: the reference runs one GEMM per call (src/phpc_gemm.cu:59). */
+int phpc_grouped_plan_create(phpc_grouped_plan **plan, const phpc_gemm_problem *problems, int count, int slices,
+                             void *workspace, size_t workspace_bytes, void *stream);
+/* Enqueues the five launches of the grouped call on `stream` (exponent scans,
+ * digit splits, one persistent slice GEMM over all problems' tiles). */
+int phpc_grouped_run(const phpc_grouped_plan *plan, void *stream);
+/* Same work, captured once into a CUDA graph on first use, then replayed. */
+int phpc_grouped_graph_launch(phpc_grouped_plan *plan, void *stream);
+void phpc_grouped_plan_destroy(phpc_grouped_plan *plan);
+
 /* Slice count the host entry points use for an m x k x n problem
  * (PHPC_SLICES, else the autotuner's table, else 7). */
 int phpc_default_slices(int m, int k, int n);

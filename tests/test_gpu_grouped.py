@@ -1,0 +1,93 @@
+"""Grouped FP64-accurate GEMM (one plan, five launches, CUDA-graph replay).
+
+Each problem of a grouped call must equal, bit for bit, the single-problem
+Ozaki GEMM of the same inputs (the integer slice sums are exact whatever the
+tiling, and the per-element fold order is the same), and stay within the
+Ozaki bar against the double-double oracle.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_batch(torch, shapes, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for m, k, n in shapes:
+        a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+        b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-20, 21, (k, n)))
+        c0 = rng.uniform(-1, 1, (m, n))
+        out.append((a, b, c0, *(torch.from_numpy(x).cuda() for x in (a, b, c0))))
+    return out
+
+
+def single(phpc, torch, A, B, C, s):
+    m, k = A.shape
+    n = B.shape[1]
+    ws = phpc.ozaki_workspace_bytes(m, k, n, s)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    phpc.dgemm_ozaki_dev(m, k, n, A, k, B, n, C, n, s, W, ws)
+
+
+@pytest.mark.parametrize("bn", ["128", "256"])
+def test_grouped_equals_single(phpc, oracle, torch_cuda, monkeypatch, bn):
+    torch = torch_cuda
+    monkeypatch.setenv("PHPC_GROUPED_BN", bn)
+    shapes = [(64, 64, 64), (16, 32, 48), (130, 70, 300), (7, 13, 5), (256, 1024, 128), (96, 2048, 80),
+              (300, 17, 1), (1, 500, 260)] + phpc.grouped_shapes(12, seed=9, lo=16, hi=512)
+    s = 7
+    batch = make_batch(torch, shapes, 3)
+    probs = [(A.shape[0], A.shape[1], B.shape[1], A, A.shape[1], B, B.shape[1], C, B.shape[1])
+             for (_, _, _, A, B, C) in batch]
+    ws = phpc.GroupedPlan.workspace_bytes(probs, s)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    plan = phpc.GroupedPlan(probs, s, W, ws)
+    plan.run()
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    for i, (a, b, c0, A, B, C) in enumerate(batch):
+        C1 = torch.from_numpy(c0).cuda()
+        single(phpc, torch, A, B, C1, s)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(C.cpu().numpy(), C1.cpu().numpy(), err_msg=f"problem {i} {shapes[i]}")
+        if i < 6:
+            err = oracle.rel_errors(C.cpu().numpy(), oracle.gemm_dd(a, b, c0))
+            assert err["frob"] <= 1e-14, (i, err)
+    plan.close()
+
+
+def test_graph_replay_accumulates(phpc, torch_cuda):
+    torch = torch_cuda
+    shapes = phpc.grouped_shapes(24, seed=2, lo=32, hi=384)
+    s = 6
+    batch = make_batch(torch, shapes, 4)
+    probs = [(A.shape[0], A.shape[1], B.shape[1], A, A.shape[1], B, B.shape[1], C, B.shape[1])
+             for (_, _, _, A, B, C) in batch]
+    ws = phpc.GroupedPlan.workspace_bytes(probs, s)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    plan = phpc.GroupedPlan(probs, s, W, ws)
+    plan.graph_launch()
+    plan.graph_launch()  # C += A B twice
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    for i, (a, b, c0, A, B, C) in enumerate(batch):
+        C2 = torch.from_numpy(c0).cuda()
+        single(phpc, torch, A, B, C2, s)
+        single(phpc, torch, A, B, C2, s)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(C.cpu().numpy(), C2.cpu().numpy(), err_msg=f"problem {i}")
+    plan.close()
+
+
+def test_plan_validation(phpc, torch_cuda):
+    torch = torch_cuda
+    A = torch.zeros(64, 64, dtype=torch.float64, device="cuda")
+    probs = [(64, 64, 64, A, 64, A, 64, A, 64)]
+    W = torch.empty(64, dtype=torch.uint8, device="cuda")
+    with pytest.raises(phpc.PhpcError) as e:
+        phpc.GroupedPlan(probs, 7, W, 64)
+    assert e.value.code == 6
+    with pytest.raises(phpc.PhpcError) as e:
+        phpc.GroupedPlan([(0, 64, 64, A, 64, A, 64, A, 64)], 7, W, 64)
+    assert e.value.code == 1
