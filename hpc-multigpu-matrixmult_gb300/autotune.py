@@ -1,0 +1,171 @@
+"""Autotuner for the FP64-accurate Ozaki GEMM: slice count, tile width, L2 raster.
+
+For each square size N it sweeps slices s, output tile width BN (128 or 256)
+and the raster height of the persistent tile order (group_rows), times the
+full call (scans + splits + slice GEMM; CUDA events, median of --reps) on
+seeded inputs resident in HBM, and measures the Frobenius relative error of
+the result against the double-double reference (phpc_dgemm_dd_rows_dev) on
+sampled rows, for two input classes: uniform [-1, 1) and wide exponents
+(u * 2^e, e uniform in [-20, 20]). A configuration qualifies when both errors
+are below target / margin; the fastest qualifying configuration wins. For the
+grouped call it picks BN on the batching workload (512 problems).
+
+Writes tune_table.txt next to this file (copied into lib/ by the build, where
+the library reads it):
+
+    python hpc-multigpu-matrixmult_gb300/autotune.py            # full sweep on the GPU
+    python hpc-multigpu-matrixmult_gb300/autotune.py --max-n 4096 --out /tmp/t.txt
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import sys
+import time
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+
+def main() -> int:
+    p = argparse.ArgumentParser()
+    p.add_argument("--sizes", default="1024,2048,4096,8192,16384")
+    p.add_argument("--max-n", type=int, default=16384)
+    p.add_argument("--slices", default="6,7,8")
+    p.add_argument("--reps", type=int, default=3)
+    p.add_argument("--target", type=float, default=1e-14)
+    p.add_argument("--margin", type=float, default=4.0)
+    p.add_argument("--rows", type=int, default=32)
+    p.add_argument("--grouped-count", type=int, default=512)
+    p.add_argument("--out", default=str(HERE / "tune_table.txt"))
+    a = p.parse_args()
+
+    import numpy as np
+    import torch
+    import phpc
+
+    st = torch.cuda.current_stream()
+    sizes = [n for n in (int(x) for x in a.sizes.split(",")) if n <= a.max_n]
+    slices = [int(x) for x in a.slices.split(",")]
+    table, report = [], []
+
+    def set_cfg(bn, gr):
+        os.environ["PHPC_OZAKI_BN"] = str(bn)
+        os.environ["PHPC_GROUP_ROWS"] = str(gr)
+
+    for n in sizes:
+        classes = {}
+        for name, (emin, emax) in {"uniform": (0, 0), "wide": (-20, 20)}.items():
+            A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+            B = torch.empty((n, n), dtype=torch.float64, device="cuda")
+            if emin == emax:
+                phpc.fill_uniform_dev(A, n * n, 11, 0, st)
+                phpc.fill_uniform_dev(B, n * n, 12, 0, st)
+            else:
+                phpc.fill_wide_dev(A, n * n, 11, 0, emin, emax, st)
+                phpc.fill_wide_dev(B, n * n, 12, 0, emin, emax, st)
+            rows = np.linspace(0, n - 1, min(a.rows, n)).astype(np.int32)
+            d_rows = torch.from_numpy(rows).cuda()
+            R = torch.empty((len(rows), n), dtype=torch.float64, device="cuda")
+            phpc.dgemm_dd_rows_dev(n, n, n, A, n, B, n, None, n, d_rows, len(rows), R, n, st)
+            classes[name] = (A, B, d_rows, R)
+        C = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        grs = [4, 8, 16] if n >= 8192 else [8]
+        cands = []
+        for s in slices:
+            ws = phpc.ozaki_workspace_bytes(n, n, n, s)
+            W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+            set_cfg(256, 8)
+            errs = {}
+            for name, (A, B, d_rows, R) in classes.items():
+                C.zero_()
+                phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
+                got = C.index_select(0, d_rows.long())
+                errs[name] = float((got - R).norm() / R.norm())
+            ok = all(e <= a.target / a.margin for e in errs.values())
+            A, B, _, _ = classes["wide"]
+            for bn in (128, 256):
+                for gr in grs:
+                    set_cfg(bn, gr)
+                    phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)  # warm
+                    ts = []
+                    for _ in range(a.reps):
+                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        e0.record(st)
+                        phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
+                        e1.record(st)
+                        e1.synchronize()
+                        ts.append(e0.elapsed_time(e1))
+                    ms = statistics.median(ts)
+                    rec = {"n": n, "slices": s, "bn": bn, "group_rows": gr, "ms": round(ms, 3),
+                           "tflops": round(2.0 * n ** 3 / ms / 1e9, 3), "err": errs, "qualifies": ok}
+                    report.append(rec)
+                    print(json.dumps(rec), flush=True)
+                    if ok:
+                        cands.append(rec)
+            del W
+            torch.cuda.empty_cache()
+        if not cands:
+            raise SystemExit(f"no configuration meets {a.target} / {a.margin} at N={n}")
+        best = min(cands, key=lambda r: r["ms"])
+        table.append(best)
+        del classes, C
+        torch.cuda.empty_cache()
+
+    # grouped call: tile width on the batching workload
+    grouped_bn, grouped_rep = 128, []
+    if a.grouped_count > 0:
+        shapes = phpc.grouped_shapes(a.grouped_count, seed=5)
+        mats = []
+        for i, (m, k, n) in enumerate(shapes):
+            A = torch.empty((m, k), dtype=torch.float64, device="cuda")
+            B = torch.empty((k, n), dtype=torch.float64, device="cuda")
+            phpc.fill_uniform_dev(A, m * k, 1000 + 2 * i, 0, st)
+            phpc.fill_uniform_dev(B, k * n, 1001 + 2 * i, 0, st)
+            mats.append((A, B, torch.zeros((m, n), dtype=torch.float64, device="cuda")))
+        s = table[-1]["slices"] if table else 7
+        probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B, C) in zip(shapes, mats)]
+        best_ms = None
+        for bn in (128, 256):
+            os.environ["PHPC_GROUPED_BN"] = str(bn)
+            ws = phpc.GroupedPlan.workspace_bytes(probs, s)
+            W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+            plan = phpc.GroupedPlan(probs, s, W, ws, st)
+            plan.graph_launch(st)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(a.reps):
+                plan.graph_launch(st)
+            e1.record(st)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / a.reps
+            plan.close()
+            del W
+            rec = {"grouped_count": a.grouped_count, "slices": s, "bn": bn, "ms": round(ms, 3)}
+            grouped_rep.append(rec)
+            print(json.dumps(rec), flush=True)
+            if best_ms is None or ms < best_ms:
+                best_ms, grouped_bn = ms, bn
+        os.environ.pop("PHPC_GROUPED_BN", None)
+
+    assert phpc.device_status() == 0
+    lines = [f"# written by autotune.py on {torch.cuda.get_device_name()} ({time.strftime('%Y-%m-%d %H:%M UTC', time.gmtime())})",
+             f"# target Frobenius error {a.target} / margin {a.margin}, uniform and wide-exponent inputs",
+             "# max_mnk slices bn group_rows   (chosen: ms, FP64-equivalent TFLOP/s, errors)"]
+    for i, b in enumerate(table):
+        nxt = table[i + 1]["n"] if i + 1 < len(table) else None
+        bound = int((b["n"] ** 3 * nxt ** 3) ** 0.5) if nxt else 2 ** 62
+        lines.append(f"# N={b['n']}: {b['ms']} ms, {b['tflops']} TFLOP/s, err {b['err']}")
+        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']}")
+    lines.append(f"grouped {2 ** 62} {table[-1]['slices'] if table else 7} {grouped_bn}")
+    Path(a.out).write_text("\n".join(lines) + "\n")
+    print(f"wrote {a.out}")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

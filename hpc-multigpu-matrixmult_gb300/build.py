@@ -64,6 +64,9 @@ def build_library(jobs: int | None = None) -> Path:
     so = LIB / "libphpc_gemm.so"
     if not _newer(so, objs):
         _run([NVCC, *GENCODE, "-shared", "-o", str(so), *map(str, objs), "-lcudart", "-ldl"])
+    table = PKG / "tune_table.txt"  # written by autotune.py; read by the library from its own directory
+    if table.exists():
+        shutil.copyfile(table, LIB / "tune_table.txt")
     return so
 
 

@@ -143,14 +143,12 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.K = k;
   a.tm = ceil_div(m, kTcBM);
   a.tn = ceil_div(n, BN);
-  a.group_rows = 8;
+  a.group_rows = default_group_rows(m, k, n);
   a.C = C;
   a.ldc = ldc;
   a.ea = ea;
   a.eb = eb;
   a.status = device_status_ptr();
-  const char* gr = getenv("PHPC_GROUP_ROWS");
-  if (gr && atoi(gr) > 0) a.group_rows = atoi(gr);
   auto kern = tc_slice_gemm_kernel<BN, MODE>;
   if (!tc_regs_ok(reinterpret_cast<const void*>(kern))) return PHPC_ERR_UNSUPPORTED;
   PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));

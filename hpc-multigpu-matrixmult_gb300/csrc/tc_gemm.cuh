@@ -158,12 +158,23 @@ __device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap
   }
 }
 
-// 2^x as a double for any int x (0 below the subnormal range, inf above).
-__device__ __forceinline__ double fold_term(int32_t s, int x) {
-  const double v = static_cast<double>(s);
-  if (x >= -1022 && x <= 1023) return v * __longlong_as_double(static_cast<long long>(x + 1023) << 52);
-  if (s == 0) return 0.0;
-  return ldexp(v, x);
+// c + s * 2^x with one rounding (the product is exact). In the normal range
+// the double s * 2^x is assembled from integer bit operations (sign, the
+// leading-one position of |s| for the exponent, the remaining bits as the
+// mantissa), so the FP64 pipe only performs the final add; FP64 throughput
+// on this GPU is ~1.6 operations per clock per SM.
+__device__ __forceinline__ double fold_add(double c, int32_t s, int x) {
+  if (s == 0) return c + 0.0;
+  const uint32_t neg = static_cast<uint32_t>(s) & 0x80000000u;
+  const uint32_t a = neg ? 0u - static_cast<uint32_t>(s) : static_cast<uint32_t>(s);
+  const int e = 31 - __clz(a);                  // a in [2^e, 2^(e+1))
+  const int E = e + x + 1023;                   // biased exponent of s * 2^x
+  if (E >= 1 && E <= 2046) {
+    const uint64_t mant = (static_cast<uint64_t>(a) << (52 - e)) & 0x000FFFFFFFFFFFFFull;
+    const uint64_t bits = (static_cast<uint64_t>(neg) << 32) | (static_cast<uint64_t>(E) << 52) | mant;
+    return c + __longlong_as_double(static_cast<long long>(bits));
+  }
+  return c + ldexp(static_cast<double>(s), x);  // subnormal or overflowing terms
 }
 
 template <int BN, int MODE, bool GROUPED = false>
@@ -221,16 +232,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       int issued = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        TcJob j;
-        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, j);
+        TcJob job;
+        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, job);
         for (int pi = 0; pi < pairs.n && ok; ++pi) {
           const int pa = pairs.a[pi], pb = pairs.b[pi];
-          for (int kb = 0; kb < j.nk; ++kb) {
+          for (int kb = 0; kb < job.nk; ++kb) {
             if (!wait_parity(&empty[stage], phase ^ 1, status, 11)) { ok = false; break; }
             mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
             uint8_t* sa = smem + stage * Cfg::kStageBytes;
-            tma_load_3d(sa, j.tmA, kb * kTcBK, j.rm * kTcBM, pa, &full[stage]);
-            tma_load_3d(sa + Cfg::kStageA, j.tmB, kb * kTcBK, j.rn * BN, pb, &full[stage]);
+            tma_load_3d(sa, job.tmA, kb * kTcBK, job.rm * kTcBM, pa, &full[stage]);
+            tma_load_3d(sa + Cfg::kStageA, job.tmB, kb * kTcBK, job.rn * BN, pb, &full[stage]);
             ++issued;
             if (++stage == S) { stage = 0; phase ^= 1; }
           }
@@ -257,8 +268,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       int buf = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        TcJob j;
-        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, j);
+        TcJob job;
+        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, job);
         int gstart = 0;
         while (gstart < pairs.n && ok) {
           int gend = gstart + 1;
@@ -266,7 +277,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
           else
             gend = pairs.n;
-          const int total = (gend - gstart) * j.nk;
+          const int total = (gend - gstart) * job.nk;
           const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
             const int len = min(chunk, total - done);
@@ -316,14 +327,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int j = 0; j < HALF; ++j) acc[j] = 0;
 
     for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      TcJob j;
-      tc_job<GROUPED>(t, args, &tmA, &tmB, gt, j);
-      const int64_t row0 = (int64_t)j.rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
-      const int col0 = j.rn * BN + half * HALF;                 // first global column of this warp's half
+      TcJob job;
+      tc_job<GROUPED>(t, args, &tmA, &tmB, gt, job);
+      const int64_t row0 = (int64_t)job.rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
+      const int col0 = job.rn * BN + half * HALF;                 // first global column of this warp's half
       int my_ea = 0;
       if (MODE == kOzaki) {
         const int64_t r = row0 + lane;
-        my_ea = r < j.M ? max(j.ea[r], -20000) : -20000;
+        my_ea = r < job.M ? max(job.ea[r], -20000) : -20000;
       }
       int gstart = 0;
       while (gstart < pairs.n && ok) {
@@ -332,7 +343,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
         else
           gend = pairs.n;
-        const int total = (gend - gstart) * j.nk;
+        const int total = (gend - gstart) * job.nk;
         const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
         const int nchunks = (total + chunk - 1) / chunk;
         for (int c = 0; c < nchunks && ok; ++c) {
@@ -374,26 +385,49 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           // transposed through shared memory so that a warp touches one
           // contiguous 32-element run of a row per access.
           const int gexp = MODE == kOzaki ? 2 - 8 * (int)pairs.g[gstart] : 0;
+          constexpr int kBatch = 16;  // rows whose C loads are in flight together
 #pragma unroll
           for (int cb = 0; cb < HALF; cb += 32) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) tr[lane * 33 + j] = (uint32_t)acc[cb + j];
+            for (int u = 0; u < 32; ++u) tr[lane * 33 + u] = (uint32_t)acc[cb + u];
             __syncwarp();
             const int col = col0 + cb + lane;
-            const bool col_ok = col < j.N;
+            const bool col_ok = col < job.N;
             int col_e = 0;
-            if (MODE == kOzaki) col_e = col_ok ? max(j.eb[col], -20000) : -20000;
-            for (int r = 0; r < 32; ++r) {
-              const int64_t grow = row0 + r;
-              const int row_e = __shfl_sync(0xffffffffu, my_ea, r);
-              if (grow < j.M && col_ok) {
-                const uint32_t v = tr[r * 33 + lane];
-                if (MODE == kOzaki) {
-                  double* cp = static_cast<double*>(j.C) + grow * j.ldc + col;
-                  *cp += fold_term((int32_t)v, row_e + col_e + gexp);
-                } else {
-                  float* cp = static_cast<float*>(j.C) + grow * j.ldc + col;
-                  *cp += __uint_as_float(v);
+            if (MODE == kOzaki) col_e = col_ok ? max(job.eb[col], -20000) : -20000;
+#pragma unroll 1
+            for (int r0 = 0; r0 < 32; r0 += kBatch) {
+              // All loads of the batch are issued before any store, so the
+              // read-modify-write of C costs one memory latency per batch
+              // instead of one per row.
+              if (MODE == kOzaki) {
+                double* Cd = static_cast<double*>(job.C);
+                double cv[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                  const int64_t grow = row0 + r0 + u;
+                  cv[u] = (grow < job.M && col_ok) ? Cd[grow * job.ldc + col] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                  const int64_t grow = row0 + r0 + u;
+                  const int row_e = __shfl_sync(0xffffffffu, my_ea, r0 + u);
+                  if (grow < job.M && col_ok)
+                    Cd[grow * job.ldc + col] =
+                        fold_add(cv[u], (int32_t)tr[(r0 + u) * 33 + lane], row_e + col_e + gexp);
+                }
+              } else {
+                float* Cf = static_cast<float*>(job.C);
+                float cv[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                  const int64_t grow = row0 + r0 + u;
+                  cv[u] = (grow < job.M && col_ok) ? Cf[grow * job.ldc + col] : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < kBatch; ++u) {
+                  const int64_t grow = row0 + r0 + u;
+                  if (grow < job.M && col_ok) Cf[grow * job.ldc + col] = cv[u] + __uint_as_float(tr[(r0 + u) * 33 + lane]);
                 }
               }
             }

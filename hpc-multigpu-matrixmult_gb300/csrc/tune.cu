@@ -23,6 +23,7 @@ struct TuneEntry {
   long long max_mnk;  // entry applies to problems with m*n*k <= max_mnk (first match wins)
   int slices;
   int bn;
+  int group_rows;     // L2 raster height of the persistent tile order (0 = default 8)
 };
 
 std::once_flag g_once;
@@ -39,9 +40,9 @@ std::string library_dir() {
   return ".";
 }
 
-// Table format (text): one entry per line, "max_mnk slices bn" for single
-// problems or "grouped max_mean_mnk slices bn" for grouped calls; '#' starts a
-// comment line.
+// Table format (text): one entry per line, "max_mnk slices bn [group_rows]"
+// for single problems or "grouped max_mean_mnk slices bn" for grouped calls;
+// '#' starts a comment line. Written by autotune.py.
 void load_table() {
   const char* env = getenv("PHPC_TUNE_TABLE");
   const std::string path = env ? std::string(env) : library_dir() + "/tune_table.txt";
@@ -57,9 +58,11 @@ void load_table() {
         g_grouped.push_back(e);
       continue;
     }
-    if (sscanf(line, "%lld %d %d", &e.max_mnk, &e.slices, &e.bn) == 3 && e.slices >= 2 && e.slices <= 8 &&
-        (e.bn == 128 || e.bn == 256))
+    const int got = sscanf(line, "%lld %d %d %d", &e.max_mnk, &e.slices, &e.bn, &e.group_rows);
+    if (got >= 3 && e.slices >= 2 && e.slices <= 8 && (e.bn == 128 || e.bn == 256)) {
+      if (got < 4 || e.group_rows < 1 || e.group_rows > 64) e.group_rows = 0;
       g_table.push_back(e);
+    }
   }
   fclose(f);
 }
@@ -92,6 +95,14 @@ int default_bn(int m, int k, int n) {
   }
   if (const TuneEntry* e = lookup(m, k, n)) return e->bn;
   return 256;
+}
+
+int default_group_rows(int m, int k, int n) {
+  const char* env = getenv("PHPC_GROUP_ROWS");
+  if (env && atoi(env) > 0 && atoi(env) <= 64) return atoi(env);
+  if (const TuneEntry* e = lookup(m, k, n))
+    if (e->group_rows > 0) return e->group_rows;
+  return 8;
 }
 
 // Tile width of the grouped slice GEMM: PHPC_GROUPED_BN, else the tuning
