@@ -10,6 +10,9 @@
 //  - the device copies use leading dimensions padded to an even number of
 //    doubles so that TMA can address every row;
 //  - buffers that are already page-locked are not registered again;
+//  - the copies of A, B and C and the digit splits overlap on three streams,
+//    and device buffers come from a grow-only library pool (PHPC_POOL_KEEP=0
+//    returns them to the system after every call, as the reference did);
 //  - every CUDA call is checked; the outcome is kept for phpc_last_error().
 #include <cstdlib>
 #include <cstring>
@@ -52,25 +55,39 @@ void unpin(Pinned& pn) {
   pn.registered = false;
 }
 
+constexpr int kStreams = 3;
+
 struct CallResources {
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaStream_t st[kStreams] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev[8] = {};
   double *dA = nullptr, *dB = nullptr, *dC = nullptr;
   void* ws = nullptr;
   ~CallResources() {
-    if (stream) {
-      if (ws) cudaFreeAsync(ws, stream);
-      if (dC) cudaFreeAsync(dC, stream);
-      if (dB) cudaFreeAsync(dB, stream);
-      if (dA) cudaFreeAsync(dA, stream);
-      cudaStreamSynchronize(stream);
-      cudaStreamDestroy(stream);
+    if (st[0]) {
+      if (ws) cudaFreeAsync(ws, st[0]);
+      if (dC) cudaFreeAsync(dC, st[0]);
+      if (dB) cudaFreeAsync(dB, st[0]);
+      if (dA) cudaFreeAsync(dA, st[0]);
+      cudaStreamSynchronize(st[0]);
     }
+    for (auto& x : st)
+      if (x) cudaStreamDestroy(x);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
   }
 };
 
+float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  return cudaEventElapsedTime(&ms, a, b) == cudaSuccess ? ms : 0.f;
+}
+
+// Copies and compute of one call overlap across three streams: A (stream 0),
+// B (stream 1) and C (stream 2) travel to the device concurrently; A's and
+// B's digit splits start as soon as their operand has arrived; the GEMM runs
+// on stream 0 once B's split and C's copy are done; C returns on stream 0.
+// Device buffers come from the library's grow-only pool, so repeated calls of
+// one size allocate no new memory. *seconds = sum of the kernels' device time.
 int host_gemm(Method method, const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k,
               int n, int gw, int gh, float* seconds) {
   if (seconds) *seconds = 0.f;
@@ -81,6 +98,9 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
   const DeviceInfo* dev = current_device();
   if (!dev) return PHPC_ERR_CUDA;
   if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
+  cudaMemPool_t pool = host_api_pool();
+  int* status = device_status_ptr();
+  if (!pool || !status) return PHPC_ERR_CUDA;
 
   Pinned pa, pb, pc;
   pin(pa, a, ((size_t)(m - 1) * lda + k) * sizeof(double));
@@ -91,76 +111,99 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
   {
     CallResources r;
     const int64_t dlda = (k + 1) & ~1, dldb = (n + 1) & ~1, dldc = (n + 1) & ~1;
-    if (cudaStreamCreateWithFlags(&r.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&r.ev[0]) != cudaSuccess || cudaEventCreate(&r.ev[1]) != cudaSuccess) {
-      rc = PHPC_ERR_CUDA;
-    }
-    if (rc == PHPC_OK &&
-        (cudaMallocAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, r.stream) != cudaSuccess ||
-         cudaMallocAsync(reinterpret_cast<void**>(&r.dB), sizeof(double) * k * dldb, r.stream) != cudaSuccess ||
-         cudaMallocAsync(reinterpret_cast<void**>(&r.dC), sizeof(double) * m * dldc, r.stream) != cudaSuccess))
-      rc = PHPC_ERR_NOMEM;
+    for (auto& x : r.st)
+      if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    for (auto& e : r.ev)
+      if (rc == PHPC_OK && cudaEventCreate(&e) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    // events: 0 allocated, 1 B ready (split done / copied), 2 C copied,
+    //         3/4 A-side kernels, 5/6 B-side kernels, 7 GEMM start
+    cudaStream_t s0 = r.st[0], s1 = r.st[1], s2 = r.st[2];
     int slices = 0;
     size_t ws_bytes = 0;
-    if (rc == PHPC_OK && method == kOzakiMethod) {
+    if (method == kOzakiMethod) {
       slices = default_slices(m, k, n);
       ws_bytes = ozaki_workspace_bytes(m, k, n, slices);
-      if (cudaMallocAsync(&r.ws, ws_bytes, r.stream) != cudaSuccess) rc = PHPC_ERR_NOMEM;
     }
+    if (rc == PHPC_OK &&
+        (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, pool, s0) !=
+             cudaSuccess ||
+         cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dB), sizeof(double) * k * dldb, pool, s0) !=
+             cudaSuccess ||
+         cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dC), sizeof(double) * m * dldc, pool, s0) !=
+             cudaSuccess ||
+         (ws_bytes && cudaMallocFromPoolAsync(&r.ws, ws_bytes, pool, s0) != cudaSuccess)))
+      rc = PHPC_ERR_NOMEM;
     if (rc == PHPC_OK) {
-      if (cudaMemcpy2DAsync(r.dA, dlda * 8, a, (size_t)lda * 8, (size_t)k * 8, m, cudaMemcpyHostToDevice,
-                            r.stream) != cudaSuccess ||
-          cudaMemcpy2DAsync(r.dB, dldb * 8, b, (size_t)ldb * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice,
-                            r.stream) != cudaSuccess ||
-          cudaMemcpy2DAsync(r.dC, dldc * 8, c, (size_t)ldc * 8, (size_t)n * 8, m, cudaMemcpyHostToDevice,
-                            r.stream) != cudaSuccess)
+      cudaMemsetAsync(status, 0, sizeof(int), s0);
+      cudaEventRecord(r.ev[0], s0);
+      cudaStreamWaitEvent(s1, r.ev[0], 0);
+      cudaStreamWaitEvent(s2, r.ev[0], 0);
+      if (cudaMemcpy2DAsync(r.dA, dlda * 8, a, (size_t)lda * 8, (size_t)k * 8, m, cudaMemcpyHostToDevice, s0) !=
+              cudaSuccess ||
+          cudaMemcpy2DAsync(r.dB, dldb * 8, b, (size_t)ldb * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s1) !=
+              cudaSuccess ||
+          cudaMemcpy2DAsync(r.dC, dldc * 8, c, (size_t)ldc * 8, (size_t)n * 8, m, cudaMemcpyHostToDevice, s2) !=
+              cudaSuccess)
         rc = PHPC_ERR_CUDA;
     }
-    int* status = device_status_ptr();
-    if (rc == PHPC_OK && status && cudaMemsetAsync(status, 0, sizeof(int), r.stream) != cudaSuccess)
-      rc = PHPC_ERR_CUDA;
     if (rc == PHPC_OK) {
-      cudaEventRecord(r.ev[0], r.stream);
-      if (method == kDmma)
-        rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, gw, gh, 256, r.stream);
-      else
-        rc = dgemm_ozaki(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, slices, r.ws, ws_bytes, r.stream,
-                         default_bn(m, k, n));
-      cudaEventRecord(r.ev[1], r.stream);
+      cudaEventRecord(r.ev[2], s2);
+      if (method == kOzakiMethod) {
+        cudaEventRecord(r.ev[3], s0);
+        cudaEventRecord(r.ev[5], s1);
+        rc = ozaki_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, slices, r.ws, ws_bytes, s0, s1);
+        cudaEventRecord(r.ev[4], s0);
+        cudaEventRecord(r.ev[6], s1);
+      }
+      cudaEventRecord(r.ev[1], s1);
+      cudaStreamWaitEvent(s0, r.ev[1], 0);
+      cudaStreamWaitEvent(s0, r.ev[2], 0);
+      cudaEventRecord(r.ev[7], s0);
+      if (rc == PHPC_OK) {
+        if (method == kDmma)
+          rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, gw, gh, 256, s0);
+        else
+          rc = ozaki_multiply(m, k, n, r.dC, dldc, slices, r.ws, ws_bytes, s0, default_bn(m, k, n));
+      }
     }
-    if (rc == PHPC_OK && cudaStreamSynchronize(r.stream) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    cudaEvent_t end_ev = nullptr;
+    if (rc == PHPC_OK && cudaEventCreate(&end_ev) == cudaSuccess) cudaEventRecord(end_ev, s0);
+    if (rc == PHPC_OK && cudaStreamSynchronize(s0) != cudaSuccess) rc = PHPC_ERR_CUDA;
     int dstatus = 0;
-    if (rc == PHPC_OK && status) {
-      if (cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    if (rc == PHPC_OK && cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = PHPC_ERR_CUDA;
+    float kernel_ms = 0.f;
+    if (rc == PHPC_OK && end_ev) {
+      kernel_ms = elapsed_ms(r.ev[7], end_ev);
+      if (method == kOzakiMethod) kernel_ms += elapsed_ms(r.ev[3], r.ev[4]) + elapsed_ms(r.ev[5], r.ev[6]);
     }
     if (rc == PHPC_OK && method == kOzakiMethod && (dstatus & 0xFF) == PHPC_ERR_NONFINITE) {
       // inf/NaN cannot be carried by integer digits: redo this call in IEEE
       // FP64 (DMMA) from the original C so that inf/NaN propagate exactly.
       dstatus = 0;
-      if (cudaMemsetAsync(status, 0, sizeof(int), r.stream) != cudaSuccess ||
-          cudaMemcpy2DAsync(r.dC, dldc * 8, c, (size_t)ldc * 8, (size_t)n * 8, m, cudaMemcpyHostToDevice,
-                            r.stream) != cudaSuccess)
+      if (cudaMemsetAsync(status, 0, sizeof(int), s0) != cudaSuccess ||
+          cudaMemcpy2DAsync(r.dC, dldc * 8, c, (size_t)ldc * 8, (size_t)n * 8, m, cudaMemcpyHostToDevice, s0) !=
+              cudaSuccess)
         rc = PHPC_ERR_CUDA;
       if (rc == PHPC_OK) {
-        cudaEventRecord(r.ev[0], r.stream);
-        rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, gw, gh, 256, r.stream);
-        cudaEventRecord(r.ev[1], r.stream);
+        cudaEventRecord(r.ev[7], s0);
+        rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, gw, gh, 256, s0);
+        cudaEventRecord(end_ev, s0);
       }
-      if (rc == PHPC_OK && cudaStreamSynchronize(r.stream) != cudaSuccess) rc = PHPC_ERR_CUDA;
+      if (rc == PHPC_OK && cudaStreamSynchronize(s0) != cudaSuccess) rc = PHPC_ERR_CUDA;
       if (rc == PHPC_OK && cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
         rc = PHPC_ERR_CUDA;
+      kernel_ms = elapsed_ms(r.ev[7], end_ev);
     }
+    if (end_ev) cudaEventDestroy(end_ev);
     if (rc == PHPC_OK && dstatus != 0) rc = dstatus;
     if (rc == PHPC_OK) {
-      if (cudaMemcpy2DAsync(c, (size_t)ldc * 8, r.dC, dldc * 8, (size_t)n * 8, m, cudaMemcpyDeviceToHost,
-                            r.stream) != cudaSuccess ||
-          cudaStreamSynchronize(r.stream) != cudaSuccess)
+      if (cudaMemcpy2DAsync(c, (size_t)ldc * 8, r.dC, dldc * 8, (size_t)n * 8, m, cudaMemcpyDeviceToHost, s0) !=
+              cudaSuccess ||
+          cudaStreamSynchronize(s0) != cudaSuccess)
         rc = PHPC_ERR_CUDA;
     }
-    if (rc == PHPC_OK && seconds) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, r.ev[0], r.ev[1]) == cudaSuccess) *seconds = ms / 1000.f;
-    }
+    if (rc == PHPC_OK && seconds) *seconds = kernel_ms / 1000.f;
   }
   unpin(pc);
   unpin(pb);

@@ -166,8 +166,10 @@ template int launch_tc_slice_gemm<128, kF32>(const void*, const void*, int, int,
 
 size_t ozaki_workspace_bytes(int m, int k, int n, int s) { return ozaki_layout(m, k, n, s).total; }
 
-int ozaki_prepare(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
-                  size_t ws_bytes, cudaStream_t stream) {
+// Scans and digit splits: A's (rows) on stream_a, B's (columns) on stream_b,
+// so that each can start as soon as its operand is on the device.
+int ozaki_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
+                   size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b) {
   const DeviceInfo* dev = current_device();
   if (!dev) return PHPC_ERR_CUDA;
   if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
@@ -180,23 +182,28 @@ int ozaki_prepare(int m, int k, int n, const double* dA, int64_t lda, const doub
   uint16_t* pb = reinterpret_cast<uint16_t*>(base + L.off_pb);
   int* status = device_status_ptr();
 
-  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream>>>(dA, lda, m, k, ea, status);
-  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(eb, n, kExpZero);
+  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream_a>>>(dA, lda, m, k, ea, status);
+  {
+    dim3 g(m, ceil_div(L.ldp / 8, 128));
+    split_rows_kernel<<<g, 128, 0, stream_a>>>(dA, lda, m, k, ea, s, pa, L.ldp, (int64_t)m * L.ldp);
+  }
+  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream_b>>>(eb, n, kExpZero);
   {
     const int krows = 256;
     dim3 g(ceil_div(n, 256), ceil_div(k, krows));
-    scan_cols_kernel<<<g, 256, 0, stream>>>(dB, ldb, k, n, krows, eb, status);
-  }
-  {
-    dim3 g(m, ceil_div(L.ldp / 8, 128));
-    split_rows_kernel<<<g, 128, 0, stream>>>(dA, lda, m, k, ea, s, pa, L.ldp, (int64_t)m * L.ldp);
+    scan_cols_kernel<<<g, 256, 0, stream_b>>>(dB, ldb, k, n, krows, eb, status);
   }
   {
     dim3 g(ceil_div(n, 64), ceil_div(k, 32));
-    split_cols_kernel<<<g, 256, 0, stream>>>(dB, ldb, k, n, eb, s, pb, L.ldp, (int64_t)n * L.ldp);
+    split_cols_kernel<<<g, 256, 0, stream_b>>>(dB, ldb, k, n, eb, s, pb, L.ldp, (int64_t)n * L.ldp);
   }
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
+}
+
+int ozaki_prepare(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
+                  size_t ws_bytes, cudaStream_t stream) {
+  return ozaki_prepare2(m, k, n, dA, lda, dB, ldb, s, ws, ws_bytes, stream, stream);
 }
 
 int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const void* ws, size_t ws_bytes,

@@ -50,6 +50,13 @@ int dgemm_dmma(int m, int k, int n, const double* dA, int64_t lda, const double*
 int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
                 int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
 size_t ozaki_workspace_bytes(int m, int k, int n, int s);
+int ozaki_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
+                   size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b);
+int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const void* ws, size_t ws_bytes,
+                   cudaStream_t stream, int bn);
+// Device memory pool of the host entry points (one per device, grow-only
+// unless PHPC_POOL_KEEP=0): buffers of one call are reused by the next.
+cudaMemPool_t host_api_pool();
 int default_slices(int m, int k, int n);
 int default_bn(int m, int k, int n);
 int default_grouped_bn(const phpc_gemm_problem* problems, int count);

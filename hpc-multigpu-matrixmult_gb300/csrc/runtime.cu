@@ -53,6 +53,29 @@ int* device_status_ptr() {
   return g_status_ptr[dev];
 }
 
+namespace {
+cudaMemPool_t g_pool[kMaxDevices];
+}  // namespace
+
+cudaMemPool_t host_api_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return nullptr;
+    const char* keep = getenv("PHPC_POOL_KEEP");
+    uint64_t threshold = (keep && atoi(keep) == 0) ? 0 : UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    g_pool[dev] = pool;
+  }
+  return g_pool[dev];
+}
+
 bool encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
                   const uint64_t* strides_bytes, const uint32_t* box, CUtensorMapSwizzle swz) {
   {
