@@ -50,7 +50,7 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
 # dominant kernel, from a one-pass ncu capture of this workload
 # (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by (N, slices).
-NCU_TRAFFIC_BYTES = {(16384, 7): 501.57e9 + 15.98e9}
+NCU_TRAFFIC_BYTES = {(16384, 7): 426.25e9 + 15.28e9}
 UNIT = "TFLOP/s"
 
 
