@@ -135,6 +135,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def reduce_max(x: float, world: int, device=None) -> float:
+    """Maximum of x over the ranks of the default process group (x itself on one rank)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(flops_per_rank: float, seconds_per_step: float, world: int) -> float:
+    """Whole-job TFLOP/s of `world` independent replicas: total work / slowest rank's time."""
+    return world * flops_per_rank / seconds_per_step / 1e12
+
+
 def ozaki_pairs(s: int) -> int:
     return s * (s + 1) // 2
 
@@ -168,11 +185,7 @@ def run_ours(args, world, rank, local):
             torch.distributed.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, world, dev)
 
     # ---- errors of both methods against the double-double reference (untimed)
     rng = np.random.default_rng(seed)
@@ -242,7 +255,7 @@ def run_ours(args, world, rank, local):
     status = phpc.device_status()
     if status != 0:
         raise RuntimeError(f"device status {status} after the timed region")
-    value = world * flops / step_s / 1e12
+    value = replica_throughput(flops, step_s, world)
 
     # ---- end to end through the reference-facing C ABI (pinned host buffers)
     Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -261,7 +274,7 @@ def run_ours(args, world, rank, local):
         phpc.gemm_cublas(an, n, bn, n, cn, n, n, n, n)
         e2e_s.append(time.perf_counter() - w0)
     e2e_step = max_over_ranks(statistics.median(e2e_s))
-    e2e_value = world * flops / e2e_step / 1e12
+    e2e_value = replica_throughput(flops, e2e_step, world)
 
     peaks = measured_peaks()
     peak = peaks.get("bf16_tflops_sustained")
