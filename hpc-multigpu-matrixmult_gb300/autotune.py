@@ -1,7 +1,9 @@
 """Autotuner for the FP64-accurate Ozaki GEMM: slice count, tile width, L2 raster.
 
-For each square size N it sweeps slices s, output tile width BN (128 or 256)
-and the raster height of the persistent tile order (group_rows), times the
+For each square size N it sweeps slices s, output tile width BN (128 or 256),
+the raster height of the persistent tile order (group_rows) and the CTA
+grouping (1 = one CTA per 128 x BN tile, 2 = CTA pairs computing 256 x BN
+tiles with M = 256 tcgen05 MMAs), times the
 full call (scans + splits + slice GEMM; CUDA events, median of --reps) on
 seeded inputs resident in HBM, and measures the Frobenius relative error of
 the result against the double-double reference (phpc_dgemm_dd_rows_dev) on
@@ -40,6 +42,7 @@ def main() -> int:
     p.add_argument("--margin", type=float, default=4.0)
     p.add_argument("--rows", type=int, default=32)
     p.add_argument("--grouped-count", type=int, default=512)
+    p.add_argument("--clusters", default="1,2")
     p.add_argument("--out", default=str(HERE / "tune_table.txt"))
     a = p.parse_args()
 
@@ -52,9 +55,12 @@ def main() -> int:
     slices = [int(x) for x in a.slices.split(",")]
     table, report = [], []
 
-    def set_cfg(bn, gr):
+    clusters = [int(x) for x in a.clusters.split(",")]
+
+    def set_cfg(bn, gr, cl=1):
         os.environ["PHPC_OZAKI_BN"] = str(bn)
         os.environ["PHPC_GROUP_ROWS"] = str(gr)
+        os.environ["PHPC_CLUSTER"] = str(cl)
 
     for n in sizes:
         classes = {}
@@ -89,23 +95,24 @@ def main() -> int:
             A, B, _, _ = classes["wide"]
             for bn in (128, 256):
                 for gr in grs:
-                    set_cfg(bn, gr)
-                    phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)  # warm
-                    ts = []
-                    for _ in range(a.reps):
-                        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                        e0.record(st)
-                        phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
-                        e1.record(st)
-                        e1.synchronize()
-                        ts.append(e0.elapsed_time(e1))
-                    ms = statistics.median(ts)
-                    rec = {"n": n, "slices": s, "bn": bn, "group_rows": gr, "ms": round(ms, 3),
-                           "tflops": round(2.0 * n ** 3 / ms / 1e9, 3), "err": errs, "qualifies": ok}
-                    report.append(rec)
-                    print(json.dumps(rec), flush=True)
-                    if ok:
-                        cands.append(rec)
+                    for cl in clusters:
+                        set_cfg(bn, gr, cl)
+                        phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)  # warm
+                        ts = []
+                        for _ in range(a.reps):
+                            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                            e0.record(st)
+                            phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
+                            e1.record(st)
+                            e1.synchronize()
+                            ts.append(e0.elapsed_time(e1))
+                        ms = statistics.median(ts)
+                        rec = {"n": n, "slices": s, "bn": bn, "group_rows": gr, "cluster": cl, "ms": round(ms, 3),
+                               "tflops": round(2.0 * n ** 3 / ms / 1e9, 3), "err": errs, "qualifies": ok}
+                        report.append(rec)
+                        print(json.dumps(rec), flush=True)
+                        if ok:
+                            cands.append(rec)
             del W
             torch.cuda.empty_cache()
         if not cands:
@@ -151,16 +158,18 @@ def main() -> int:
             if best_ms is None or ms < best_ms:
                 best_ms, grouped_bn = ms, bn
         os.environ.pop("PHPC_GROUPED_BN", None)
+    for key in ("PHPC_OZAKI_BN", "PHPC_GROUP_ROWS", "PHPC_CLUSTER"):
+        os.environ.pop(key, None)
 
     assert phpc.device_status() == 0
     lines = [f"# written by autotune.py on {torch.cuda.get_device_name()} ({time.strftime('%Y-%m-%d %H:%M UTC', time.gmtime())})",
              f"# target Frobenius error {a.target} / margin {a.margin}, uniform and wide-exponent inputs",
-             "# max_mnk slices bn group_rows   (chosen: ms, FP64-equivalent TFLOP/s, errors)"]
+             "# max_mnk slices bn group_rows cluster   (chosen: ms, FP64-equivalent TFLOP/s, errors)"]
     for i, b in enumerate(table):
         nxt = table[i + 1]["n"] if i + 1 < len(table) else None
         bound = int((b["n"] ** 3 * nxt ** 3) ** 0.5) if nxt else 2 ** 62
         lines.append(f"# N={b['n']}: {b['ms']} ms, {b['tflops']} TFLOP/s, err {b['err']}")
-        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']}")
+        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']} {b['cluster']}")
     lines.append(f"grouped {2 ** 62} {table[-1]['slices'] if table else 7} {grouped_bn}")
     Path(a.out).write_text("\n".join(lines) + "\n")
     print(f"wrote {a.out}")

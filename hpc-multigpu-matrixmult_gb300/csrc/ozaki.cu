@@ -133,7 +133,8 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   const uint32_t bA[3] = {kTcBK, kTcBM, 1};
   const uint64_t dB[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)nplanesB};
   const uint64_t sB[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * n};
-  const uint32_t bB[3] = {kTcBK, (uint32_t)BN, 1};
+  const int cluster = default_cluster(m, k, n);
+  const uint32_t bB[3] = {kTcBK, (uint32_t)(BN / cluster), 1};  // with a 2-CTA cluster each CTA loads half of B
   if (!encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesA, dA, sA, bA, CU_TENSOR_MAP_SWIZZLE_128B) ||
       !encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesB, dB, sB, bB, CU_TENSOR_MAP_SWIZZLE_128B))
     return PHPC_ERR_CUDA;
@@ -149,13 +150,39 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.ea = ea;
   a.eb = eb;
   a.status = device_status_ptr();
-  auto kern = tc_slice_gemm_kernel<BN, MODE>;
+  if (cluster == 1) {
+    auto kern = tc_slice_gemm_kernel<BN, MODE>;
+    if (!tc_regs_ok(reinterpret_cast<const void*>(kern))) return PHPC_ERR_UNSUPPORTED;
+    PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
+    const int ntiles = a.tm * a.tn;
+    const int grid = std::min(ntiles, dev->sm_count);
+    kern<<<grid, kTcThreads, Cfg::kSmem, stream>>>(tmA, tmB, pairs, a, TcGroupTable{});
+    PHPC_CUDA_TRY(cudaGetLastError());
+    return PHPC_OK;
+  }
+  // CTA pairs (2-CTA clusters) computing 256 x BN tiles with M = 256 MMAs.
+  using Cfg2 = TcCfg<BN, 2>;
+  auto kern = tc_slice_gemm_kernel<BN, MODE, false, 2>;
   if (!tc_regs_ok(reinterpret_cast<const void*>(kern))) return PHPC_ERR_UNSUPPORTED;
-  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
-  const int ntiles = a.tm * a.tn;
-  const int grid = std::min(ntiles, dev->sm_count);
-  kern<<<grid, kTcThreads, Cfg::kSmem, stream>>>(tmA, tmB, pairs, a, TcGroupTable{});
-  PHPC_CUDA_TRY(cudaGetLastError());
+  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg2::kSmem));
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kTcThreads, 1, 1);
+  cfg.dynamicSmemBytes = Cfg2::kSmem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int npairs = ((a.tm + 1) / 2) * a.tn;
+  cfg.gridDim = dim3(2 * std::min(npairs, dev->sm_count / 2), 1, 1);
+  int max_clusters = 0;
+  PHPC_CUDA_TRY(cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg));
+  if (max_clusters < 1) return PHPC_ERR_UNSUPPORTED;
+  cfg.gridDim = dim3(2 * std::min(npairs, max_clusters), 1, 1);
+  PHPC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, tmA, tmB, pairs, a, TcGroupTable{}));
   return PHPC_OK;
 }
 

@@ -61,6 +61,7 @@ int default_slices(int m, int k, int n);
 int default_bn(int m, int k, int n);
 int default_grouped_bn(const phpc_gemm_problem* problems, int count);
 int default_group_rows(int m, int k, int n);
+int default_cluster(int m, int k, int n);
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 

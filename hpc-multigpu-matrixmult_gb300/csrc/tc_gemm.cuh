@@ -100,12 +100,16 @@ struct TcJob {
   const int* eb;
 };
 
-template <int BN>
+// Shared-memory plan: a 192 KB ring of K-stages (64 bf16 deep), the epilogue
+// transpose scratch and the barriers. With CLUSTER = 2 (CTA pair, M = 256
+// MMAs) each CTA stages its own 128 rows of A and half of the BN rows of B,
+// so the same ring holds more stages.
+template <int BN, int CLUSTER = 1>
 struct TcCfg {
-  static constexpr int kStages = BN == 256 ? 4 : 6;
   static constexpr int kStageA = kTcBM * kTcBK * 2;
-  static constexpr int kStageB = BN * kTcBK * 2;
+  static constexpr int kStageB = (BN / CLUSTER) * kTcBK * 2;
   static constexpr int kStageBytes = kStageA + kStageB;
+  static constexpr int kStages = (192 * 1024) / kStageBytes;  // 4 / 6 (BN 256, solo / pair), 6 / 8 (BN 128)
   static constexpr int kScratchPerWarp = 32 * 33 * 4;       // 32x32 transpose tile, padded
   static constexpr int kTmemCols = 2 * BN;                  // two accumulator buffers
   static constexpr size_t kSmem =
@@ -124,14 +128,24 @@ __device__ __forceinline__ void tc_tile_coords(int tm, int tn, int group_rows, i
   rm = r0 + w % rows;
 }
 
-template <bool GROUPED>
+// Output tile of work unit t. With CLUSTER = 2 a unit is a 256 x BN tile
+// computed by the CTA pair; CTA `crank` owns its 128-row half, tile row
+// 2 * pair_row + crank (a half beyond the matrix reads zeros and writes
+// nothing).
+template <bool GROUPED, int CLUSTER>
 __device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap* tmA, const CUtensorMap* tmB,
-                                       const TcGroupTable& g, TcJob& j) {
+                                       const TcGroupTable& g, uint32_t crank, TcJob& j) {
   if (!GROUPED) {
     j.M = a.M;
     j.N = a.N;
     j.nk = (a.K + kTcBK - 1) / kTcBK;
-    tc_tile_coords(a.tm, a.tn, a.group_rows, t, j.rm, j.rn);
+    if (CLUSTER == 1) {
+      tc_tile_coords(a.tm, a.tn, a.group_rows, t, j.rm, j.rn);
+    } else {
+      int prow;
+      tc_tile_coords((a.tm + 1) / 2, a.tn, max(1, a.group_rows / 2), t, prow, j.rn);
+      j.rm = 2 * prow + static_cast<int>(crank);
+    }
     j.tmA = tmA;
     j.tmB = tmB;
     j.C = a.C;
@@ -177,14 +191,16 @@ __device__ __forceinline__ double fold_add(double c, int32_t s, int x) {
   return c + ldexp(static_cast<double>(s), x);  // subnormal or overflowing terms
 }
 
-template <int BN, int MODE, bool GROUPED = false>
+template <int BN, int MODE, bool GROUPED = false, int CLUSTER = 1>
 __global__ void __launch_bounds__(kTcThreads, 1)
     tc_slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                          const __grid_constant__ PairList pairs, const __grid_constant__ TcArgs args,
                          const __grid_constant__ TcGroupTable gt) {
-  using Cfg = TcCfg<BN>;
+  static_assert(CLUSTER == 1 || (CLUSTER == 2 && !GROUPED), "the CTA pair computes tiles of one problem");
+  using Cfg = TcCfg<BN, CLUSTER>;
   constexpr int S = Cfg::kStages;
   constexpr int HALF = BN / 2;
+  constexpr uint16_t kPair = 0x3;  // multicast mask: both CTAs of the pair
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* scratch = smem + S * Cfg::kStageBytes;
@@ -196,26 +212,46 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = GROUPED ? gt.ntiles : args.tm * args.tn;
+  // Work units: 128 x BN tiles (CLUSTER = 1) or 256 x BN pair tiles (CLUSTER = 2).
+  const uint32_t crank = CLUSTER > 1 ? cluster_ctarank() : 0u;
+  const bool leader = crank == 0;
+  const int unit0 = CLUSTER > 1 ? static_cast<int>(cluster_id_x()) : static_cast<int>(blockIdx.x);
+  const int ustride = CLUSTER > 1 ? static_cast<int>(nclusters_x()) : static_cast<int>(gridDim.x);
+  const int ntiles = GROUPED ? gt.ntiles : (CLUSTER > 1 ? (args.tm + 1) / 2 : args.tm) * args.tn;
   int* status = args.status;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&full[s], 1);   // pair: the leader's, fed by both CTAs' loads
+      mbar_init(&empty[s], 1);  // pair: the leader's commit, multicast to both CTAs
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], kTcEpiWarps);
+      mbar_init(&tempty[b], CLUSTER * kTcEpiWarps);  // pair: the leader's, released by both CTAs' epilogues
     }
     mbar_init(drain, 1);
     fence_mbar_init();
   }
-  if (warp == 1) tmem_alloc(tmem_slot, Cfg::kTmemCols);
+  if (warp == 1) {
+    if (CLUSTER == 1)
+      tmem_alloc(tmem_slot, Cfg::kTmemCols);
+    else
+      tmem_alloc_pair(tmem_slot, Cfg::kTmemCols);
+  }
   tc_fence_before();
   __syncthreads();
+  if (CLUSTER > 1) cluster_sync();  // peer barriers initialised and TMEM allocated in both CTAs
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
+  bool pair_ok = true;
+  if (CLUSTER > 1) {
+    // The pair's MMAs address the same TMEM columns in both CTAs; refuse to run
+    // (status PHPC_ERR_UNSUPPORTED, site 15) if the allocation differs.
+    const uint32_t peer_base = ld_shared_cluster_u32(mapa_shared(smem_u32(tmem_slot), crank ^ 1u));
+    pair_ok = peer_base == tmem_base;
+    if (!pair_ok && threadIdx.x == 0) record_error(status, PHPC_ERR_UNSUPPORTED | (15 << 8));
+  }
+  const int nunits = pair_ok ? ntiles : 0;
   // Each role's code is dominated by its own setmaxnreg, so the compiler can
   // allocate up to kTcRegsHigh registers in the epilogue branch.
   if (warp < kTcFirstEpiWarp) {
@@ -231,23 +267,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t phase = 0;
       int issued = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      for (int t = unit0; t < nunits && ok; t += ustride) {
         TcJob job;
-        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, job);
+        tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
         for (int pi = 0; pi < pairs.n && ok; ++pi) {
           const int pa = pairs.a[pi], pb = pairs.b[pi];
           for (int kb = 0; kb < job.nk; ++kb) {
             if (!wait_parity(&empty[stage], phase ^ 1, status, 11)) { ok = false; break; }
-            mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
             uint8_t* sa = smem + stage * Cfg::kStageBytes;
-            tma_load_3d(sa, job.tmA, kb * kTcBK, job.rm * kTcBM, pa, &full[stage]);
-            tma_load_3d(sa + Cfg::kStageA, job.tmB, kb * kTcBK, job.rn * BN, pb, &full[stage]);
+            if (CLUSTER == 1) {
+              mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
+              tma_load_3d(sa, job.tmA, kb * kTcBK, job.rm * kTcBM, pa, &full[stage]);
+              tma_load_3d(sa + Cfg::kStageA, job.tmB, kb * kTcBK, job.rn * BN, pb, &full[stage]);
+            } else {
+              // This CTA's 128 rows of A and half of B, into its own shared
+              // memory, counted on the leader's full barrier.
+              const uint32_t bar = mapa_shared(smem_u32(&full[stage]), 0);
+              if (leader) mbar_arrive_expect_tx(&full[stage], 2 * Cfg::kStageBytes);
+              tma_load_3d_pair(sa, job.tmA, kb * kTcBK, job.rm * kTcBM, pa, bar);
+              tma_load_3d_pair(sa + Cfg::kStageA, job.tmB, kb * kTcBK,
+                               job.rn * BN + static_cast<int>(crank) * (BN / 2), pb, bar);
+            }
             ++issued;
             if (++stage == S) { stage = 0; phase ^= 1; }
           }
         }
       }
-      if (!ok) {
+      if (!ok && leader) {  // pair: the leader's full barriers also count the peer's loads
         int s = stage;
         uint32_t ph = phase;
         for (int i = 0; i < min(issued, S); ++i) {
@@ -260,16 +306,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------------ MMA
-    if (lane == 0) {
-      constexpr uint32_t idesc = idesc_bf16_f32(kTcBM, BN);
+    if (lane == 0 && leader) {
+      constexpr uint32_t idesc = idesc_bf16_f32(kTcBM * CLUSTER, BN);
       int stage = 0;
       uint32_t phase = 0;
       uint32_t tphase[2] = {0, 0};
       int buf = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      for (int t = unit0; t < nunits && ok; t += ustride) {
         TcJob job;
-        tc_job<GROUPED>(t, args, &tmA, &tmB, gt, job);
+        tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
         int gstart = 0;
         while (gstart < pairs.n && ok) {
           int gend = gstart + 1;
@@ -291,13 +337,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               const uint64_t adesc = sdesc_kmajor_sw128(sa);
               const uint64_t bdesc = sdesc_kmajor_sw128(sa + Cfg::kStageA);
 #pragma unroll
-              for (int kk = 0; kk < kTcBK / 16; ++kk)
-                tc_mma_bf16(dt, adesc + 2 * kk, bdesc + 2 * kk, idesc, (s > 0 || kk > 0) ? 1u : 0u);
-              tc_commit(&empty[stage]);
+              for (int kk = 0; kk < kTcBK / 16; ++kk) {
+                if (CLUSTER == 1)
+                  tc_mma_bf16(dt, adesc + 2 * kk, bdesc + 2 * kk, idesc, (s > 0 || kk > 0) ? 1u : 0u);
+                else
+                  tc_mma_bf16_pair(dt, adesc + 2 * kk, bdesc + 2 * kk, idesc, (s > 0 || kk > 0) ? 1u : 0u);
+              }
+              if (CLUSTER == 1)
+                tc_commit(&empty[stage]);
+              else
+                tc_commit_pair_multicast(&empty[stage], kPair);
               if (++stage == S) { stage = 0; phase ^= 1; }
             }
             if (!ok) break;
-            tc_commit(&tfull[buf]);
+            if (CLUSTER == 1)
+              tc_commit(&tfull[buf]);
+            else
+              tc_commit_pair_multicast(&tfull[buf], kPair);
             tphase[buf] ^= 1;
             buf ^= 1;
           }
@@ -306,7 +362,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       // Every MMA this thread issued has completed once the drain barrier
       // flips, so TMEM can be released safely even on the error path.
-      tc_commit(drain);
+      if (CLUSTER == 1)
+        tc_commit(drain);
+      else
+        tc_commit_pair(drain);
       const uint32_t daddr = smem_u32(drain);
       const uint64_t t0 = globaltimer_ns();
       while (!mbar_try_wait(daddr, 0) && globaltimer_ns() - t0 < PHPC_WAIT_LIMIT_NS) {}
@@ -326,9 +385,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
     for (int j = 0; j < HALF; ++j) acc[j] = 0;
 
-    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    for (int t = unit0; t < nunits && ok; t += ustride) {
       TcJob job;
-      tc_job<GROUPED>(t, args, &tmA, &tmB, gt, job);
+      tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
       const int64_t row0 = (int64_t)job.rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
       const int col0 = job.rn * BN + half * HALF;                 // first global column of this warp's half
       int my_ea = 0;
@@ -374,7 +433,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           }
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&tempty[buf]);
+          if (lane == 0) {
+            if (CLUSTER == 1)
+              mbar_arrive(&tempty[buf]);
+            else
+              mbar_arrive_cluster(mapa_shared(smem_u32(&tempty[buf]), 0));  // the leader's barrier
+          }
           tphase[buf] ^= 1;
           buf ^= 1;
 
@@ -443,9 +507,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
   tc_fence_before();
   __syncthreads();
+  if (CLUSTER > 1) cluster_sync();  // the pair's MMAs are drained; no peer still signals this CTA
   if (warp == 1) {
     tc_fence_after();
-    tmem_dealloc(tmem_base, Cfg::kTmemCols);
+    if (CLUSTER == 1)
+      tmem_dealloc(tmem_base, Cfg::kTmemCols);
+    else
+      tmem_dealloc_pair(tmem_base, Cfg::kTmemCols);
   }
 }
 

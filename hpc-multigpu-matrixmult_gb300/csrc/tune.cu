@@ -24,6 +24,7 @@ struct TuneEntry {
   int slices;
   int bn;
   int group_rows;     // L2 raster height of the persistent tile order (0 = default 8)
+  int cluster;        // CTAs per cluster sharing B (1 or 2; 0 = default 1)
 };
 
 std::once_flag g_once;
@@ -40,7 +41,7 @@ std::string library_dir() {
   return ".";
 }
 
-// Table format (text): one entry per line, "max_mnk slices bn [group_rows]"
+// Table format (text): one entry per line, "max_mnk slices bn [group_rows [cluster]]"
 // for single problems or "grouped max_mean_mnk slices bn" for grouped calls;
 // '#' starts a comment line. Written by autotune.py.
 void load_table() {
@@ -58,9 +59,10 @@ void load_table() {
         g_grouped.push_back(e);
       continue;
     }
-    const int got = sscanf(line, "%lld %d %d %d", &e.max_mnk, &e.slices, &e.bn, &e.group_rows);
+    const int got = sscanf(line, "%lld %d %d %d %d", &e.max_mnk, &e.slices, &e.bn, &e.group_rows, &e.cluster);
     if (got >= 3 && e.slices >= 2 && e.slices <= 8 && (e.bn == 128 || e.bn == 256)) {
       if (got < 4 || e.group_rows < 1 || e.group_rows > 64) e.group_rows = 0;
+      if (got < 5 || (e.cluster != 1 && e.cluster != 2)) e.cluster = 0;
       g_table.push_back(e);
     }
   }
@@ -95,6 +97,16 @@ int default_bn(int m, int k, int n) {
   }
   if (const TuneEntry* e = lookup(m, k, n)) return e->bn;
   return 256;
+}
+
+// CTAs per cluster of the single-problem slice GEMM (1, or 2 = B multicast
+// between vertically adjacent tiles): PHPC_CLUSTER, else the table, else 1.
+int default_cluster(int m, int k, int n) {
+  const char* env = getenv("PHPC_CLUSTER");
+  if (env && (atoi(env) == 1 || atoi(env) == 2)) return atoi(env);
+  if (const TuneEntry* e = lookup(m, k, n))
+    if (e->cluster == 2) return 2;
+  return 1;
 }
 
 int default_group_rows(int m, int k, int n) {

@@ -75,3 +75,15 @@ def test_workspace_validation(phpc, torch_cuda):
     with pytest.raises(phpc.PhpcError) as e:
         phpc.sgemm_bf16x3_dev(64, 64, 64, A, 64, A, 64, A, 64, W, 16)
     assert e.value.code == 6
+
+
+def test_cta_pair_same_bits(phpc, torch_cuda, monkeypatch):
+    rng = np.random.default_rng(12)
+    a = rng.standard_normal((700, 1000)).astype(np.float32)
+    b = rng.standard_normal((1000, 600)).astype(np.float32)
+    c0 = np.zeros((700, 600), np.float32)
+    monkeypatch.setenv("PHPC_CLUSTER", "1")
+    one = run(phpc, torch_cuda, "bf16x3", a, b, c0)
+    monkeypatch.setenv("PHPC_CLUSTER", "2")
+    two = run(phpc, torch_cuda, "bf16x3", a, b, c0)
+    np.testing.assert_array_equal(one, two)

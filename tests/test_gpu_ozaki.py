@@ -143,3 +143,19 @@ def test_workspace_and_slices_validation(phpc, torch_cuda):
     with pytest.raises(phpc.PhpcError) as e:
         phpc.dgemm_ozaki_dev(64, 64, 64, A, 64, A, 64, A, 64, 1, W, 16)
     assert e.value.code == 1
+
+
+@pytest.mark.parametrize("s", [3, 7])
+@pytest.mark.parametrize("m,k,n", [(128, 64, 256), (300, 700, 520), (7, 13, 5), (130, 2500, 260), (640, 1024, 768)])
+@pytest.mark.parametrize("bn", ["128", "256"])
+def test_bitexact_vs_model_cta_pair(phpc, torch_cuda, monkeypatch, s, m, k, n, bn):
+    """CTA pairs (2-CTA clusters, M = 256 tcgen05 MMAs over both CTAs' shared
+    memory); odd tile-row counts leave a zero-filled half."""
+    monkeypatch.setenv("PHPC_CLUSTER", "2")
+    monkeypatch.setenv("PHPC_OZAKI_BN", bn)
+    rng = np.random.default_rng(s * 31 + m + k + n)
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+    b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-20, 21, (k, n)))
+    c0 = rng.uniform(-1, 1, (m, n))
+    got = run_dev(phpc, torch_cuda, a, b, c0, s)
+    np.testing.assert_array_equal(got, ozaki_model.gemm(a, b, c0, s))

@@ -44,5 +44,7 @@ def test_committed_table_is_well_formed():
     lines = [ln for ln in (PKG / "tune_table.txt").read_text().splitlines() if ln and not ln.startswith("#")]
     assert lines[-1].startswith("grouped ")
     for ln in lines[:-1]:
-        mnk, s, bn, gr = (int(x) for x in ln.split())
+        f = [int(x) for x in ln.split()]
+        mnk, s, bn, gr = f[:4]
         assert 2 <= s <= 8 and bn in (128, 256) and 1 <= gr <= 64
+        assert len(f) == 4 or f[4] in (1, 2)
