@@ -25,7 +25,7 @@ namespace phpc {
 template <int BN, int MODE>
 int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
                          int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream);
+                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane);
 
 namespace {
 
@@ -239,8 +239,10 @@ extern "C" int phpc_sgemm_bf16x3_dev(int m, int k, int n, const float* dA, int64
       } else {
         const PairList pl = bf16x3_pairs();
         rc = default_bn(m, k, n) == 128
-                 ? launch_tc_slice_gemm<128, kF32>(pa, pb, 3, 3, L.ldp, m, n, k, pl, dC, ldc, nullptr, nullptr, st)
-                 : launch_tc_slice_gemm<256, kF32>(pa, pb, 3, 3, L.ldp, m, n, k, pl, dC, ldc, nullptr, nullptr, st);
+                 ? launch_tc_slice_gemm<128, kF32>(pa, pb, 3, 3, L.ldp, m, n, k, pl, dC, ldc, nullptr, nullptr, st,
+                                                   nullptr, 0, 0)
+                 : launch_tc_slice_gemm<256, kF32>(pa, pb, 3, 3, L.ldp, m, n, k, pl, dC, ldc, nullptr, nullptr, st,
+                                                   nullptr, 0, 0);
       }
     }
   }

@@ -37,33 +37,6 @@ namespace phpc {
 
 namespace {
 
-// One warp per row of A: ea[i] = max_k e(A[i][k]).
-__global__ void scan_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K, int* __restrict__ ea,
-                                 int* status) {
-  const int warps = blockDim.x >> 5;
-  const int64_t row = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
-  if (row >= M) return;
-  scan_row_warp(A + row * lda, K, ea + row, status);
-}
-
-// eb[j] = max_k e(B[k][j]); eb is pre-filled with kExpZero, blockIdx.y splits K.
-__global__ void scan_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N, int krows,
-                                 int* __restrict__ eb, int* status) {
-  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= N) return;
-  const int k0 = blockIdx.y * krows, k1 = min(K, k0 + krows);
-  int e = kExpZero;
-  bool nf = false;
-  for (int k = k0; k < k1; ++k) e = max(e, exponent_of(B[(int64_t)k * ldb + col], nf));
-  if (e > kExpZero) atomicMax(&eb[col], e);
-  if (nf) record_error(status, PHPC_ERR_NONFINITE);
-}
-
-__global__ void fill_int_kernel(int* p, int n, int v) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = v;
-}
-
 // A planes [s][M][ldp]: blockIdx.x = row, each thread 8 consecutive k.
 __global__ void split_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K, const int* __restrict__ ea,
                                   int s, uint16_t* __restrict__ planes, int64_t ldp, int64_t plane_stride) {
@@ -123,7 +96,7 @@ PairList ozaki_pairs(int s) {
 template <int BN, int MODE>
 int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
                          int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane) {
   using Cfg = TcCfg<BN>;
   const DeviceInfo* dev = current_device();
   if (!dev) return PHPC_ERR_CUDA;
@@ -150,6 +123,9 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.ea = ea;
   a.eb = eb;
   a.status = device_status_ptr();
+  a.R = R;
+  a.ldr = ldr;
+  a.rplane = rplane;
   if (cluster == 1) {
     auto kern = tc_slice_gemm_kernel<BN, MODE>;
     if (!tc_regs_ok(reinterpret_cast<const void*>(kern))) return PHPC_ERR_UNSUPPORTED;
@@ -186,10 +162,15 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   return PHPC_OK;
 }
 
-template int launch_tc_slice_gemm<256, kF32>(const void*, const void*, int, int, int64_t, int, int, int,
-                                              const PairList&, void*, int64_t, const int*, const int*, cudaStream_t);
-template int launch_tc_slice_gemm<128, kF32>(const void*, const void*, int, int, int64_t, int, int, int,
-                                              const PairList&, void*, int64_t, const int*, const int*, cudaStream_t);
+#define PHPC_INSTANTIATE_TC(BN, MODE)                                                                         \
+  template int launch_tc_slice_gemm<BN, MODE>(const void*, const void*, int, int, int64_t, int, int, int,         \
+                                              const PairList&, void*, int64_t, const int*, const int*, cudaStream_t, \
+                                              uint8_t*, int64_t, int64_t);
+PHPC_INSTANTIATE_TC(256, kF32)
+PHPC_INSTANTIATE_TC(128, kF32)
+PHPC_INSTANTIATE_TC(256, kResidue)
+PHPC_INSTANTIATE_TC(128, kResidue)
+#undef PHPC_INSTANTIATE_TC
 
 size_t ozaki_workspace_bytes(int m, int k, int n, int s) { return ozaki_layout(m, k, n, s).total; }
 
@@ -244,8 +225,8 @@ int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const vo
   const void* pb = base + L.off_pb;
   const PairList pl = ozaki_pairs(s);
   if (bn == 128)
-    return launch_tc_slice_gemm<128, kOzaki>(pa, pb, s, s, L.ldp, m, n, k, pl, dC, ldc, ea, eb, stream);
-  return launch_tc_slice_gemm<256, kOzaki>(pa, pb, s, s, L.ldp, m, n, k, pl, dC, ldc, ea, eb, stream);
+    return launch_tc_slice_gemm<128, kOzaki>(pa, pb, s, s, L.ldp, m, n, k, pl, dC, ldc, ea, eb, stream, nullptr, 0, 0);
+  return launch_tc_slice_gemm<256, kOzaki>(pa, pb, s, s, L.ldp, m, n, k, pl, dC, ldc, ea, eb, stream, nullptr, 0, 0);
 }
 
 int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,

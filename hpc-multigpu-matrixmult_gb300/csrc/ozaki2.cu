@@ -1,0 +1,402 @@
+// FP64-accurate GEMM by the modular (Chinese-remainder) Ozaki scheme on
+// tcgen05 BF16 tensor cores.
+//
+// C += A * B (the reference's semantics, src/phpc_gemm.cu:55) computed as:
+//  1. Exponent scans, as in ozaki.cu: ea[i] = max_k e(A[i][k]),
+//     eb[j] = max_k e(B[k][j]).
+//  2. Residue split (integer only): each element becomes the integer
+//     A'[i][k] = sign * round(|A[i][k]| * 2^(b - ea[i])), |A'| <= 2^b (B'
+//     likewise with eb[j]), and then its symmetric residues modulo n pairwise
+//     coprime moduli m_1..m_n <= 256: integers in [-128, 127], exact in BF16.
+//     Planes A_i = [n][M][ldp], B_i = [n][N][ldp] (transposed, K-major).
+//  3. n residue GEMMs on the tcgen05 engine (tc_gemm.cuh, kResidue): the exact
+//     int32 sum of A_i * B_i^T (f32 chunks of 1024 products, as in the digit
+//     scheme) reduced mod m_i, one byte per element, into plane i of R.
+//  4. CRT (this file): C_int = sum_i r_i * W_i mod M, W_i = (M/m_i) *
+//     ((M/m_i)^-1 mod m_i), M = prod m_i, in 160-bit integer arithmetic;
+//     b is the largest width with 2 * K * 2^(2b) < M, so the symmetric
+//     representative of C_int is the exact integer product A' * B'^T.
+//     C += round_to_double(C_int) * 2^(ea[i] + eb[j] - 2b).
+//
+// Compared with the digit scheme (s slices, s(s+1)/2 slice products) the
+// tensor-core work is n GEMMs with no triangular truncation: n = 16 gives
+// b = 55 at K = 16384, the grid of 7 digits, for 16 GEMMs instead of 28.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+
+#include "ozaki_digits.cuh"
+#include "phpc_host.hpp"
+#include "tc_gemm.cuh"
+
+namespace phpc {
+
+template <int BN, int MODE>
+int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
+                         int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
+                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane);
+
+namespace {
+
+constexpr int kMaxModuli = 16;  // M < 2^126: weights in four 32-bit limbs, sums in five
+constexpr int kMinModuli = 8;
+// Pairwise coprime, largest first: 256 = 2^8, 255 = 3 5 17, 253 = 11 23, 247 = 13 19, the rest prime.
+constexpr uint32_t kModuli[kMaxModuli] = {256, 255, 253, 251, 247, 241, 239, 233,
+                                          229, 227, 223, 211, 199, 197, 193, 191};
+
+struct ModTable {
+  int n;     // number of moduli
+  int bits;  // b: operands are integers of magnitude <= 2^b
+  uint32_t m[kMaxModuli];
+  uint32_t magic[kMaxModuli];  // floor(2^32 / m)
+  uint32_t c21[kMaxModuli];    // 2^21 mod m
+  uint32_t c42[kMaxModuli];    // 2^42 mod m
+  uint32_t W[kMaxModuli][4];   // CRT weights, little-endian 32-bit limbs
+  uint32_t M[4];               // product of the moduli
+  uint32_t Mhalf[4];           // floor(M / 2)
+  int qlimb;                   // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
+  float Mtop;                  // (M >> 32 qlimb) as a float
+};
+
+using u128 = unsigned __int128;
+
+ModTable make_table(int nmod, int k) {
+  ModTable T{};
+  T.n = nmod;
+  u128 M = 1;
+  double log_m = 0;
+  for (int i = 0; i < nmod; ++i) {
+    M *= kModuli[i];
+    log_m += std::log2(static_cast<double>(kModuli[i]));
+  }
+  int log_k = 1;
+  while ((1ll << log_k) < k) ++log_k;
+  T.bits = std::min(62, static_cast<int>(std::floor((log_m - 1.0 - log_k) / 2.0 - 1e-9)));
+  for (int i = 0; i < nmod; ++i) {
+    const uint32_t m = kModuli[i];
+    T.m[i] = m;
+    T.magic[i] = static_cast<uint32_t>((1ull << 32) / m);
+    T.c21[i] = static_cast<uint32_t>((1ull << 21) % m);
+    T.c42[i] = static_cast<uint32_t>((1ull << 42) % m);
+    const u128 Mi = M / m;
+    const uint32_t mi_mod = static_cast<uint32_t>(Mi % m);
+    uint32_t inv = 0;
+    for (uint32_t v = 1; v < m; ++v)
+      if ((static_cast<uint64_t>(mi_mod) * v) % m == 1) { inv = v; break; }
+    const u128 W = Mi * inv;  // < M
+    for (int l = 0; l < 4; ++l) T.W[i][l] = static_cast<uint32_t>(W >> (32 * l));
+  }
+  for (int l = 0; l < 4; ++l) {
+    T.M[l] = static_cast<uint32_t>(M >> (32 * l));
+    T.Mhalf[l] = static_cast<uint32_t>((M >> 1) >> (32 * l));
+  }
+  int bitlen = 0;
+  while (bitlen < 128 && (M >> bitlen) != 0) ++bitlen;
+  T.qlimb = std::max(0, (bitlen - 20) / 32);
+  T.Mtop = static_cast<float>(static_cast<double>(static_cast<uint64_t>(M >> (32 * T.qlimb))));
+  return T;
+}
+
+// Symmetric residues of sign * X modulo each modulus, X < 2^63 given as three
+// 21-bit limbs (X mod m = L2 * (2^42 mod m) + L1 * (2^21 mod m) + L0, mod m).
+__device__ __forceinline__ int residue_of(uint32_t L0, uint32_t L1, uint32_t L2, bool neg, const ModTable& T,
+                                          int i) {
+  const uint32_t m = T.m[i];
+  const uint32_t t = L2 * T.c42[i] + L1 * T.c21[i] + L0;  // < 2^31
+  uint32_t r = mod_small(t, m, T.magic[i]);
+  if (neg && r) r = m - r;
+  int v = static_cast<int>(r);
+  if (2 * r >= m) v -= static_cast<int>(m);  // [-(m/2), (m-1)/2]: |v| <= 128
+  return v;
+}
+
+__device__ __forceinline__ void limbs21(uint64_t X, uint32_t& L0, uint32_t& L1, uint32_t& L2) {
+  L0 = static_cast<uint32_t>(X & 0x1FFFFF);
+  L1 = static_cast<uint32_t>((X >> 21) & 0x1FFFFF);
+  L2 = static_cast<uint32_t>(X >> 42);
+}
+
+// A residue planes [n][M][ldp]: blockIdx.x = row, each thread 8 consecutive k.
+__global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K,
+                                    const int* __restrict__ ea, const __grid_constant__ ModTable T,
+                                    uint16_t* __restrict__ planes, int64_t ldp, int64_t plane_stride) {
+  const int64_t row = blockIdx.x;
+  const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
+  if (row >= M || k0 >= ldp) return;
+  const int e = ea[row];
+  const double* a = A + row * lda;
+  uint32_t L0[8], L1[8], L2[8];
+  bool neg[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint64_t X = fixed_point(k0 + j < K ? a[k0 + j] : 0.0, e, T.bits, neg[j]);
+    limbs21(X, L0[j], L1[j], L2[j]);
+  }
+  uint16_t* out = planes + row * ldp + k0;
+  for (int i = 0; i < T.n; ++i) {
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 8; j += 2)
+      w[j >> 1] = static_cast<uint32_t>(bf16_bits_of_int(residue_of(L0[j], L1[j], L2[j], neg[j], T, i))) |
+                  (static_cast<uint32_t>(bf16_bits_of_int(residue_of(L0[j + 1], L1[j + 1], L2[j + 1], neg[j + 1], T, i)))
+                   << 16);
+    *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// B residue planes, transposed ([n][N][ldp]): one 32 (k) x 64 (j) block per
+// CTA; the residues are staged through shared memory 8 planes at a time.
+__global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
+                                                           const int* __restrict__ eb,
+                                                           const __grid_constant__ ModTable T,
+                                                           uint16_t* __restrict__ planes, int64_t ldp,
+                                                           int64_t plane_stride) {
+  __shared__ uint32_t st[8][64][17];
+  const int j = threadIdx.x & 63;
+  const int kp0 = threadIdx.x >> 6;  // 0..3
+  const int64_t k0 = (int64_t)blockIdx.y * 32;
+  const int64_t j0 = (int64_t)blockIdx.x * 64;
+  const int64_t col = j0 + j;
+  const int e = col < N ? eb[col] : kExpZero;
+  uint32_t L0[8], L1[8], L2[8];
+  bool neg[8];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {  // k pairs kp0, kp0 + 4, ...: elements 2u, 2u + 1
+    const int64_t k = k0 + 2 * (kp0 + 4 * u);
+    const uint64_t X0 = fixed_point((col < N && k < K) ? B[k * ldb + col] : 0.0, e, T.bits, neg[2 * u]);
+    const uint64_t X1 = fixed_point((col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0, e, T.bits, neg[2 * u + 1]);
+    limbs21(X0, L0[2 * u], L1[2 * u], L2[2 * u]);
+    limbs21(X1, L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1]);
+  }
+  const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;
+  const int64_t gj = j0 + wj, gk = k0 + 8 * q;
+  for (int i0 = 0; i0 < T.n; i0 += 8) {
+    const int cnt = min(8, T.n - i0);
+    for (int p = 0; p < cnt; ++p) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        st[p][j][kp0 + 4 * u] =
+            static_cast<uint32_t>(bf16_bits_of_int(residue_of(L0[2 * u], L1[2 * u], L2[2 * u], neg[2 * u], T, i0 + p))) |
+            (static_cast<uint32_t>(
+                 bf16_bits_of_int(residue_of(L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1], neg[2 * u + 1], T, i0 + p)))
+             << 16);
+    }
+    __syncthreads();
+    if (gj < N && gk < ldp)
+      for (int p = 0; p < cnt; ++p)
+        *reinterpret_cast<uint4*>(planes + (int64_t)(i0 + p) * plane_stride + gj * ldp + gk) =
+            make_uint4(st[p][wj][4 * q], st[p][wj][4 * q + 1], st[p][wj][4 * q + 2], st[p][wj][4 * q + 3]);
+    __syncthreads();
+  }
+}
+
+// c + v * 2^x for a double v and an int x, one rounding (the scaling is exact
+// unless the result leaves the normal range).
+__device__ __forceinline__ double add_scaled(double c, double v, int x) {
+  const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(v));
+  const int E = static_cast<int>((bits >> 52) & 0x7FF) + x;
+  if (E >= 1 && E <= 2046)
+    return c + __longlong_as_double(static_cast<long long>((bits & ~(0x7FFull << 52)) | (static_cast<uint64_t>(E) << 52)));
+  return c + ldexp(v, x);
+}
+
+// C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
+__global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
+                                                  int N, const int* __restrict__ ea, const int* __restrict__ eb,
+                                                  const __grid_constant__ ModTable T, double* __restrict__ C,
+                                                  int64_t ldc) {
+  const int64_t row = blockIdx.x;
+  const int64_t col = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
+  if (row >= M || col >= N) return;
+  // acc = sum r_i W_i: 32-bit limbs accumulated in 64 bits (no overflow: 16 x 2^8 x 2^32 < 2^45)
+  uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+  const uint8_t* rp = R + row * ldr + col;
+  for (int i = 0; i < T.n; ++i) {
+    const uint64_t r = rp[i * rplane];
+    a0 += r * T.W[i][0];
+    a1 += r * T.W[i][1];
+    a2 += r * T.W[i][2];
+    a3 += r * T.W[i][3];
+  }
+  uint32_t l[5];
+  uint64_t t = a0;
+  l[0] = static_cast<uint32_t>(t);
+  t = (t >> 32) + a1;
+  l[1] = static_cast<uint32_t>(t);
+  t = (t >> 32) + a2;
+  l[2] = static_cast<uint32_t>(t);
+  t = (t >> 32) + a3;
+  l[3] = static_cast<uint32_t>(t);
+  l[4] = static_cast<uint32_t>(t >> 32);
+  // q = floor(acc / M) < 2^12 (acc < 16 * 256 * M), estimated in single
+  // precision from the 64 bits at limb qlimb (acc >> 32 qlimb < 2^64), then
+  // corrected by at most one in either direction below
+  const float top = static_cast<float>((static_cast<uint64_t>(l[T.qlimb + 1]) << 32) | l[T.qlimb]);
+  uint32_t q = static_cast<uint32_t>(top / T.Mtop);
+  // r = acc - q M (160-bit, two's complement)
+  uint32_t rr[5];
+  uint64_t carry = 0, borrow = 0;
+  for (int w = 0; w < 5; ++w) {
+    const uint64_t pm = (w < 4 ? static_cast<uint64_t>(T.M[w]) * q : 0) + carry;
+    carry = pm >> 32;
+    const uint64_t sub = static_cast<uint64_t>(l[w]) - static_cast<uint32_t>(pm) - borrow;
+    rr[w] = static_cast<uint32_t>(sub);
+    borrow = (sub >> 63) & 1;
+  }
+  // negative: add M back (q was one too large)
+  if (rr[4] & 0x80000000u) {
+    uint64_t c2 = 0;
+    for (int w = 0; w < 5; ++w) {
+      const uint64_t s = static_cast<uint64_t>(rr[w]) + (w < 4 ? T.M[w] : 0) + c2;
+      rr[w] = static_cast<uint32_t>(s);
+      c2 = s >> 32;
+    }
+  }
+  // r >= M: subtract M (q was one too small)
+  auto geq_M = [&]() {
+    if (rr[4]) return true;
+    for (int w = 3; w >= 0; --w)
+      if (rr[w] != T.M[w]) return rr[w] > T.M[w];
+    return true;
+  };
+  if (geq_M()) {
+    uint64_t b2 = 0;
+    for (int w = 0; w < 5; ++w) {
+      const uint64_t s = static_cast<uint64_t>(rr[w]) - (w < 4 ? T.M[w] : 0) - b2;
+      rr[w] = static_cast<uint32_t>(s);
+      b2 = (s >> 63) & 1;
+    }
+  }
+  // symmetric representative: r > M/2 -> r - M (negative), magnitude M - r
+  bool gt_half = false;
+  for (int w = 3; w >= 0; --w)
+    if (rr[w] != T.Mhalf[w]) { gt_half = rr[w] > T.Mhalf[w]; break; }
+  bool neg = false;
+  uint32_t x[4] = {rr[0], rr[1], rr[2], rr[3]};
+  if (gt_half) {
+    neg = true;
+    uint64_t b2 = 0;
+    for (int w = 0; w < 4; ++w) {
+      const uint64_t s = static_cast<uint64_t>(T.M[w]) - x[w] - b2;
+      x[w] = static_cast<uint32_t>(s);
+      b2 = (s >> 63) & 1;
+    }
+  }
+  double* cp = C + row * ldc + col;
+  const uint64_t hi = (static_cast<uint64_t>(x[3]) << 32) | x[2];
+  const uint64_t lo = (static_cast<uint64_t>(x[1]) << 32) | x[0];
+  if (hi == 0 && lo == 0) {
+    *cp = *cp + 0.0;
+    return;
+  }
+  double v;
+  int shift;
+  if (hi == 0) {
+    v = __ull2double_rn(lo);
+    shift = 0;
+  } else {
+    // round the 128-bit magnitude to 53 bits once: its top 64 bits plus a
+    // sticky bit for everything below them, converted with round-to-nearest
+    const int lz = __clzll(static_cast<long long>(hi));
+    const uint64_t topbits = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    const uint64_t rest = lz ? (lo << lz) : lo;
+    v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
+    shift = 64 - lz;
+  }
+  if (neg) v = -v;
+  *cp = add_scaled(*cp, v, shift + max(ea[row], -20000) + max(eb[col], -20000) - 2 * T.bits);
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Ozaki2Layout {
+  int64_t ldp, ldr;
+  size_t off_ea, off_eb, off_pa, off_pb, off_r, total;
+};
+
+Ozaki2Layout ozaki2_layout(int m, int k, int n, int nmod) {
+  Ozaki2Layout L;
+  L.ldp = ((int64_t)k + 7) / 8 * 8;
+  L.ldr = ((int64_t)n + 15) / 16 * 16;
+  L.off_ea = 0;
+  L.off_eb = align256(sizeof(int) * (size_t)m);
+  L.off_pa = align256(L.off_eb + sizeof(int) * (size_t)n);
+  L.off_pb = align256(L.off_pa + (size_t)nmod * m * L.ldp * 2);
+  L.off_r = align256(L.off_pb + (size_t)nmod * n * L.ldp * 2);
+  L.total = align256(L.off_r + (size_t)nmod * m * L.ldr);
+  return L;
+}
+
+}  // namespace
+
+size_t ozaki2_workspace_bytes(int m, int k, int n, int nmod) { return ozaki2_layout(m, k, n, nmod).total; }
+
+int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
+                 int64_t ldc, int nmod, void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
+  const DeviceInfo* dev = current_device();
+  if (!dev) return PHPC_ERR_CUDA;
+  if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
+  const Ozaki2Layout L = ozaki2_layout(m, k, n, nmod);
+  if (!ws || ws_bytes < L.total || !aligned16(ws)) return PHPC_ERR_WORKSPACE;
+  const ModTable T = make_table(nmod, k);
+  uint8_t* base = static_cast<uint8_t*>(ws);
+  int* ea = reinterpret_cast<int*>(base + L.off_ea);
+  int* eb = reinterpret_cast<int*>(base + L.off_eb);
+  uint16_t* pa = reinterpret_cast<uint16_t*>(base + L.off_pa);
+  uint16_t* pb = reinterpret_cast<uint16_t*>(base + L.off_pb);
+  uint8_t* R = base + L.off_r;
+  int* status = device_status_ptr();
+
+  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream>>>(dA, lda, m, k, ea, status);
+  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(eb, n, kExpZero);
+  scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream>>>(dB, ldb, k, n, 256, eb, status);
+  residue_rows_kernel<<<dim3(m, ceil_div(L.ldp / 8, 128)), 128, 0, stream>>>(dA, lda, m, k, ea, T, pa, L.ldp,
+                                                                              (int64_t)m * L.ldp);
+  residue_cols_kernel<<<dim3(ceil_div(n, 64), ceil_div(k, 32)), 256, 0, stream>>>(dB, ldb, k, n, eb, T, pb, L.ldp,
+                                                                                  (int64_t)n * L.ldp);
+  PHPC_CUDA_TRY(cudaGetLastError());
+  PairList pl{};
+  pl.n = nmod;
+  for (int i = 0; i < nmod; ++i) {
+    pl.a[i] = static_cast<uint8_t>(i);
+    pl.b[i] = static_cast<uint8_t>(i);
+    pl.g[i] = static_cast<uint8_t>(i);
+    pl.mod[i] = static_cast<uint16_t>(T.m[i]);
+    pl.magic[i] = T.magic[i];
+  }
+  const int64_t rplane = (int64_t)m * L.ldr;
+  const int rc = bn == 128 ? launch_tc_slice_gemm<128, kResidue>(pa, pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
+                                                                  nullptr, nullptr, stream, R, L.ldr, rplane)
+                           : launch_tc_slice_gemm<256, kResidue>(pa, pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
+                                                                  nullptr, nullptr, stream, R, L.ldr, rplane);
+  if (rc != PHPC_OK) return rc;
+  crt_kernel<<<dim3(m, ceil_div(n, 128)), 128, 0, stream>>>(R, L.ldr, rplane, m, n, ea, eb, T, dC, ldc);
+  PHPC_CUDA_TRY(cudaGetLastError());
+  return PHPC_OK;
+}
+
+}  // namespace phpc
+
+extern "C" size_t phpc_ozaki2_workspace_bytes(int m, int k, int n, int moduli) {
+  if (m <= 0 || k <= 0 || n <= 0 || moduli < phpc::kMinModuli || moduli > phpc::kMaxModuli) return 0;
+  return phpc::ozaki2_workspace_bytes(m, k, n, moduli);
+}
+
+extern "C" int phpc_dgemm_ozaki2_dev(int m, int k, int n, const double* dA, int64_t lda, const double* dB,
+                                     int64_t ldb, double* dC, int64_t ldc, int moduli, void* workspace,
+                                     size_t workspace_bytes, void* stream) {
+  using namespace phpc;
+  int rc;
+  if (m < 0 || k < 0 || n < 0 || moduli < kMinModuli || moduli > kMaxModuli) {
+    rc = PHPC_ERR_ARG;
+  } else if (m == 0 || n == 0 || k == 0) {
+    rc = PHPC_OK;
+  } else if (!dA || !dB || !dC || lda < k || ldb < n || ldc < n || m > 65535 * 128) {
+    rc = PHPC_ERR_ARG;
+  } else {
+    rc = dgemm_ozaki2(m, k, n, dA, lda, dB, ldb, dC, ldc, moduli, workspace, workspace_bytes,
+                      static_cast<cudaStream_t>(stream), default_bn(m, k, n));
+  }
+  set_last_error(rc);
+  return rc;
+}

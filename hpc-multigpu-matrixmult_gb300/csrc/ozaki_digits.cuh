@@ -31,9 +31,12 @@ __device__ __forceinline__ int warp_max(int v) {
 // Balanced base-256 digits of round(|x| * 2^(P - e)), P = 8s - 1, most
 // significant first, with the sign of x applied. Non-finite and zero inputs
 // give all-zero digits.
-__device__ __forceinline__ void split_digits(double x, int e, int s, int (&d)[8]) {
+// |x| on the fixed-point grid of its row/column: X = round-half-up(|x| *
+// 2^(P - e)) <= 2^P (P <= 63), with the sign of x in *neg. Zero, non-finite
+// values and all-zero rows/columns give X = 0.
+__device__ __forceinline__ uint64_t fixed_point(double x, int e, int P, bool& neg) {
   uint64_t b = static_cast<uint64_t>(__double_as_longlong(x));
-  const bool neg = (b >> 63) != 0;
+  neg = (b >> 63) != 0;
   b &= 0x7FFFFFFFFFFFFFFFull;
   const int E = static_cast<int>(b >> 52);
   uint64_t m = b & 0x000FFFFFFFFFFFFFull;
@@ -47,13 +50,16 @@ __device__ __forceinline__ void split_digits(double x, int e, int s, int (&d)[8]
   } else {
     elsb = -1074;
   }
-  const int P = 8 * s - 1;
   const int sh = elsb + P - e;
-  uint64_t X;
-  if (m == 0) X = 0;
-  else if (sh >= 0) X = m << sh;  // |x| < 2^e  =>  X < 2^P <= 2^63
-  else if (sh > -64) X = (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
-  else X = 0;
+  if (m == 0) return 0;
+  if (sh >= 0) return m << sh;  // |x| < 2^e  =>  X < 2^P <= 2^63
+  if (sh > -64) return (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
+  return 0;
+}
+
+__device__ __forceinline__ void split_digits(double x, int e, int s, int (&d)[8]) {
+  bool neg;
+  uint64_t X = fixed_point(x, e, 8 * s - 1, neg);
 #pragma unroll
   for (int p = 7; p >= 1; --p) {
     if (p < s) {
@@ -75,6 +81,7 @@ __device__ __forceinline__ void split_digits(double x, int e, int s, int (&d)[8]
 __device__ __forceinline__ uint16_t bf16_bits_of_int(int v) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(static_cast<float>(v)));
 }
+
 
 // Warp-cooperative scan of one row: *out = max_k e(a[k]); flags inf/NaN.
 __device__ __forceinline__ void scan_row_warp(const double* __restrict__ a, int K, int* out, int* status) {
@@ -143,5 +150,37 @@ __device__ __forceinline__ void split_col_block(const double* __restrict__ B, in
     *reinterpret_cast<uint4*>(planes + p * plane_stride + gj * ldp + gk) =
         make_uint4(st[p][wj][4 * q], st[p][wj][4 * q + 1], st[p][wj][4 * q + 2], st[p][wj][4 * q + 3]);
 }
+
+// Exponent scans (one warp per row of A; column blocks of B) shared by the
+// digit and the modular Ozaki GEMMs.
+namespace {
+// One warp per row of A: ea[i] = max_k e(A[i][k]).
+__global__ void scan_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K, int* __restrict__ ea,
+                                 int* status) {
+  const int warps = blockDim.x >> 5;
+  const int64_t row = (int64_t)blockIdx.x * warps + (threadIdx.x >> 5);
+  if (row >= M) return;
+  scan_row_warp(A + row * lda, K, ea + row, status);
+}
+
+// eb[j] = max_k e(B[k][j]); eb is pre-filled with kExpZero, blockIdx.y splits K.
+__global__ void scan_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N, int krows,
+                                 int* __restrict__ eb, int* status) {
+  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= N) return;
+  const int k0 = blockIdx.y * krows, k1 = min(K, k0 + krows);
+  int e = kExpZero;
+  bool nf = false;
+  for (int k = k0; k < k1; ++k) e = max(e, exponent_of(B[(int64_t)k * ldb + col], nf));
+  if (e > kExpZero) atomicMax(&eb[col], e);
+  if (nf) record_error(status, PHPC_ERR_NONFINITE);
+}
+
+__global__ void fill_int_kernel(int* p, int n, int v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
+}  // namespace
 
 }  // namespace phpc

@@ -50,6 +50,9 @@ int dgemm_dmma(int m, int k, int n, const double* dA, int64_t lda, const double*
 int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
                 int64_t ldc, int s, void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
 size_t ozaki_workspace_bytes(int m, int k, int n, int s);
+size_t ozaki2_workspace_bytes(int m, int k, int n, int nmod);
+int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
+                 int64_t ldc, int nmod, void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
 int ozaki_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
                    size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b);
 int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const void* ws, size_t ws_bytes,

@@ -11,6 +11,10 @@
 //          per-thread int32 registers. At the end of a group (or after 127
 //          chunks, before int32 could overflow) it folds the integer sums into
 //          the FP64 output: C[i][j] += S * 2^(ea[i] + eb[j] + 2 - 8g).
+//  kResidue Modular Ozaki GEMM: pair i multiplies the residue planes of
+//          modulus m_i; its exact int32 sum (f32 chunks of 1024 products, as
+//          in kOzaki) is reduced mod m_i and stored as one byte per element
+//          in residue plane i of R; the CRT pass (ozaki2.cu) combines them.
 //  kF32    3xBF16 split GEMM: all pairs accumulate into one f32 result. The
 //          tensor cores' f32 accumulation does not round to nearest, so its
 //          error grows with the number of MMAs summed; the accumulator is
@@ -33,7 +37,7 @@
 
 namespace phpc {
 
-enum TcMode { kOzaki = 0, kF32 = 1 };
+enum TcMode { kOzaki = 0, kF32 = 1, kResidue = 2 };
 
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;              // bf16 elements of K per stage (one 128-byte swizzle row)
@@ -54,7 +58,24 @@ struct PairList {
   uint8_t a[kTcMaxPairs];     // A plane index (0-based)
   uint8_t b[kTcMaxPairs];     // B plane index (0-based)
   uint8_t g[kTcMaxPairs];     // group id (Ozaki: diagonal p + q, 1-based digits); pairs of a group are contiguous
+  uint16_t mod[kTcMaxPairs];  // kResidue: modulus of the group
+  uint32_t magic[kTcMaxPairs];  // kResidue: floor(2^32 / modulus)
 };
+
+// x mod m for 0 <= x < 2^32, m <= 256, magic = floor(2^32 / m) (Barrett: the
+// quotient estimate is low by at most one).
+__device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t m, uint32_t magic) {
+  const uint32_t q = __umulhi(x, magic);
+  uint32_t r = x - q * m;
+  if (r >= m) r -= m;
+  return r;
+}
+// Residue in [0, m) of a signed 32-bit integer.
+__device__ __forceinline__ uint32_t mod_signed(int32_t x, uint32_t m, uint32_t magic) {
+  const uint32_t mag = x < 0 ? 0u - static_cast<uint32_t>(x) : static_cast<uint32_t>(x);
+  const uint32_t r = mod_small(mag, m, magic);
+  return (x < 0 && r) ? m - r : r;
+}
 
 struct TcArgs {
   int M, N, K;
@@ -65,6 +86,9 @@ struct TcArgs {
   const int* ea;              // kOzaki: per-row exponent of A
   const int* eb;              // kOzaki: per-column exponent of B
   int* status;
+  uint8_t* R;                 // kResidue: residue planes [pairs][M][ldr]
+  int64_t ldr;                // kResidue: row stride of a residue plane (multiple of 16)
+  int64_t rplane;             // kResidue: plane stride
 };
 
 // Grouped mode: many independent problems in one persistent launch. The
@@ -319,12 +343,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         int gstart = 0;
         while (gstart < pairs.n && ok) {
           int gend = gstart + 1;
-          if (MODE == kOzaki)
+          if (MODE != kF32)
             while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
           else
             gend = pairs.n;
           const int total = (gend - gstart) * job.nk;
-          const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
+          const int chunk = MODE != kF32 ? kTcChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
             const int len = min(chunk, total - done);
             if (!wait_parity(&tempty[buf], tphase[buf] ^ 1, status, 12)) { ok = false; break; }
@@ -398,12 +422,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       int gstart = 0;
       while (gstart < pairs.n && ok) {
         int gend = gstart + 1;
-        if (MODE == kOzaki)
+        if (MODE != kF32)
           while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
         else
           gend = pairs.n;
         const int total = (gend - gstart) * job.nk;
-        const int chunk = MODE == kOzaki ? kTcChunkSteps : kTcF32ChunkSteps;
+        const int chunk = MODE != kF32 ? kTcChunkSteps : kTcF32ChunkSteps;
         const int nchunks = (total + chunk - 1) / chunk;
         for (int c = 0; c < nchunks && ok; ++c) {
           // all lanes must agree before the warp-collective tcgen05.ld below
@@ -411,7 +435,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if (!ok) break;
           tc_fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + buf * BN + half * HALF;
-          if (MODE == kOzaki) {
+          if (MODE != kF32) {
 #pragma unroll
             for (int cb = 0; cb < HALF; cb += 32) {
               uint32_t r[32];
@@ -443,8 +467,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           buf ^= 1;
 
           const bool group_end = (c == nchunks - 1);
-          const bool fold = MODE == kOzaki ? (group_end || ((c + 1) % kTcFoldChunks) == 0) : group_end;
+          const bool fold = MODE != kF32 ? (group_end || ((c + 1) % kTcFoldChunks) == 0) : group_end;
           if (!fold) continue;
+          if (MODE == kResidue) {
+            const uint32_t m = pairs.mod[gstart], magic = pairs.magic[gstart];
+#pragma unroll
+            for (int u = 0; u < HALF; ++u) acc[u] = static_cast<int32_t>(mod_signed(acc[u], m, magic));
+            if (!group_end) continue;  // keep the partial residue; more chunks of this modulus follow
+            // One byte per element: the thread's row segment of HALF columns is
+            // contiguous in the residue plane, stored as 16-byte vectors.
+            const int64_t grow = row0 + lane;
+            if (grow < job.M) {
+              uint8_t* rp = args.R + static_cast<int64_t>(pairs.g[gstart]) * args.rplane + grow * args.ldr + col0;
+#pragma unroll
+              for (int u = 0; u < HALF; u += 16) {
+                if (col0 + u + 16 <= job.N) {
+                  uint32_t w[4];
+#pragma unroll
+                  for (int q = 0; q < 4; ++q)
+                    w[q] = static_cast<uint32_t>(acc[u + 4 * q]) | (static_cast<uint32_t>(acc[u + 4 * q + 1]) << 8) |
+                           (static_cast<uint32_t>(acc[u + 4 * q + 2]) << 16) |
+                           (static_cast<uint32_t>(acc[u + 4 * q + 3]) << 24);
+                  *reinterpret_cast<uint4*>(rp + u) = make_uint4(w[0], w[1], w[2], w[3]);
+                } else {
+#pragma unroll
+                  for (int q = 0; q < 16; ++q)
+                    if (col0 + u + q < job.N) rp[u + q] = static_cast<uint8_t>(acc[u + q]);
+                }
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < HALF; ++u) acc[u] = 0;
+            continue;
+          }
           // Write the warp's 32 rows x HALF columns out, 32 columns at a time,
           // transposed through shared memory so that a warp touches one
           // contiguous 32-element run of a row per access.

@@ -74,6 +74,12 @@ _lib.phpc_sgemm_bf16x3_dev.restype = ct.c_int
 _lib.phpc_sgemm_ffma_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p, ct.c_int64,
                                      ct.c_void_p, ct.c_int64, ct.c_void_p]
 _lib.phpc_sgemm_ffma_dev.restype = ct.c_int
+_lib.phpc_ozaki2_workspace_bytes.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+_lib.phpc_ozaki2_workspace_bytes.restype = ct.c_size_t
+_lib.phpc_dgemm_ozaki2_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p,
+                                       ct.c_int64, ct.c_void_p, ct.c_int64, ct.c_int, ct.c_void_p, ct.c_size_t,
+                                       ct.c_void_p]
+_lib.phpc_dgemm_ozaki2_dev.restype = ct.c_int
 
 
 class GemmProblem(ct.Structure):
@@ -181,6 +187,16 @@ def default_slices(m, k, n) -> int:
 def dgemm_ozaki_dev(m, k, n, A, lda, B, ldb, C, ldc, slices, workspace, workspace_bytes, stream=None) -> None:
     _check(_lib.phpc_dgemm_ozaki_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, slices,
                                      _dptr(workspace), workspace_bytes, _stream(stream)), "phpc_dgemm_ozaki_dev")
+
+
+def ozaki2_workspace_bytes(m, k, n, moduli) -> int:
+    return int(_lib.phpc_ozaki2_workspace_bytes(m, k, n, moduli))
+
+
+def dgemm_ozaki2_dev(m, k, n, A, lda, B, ldb, C, ldc, moduli, workspace, workspace_bytes, stream=None) -> None:
+    """FP64-accurate C += A @ B by the modular (CRT) Ozaki scheme with `moduli` residue GEMMs."""
+    _check(_lib.phpc_dgemm_ozaki2_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, moduli,
+                                      _dptr(workspace), workspace_bytes, _stream(stream)), "phpc_dgemm_ozaki2_dev")
 
 
 def ozaki_prepare_dev(m, k, n, A, lda, B, ldb, slices, workspace, workspace_bytes, stream=None) -> None:

@@ -3,11 +3,12 @@
 Used to reproduce single launches for profiling (ncu) and timing:
 
     python hpc-multigpu-matrixmult_gb300/run_case.py --method ozaki --n 4096 --slices 7 --reps 2
+    python hpc-multigpu-matrixmult_gb300/run_case.py --method ozaki2 --n 4096 --moduli 16 --reps 2
     python hpc-multigpu-matrixmult_gb300/run_case.py --method dmma --n 2048
     python hpc-multigpu-matrixmult_gb300/run_case.py --method bf16x3 --m 32768 --n 8192 --k 4096
     python hpc-multigpu-matrixmult_gb300/run_case.py --method grouped --count 512
 
-FP64 methods (ozaki, dmma) use A_ij = u * 2^e (u uniform [-1, 1), e uniform
+FP64 methods (ozaki, ozaki2, dmma) use A_ij = u * 2^e (u uniform [-1, 1), e uniform
 in [emin, emax]) from the library's device generator; FP32 methods (bf16x3,
 ffma) use normal(0, 1) FP32 inputs. Prints one JSON line with the CUDA-event
 time of the last repetition and, with --check-rows R, the max-abs and
@@ -27,12 +28,13 @@ sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 def main() -> int:
     p = argparse.ArgumentParser()
-    p.add_argument("--method", choices=["ozaki", "dmma", "bf16x3", "ffma", "grouped"], default="ozaki")
+    p.add_argument("--method", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma", "grouped"], default="ozaki")
     p.add_argument("--count", type=int, default=512, help="grouped: number of problems")
     p.add_argument("--n", type=int, default=4096)
     p.add_argument("--m", type=int, default=0)
     p.add_argument("--k", type=int, default=0)
     p.add_argument("--slices", type=int, default=7)
+    p.add_argument("--moduli", type=int, default=16, help="ozaki2: number of residue GEMMs")
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--emin", type=int, default=-20)
     p.add_argument("--emax", type=int, default=20)
@@ -64,6 +66,8 @@ def main() -> int:
     ws = 0
     if a.method == "ozaki":
         ws = phpc.ozaki_workspace_bytes(m, k, n, a.slices)
+    elif a.method == "ozaki2":
+        ws = phpc.ozaki2_workspace_bytes(m, k, n, a.moduli)
     elif a.method == "bf16x3":
         ws = phpc.bf16x3_workspace_bytes(m, k, n)
     if ws:
@@ -72,6 +76,8 @@ def main() -> int:
     def once():
         if a.method == "ozaki":
             phpc.dgemm_ozaki_dev(m, k, n, A, k, B, n, C, n, a.slices, W, ws, st)
+        elif a.method == "ozaki2":
+            phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, a.moduli, W, ws, st)
         elif a.method == "dmma":
             phpc.dgemm_dmma_dev(m, k, n, A, k, B, n, C, n, 1, 1, 256, st)
         elif a.method == "bf16x3":
@@ -103,7 +109,7 @@ def main() -> int:
         d = (got - R).abs()
         err = {"max": float(d.max() / R.abs().max()), "frob": float(d.norm() / R.norm())}
     status = phpc.device_status()
-    print(json.dumps({"method": a.method, "m": m, "n": n, "k": k, "slices": a.slices, "ms": round(ms, 3),
+    print(json.dumps({"method": a.method, "m": m, "n": n, "k": k, "slices": a.slices, "moduli": a.moduli, "ms": round(ms, 3),
                       "tflops": round(2.0 * m * n * k / ms / 1e9, 3), "rel_err": err, "status": status}))
     return 0 if status == 0 else 1
 

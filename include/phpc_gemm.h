@@ -83,6 +83,17 @@ size_t phpc_ozaki_workspace_bytes(int m, int k, int n, int slices);
 int phpc_dgemm_ozaki_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
                          double *dC, int64_t ldc, int slices, void *workspace, size_t workspace_bytes, void *stream);
 
+/* FP64-accurate GEMM by the modular (Chinese-remainder) Ozaki scheme:
+ * C += A * B from `moduli` (8..16) residue GEMMs. Each operand element becomes
+ * an integer on the fixed-point grid of its row (A) / column (B), b bits wide
+ * with b the largest width for which 2 K 2^(2b) < M = product of the moduli
+ * (moduli = 16: b = 55 at K = 16384); its residues (|r| <= 128) are exact in
+ * BF16, the residue products run on tcgen05, and the exact integer product is
+ * recovered by the CRT and rounded once to double. */
+size_t phpc_ozaki2_workspace_bytes(int m, int k, int n, int moduli);
+int phpc_dgemm_ozaki2_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
+                          double *dC, int64_t ldc, int moduli, void *workspace, size_t workspace_bytes, void *stream);
+
 /* The two phases of phpc_dgemm_ozaki_dev, for callers that reuse the digit
  * planes of A and B or time the phases separately:
  * prepare = exponent scans + digit split of A and B into the workspace;

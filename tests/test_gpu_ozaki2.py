@@ -1,0 +1,95 @@
+"""Parity of the modular (CRT) Ozaki GEMM with the oracle.
+
+Bit-exact against tests/ozaki2_model.py (exact integer product of the
+fixed-point operands, rounded once to double): checks the residue split, the
+exactness of the residue GEMMs on tcgen05, the CRT reconstruction and its
+rounding. Also exact on the reference's index inputs and within 1e-14
+(Frobenius) of the double-double oracle on wide-exponent inputs.
+"""
+import numpy as np
+import pytest
+
+import ozaki2_model
+from golden_inputs import golden_cases, golden_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def run_dev(phpc, torch, a, b, c0, nmod):
+    m, k = a.shape
+    n = b.shape[1]
+    A = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    B = torch.from_numpy(np.ascontiguousarray(b)).cuda()
+    C = torch.from_numpy(np.ascontiguousarray(c0)).cuda()
+    nbytes = phpc.ozaki2_workspace_bytes(m, k, n, nmod)
+    W = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, nmod, W, nbytes)
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    return C.cpu().numpy()
+
+
+@pytest.mark.parametrize("nmod", [8, 12, 14, 16])
+@pytest.mark.parametrize("m,k,n", [(128, 64, 256), (70, 300, 130), (7, 13, 5), (200, 1100, 96)])
+def test_bitexact_vs_model(phpc, torch_cuda, nmod, m, k, n):
+    rng = np.random.default_rng(nmod * 1009 + m + k + n)
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+    b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-20, 21, (k, n)))
+    c0 = rng.uniform(-1, 1, (m, n))
+    got = run_dev(phpc, torch_cuda, a, b, c0, nmod)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, nmod))
+
+
+@pytest.mark.parametrize("cluster,bn", [("1", "128"), ("2", "256")])
+def test_bitexact_tile_variants(phpc, torch_cuda, monkeypatch, cluster, bn):
+    monkeypatch.setenv("PHPC_CLUSTER", cluster)
+    monkeypatch.setenv("PHPC_OZAKI_BN", bn)
+    rng = np.random.default_rng(77)
+    a = rng.uniform(-1, 1, (300, 400))
+    b = rng.uniform(-1, 1, (400, 520))
+    got = run_dev(phpc, torch_cuda, a, b, np.zeros((300, 520)), 16)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 16))
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] == "index"], ids=lambda c: c["name"])
+def test_index_inputs_exact(case, phpc, torch_cuda, oracle):
+    a, b, c = golden_inputs(case)
+    ref = c.copy()
+    oracle.gemm_iterative(a, b, ref)
+    np.testing.assert_array_equal(run_dev(phpc, torch_cuda, a, b, c, 16), ref)
+
+
+@pytest.mark.parametrize("dist", ["uniform", "wide"])
+def test_n1024_frobenius_1e14(phpc, torch_cuda, oracle, dist):
+    rng = np.random.default_rng(19)
+    n = 1024
+    a = rng.uniform(-1, 1, (n, n))
+    b = rng.uniform(-1, 1, (n, n))
+    if dist == "wide":
+        a *= np.exp2(rng.integers(-20, 21, (n, n)))
+        b *= np.exp2(rng.integers(-20, 21, (n, n)))
+    c = run_dev(phpc, torch_cuda, a, b, np.zeros((n, n)), 16)
+    rows = np.arange(0, n, 16)
+    err = oracle.rel_errors(c[rows], oracle.gemm_dd(a, b, rows=rows))
+    assert err["frob"] <= 1e-15 and err["max"] <= 1e-15, err
+
+
+def test_zero_rows_columns_and_argument_errors(phpc, torch_cuda):
+    rng = np.random.default_rng(4)
+    a = rng.uniform(-1, 1, (64, 96))
+    b = rng.uniform(-1, 1, (96, 80))
+    a[3] = 0.0
+    b[:, 7] = 0.0
+    c0 = rng.uniform(-1, 1, (64, 80))
+    got = run_dev(phpc, torch_cuda, a, b, c0, 16)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 16))
+    np.testing.assert_array_equal(got[3], c0[3])
+    torch = torch_cuda
+    A = torch.zeros(64, 64, dtype=torch.float64, device="cuda")
+    W = torch.empty(16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(phpc.PhpcError) as e:
+        phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 16, W, 16)
+    assert e.value.code == 6
+    with pytest.raises(phpc.PhpcError) as e:
+        phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 17, W, 16)
+    assert e.value.code == 1

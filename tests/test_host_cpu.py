@@ -138,3 +138,36 @@ def test_model_error_vs_dd_oracle(oracle, dist, s, bound):
     ref = oracle.gemm_dd(a, b)
     err = oracle.rel_errors(c, ref)
     assert err["frob"] <= bound, err
+
+
+# ------------------------------------------------ modular (CRT) Ozaki scheme
+def test_moduli_pairwise_coprime_and_bits():
+    import math
+
+    import ozaki2_model
+
+    mods = ozaki2_model.MODULI[:16]
+    for i in range(len(mods)):
+        for j in range(i + 1, len(mods)):
+            assert math.gcd(mods[i], mods[j]) == 1
+    assert ozaki2_model.bits_for(16, 16384) == 55
+    for nmod in range(8, 17):
+        for k in (16, 1000, 16384):
+            b = ozaki2_model.bits_for(nmod, k)
+            assert 2 * k * 2 ** (2 * b) < math.prod(mods[:nmod])
+
+
+@pytest.mark.parametrize("dist,nmod,bound", [("uniform", 16, 1e-16), ("wide", 16, 1e-16), ("wide", 14, 5e-15),
+                                             ("uniform", 12, 2e-13)])
+def test_crt_model_error_vs_dd_oracle(oracle, dist, nmod, bound):
+    import ozaki2_model
+
+    rng = np.random.default_rng(21)
+    n = 64
+    a = rng.uniform(-1, 1, (n, n))
+    b = rng.uniform(-1, 1, (n, n))
+    if dist == "wide":
+        a *= np.exp2(rng.integers(-20, 21, (n, n)))
+        b *= np.exp2(rng.integers(-20, 21, (n, n)))
+    err = oracle.rel_errors(ozaki2_model.gemm(a, b, None, nmod), oracle.gemm_dd(a, b))
+    assert err["frob"] <= bound, err
