@@ -51,6 +51,8 @@ struct ModTable {
   uint32_t magic[kMaxModuli];  // floor(2^32 / m)
   uint32_t c21[kMaxModuli];    // 2^21 mod m
   uint32_t c42[kMaxModuli];    // 2^42 mod m
+  uint32_t d63[kMaxModuli];    // -2^63 mod m (removes the 2^63 offset of the operands)
+  uint32_t h[kMaxModuli];      // (m + 1) / 2: residues at or above it map to r - m
   uint32_t W[kMaxModuli][4];   // CRT weights, little-endian 32-bit limbs
   uint32_t M[4];               // product of the moduli
   uint32_t Mhalf[4];           // floor(M / 2)
@@ -78,6 +80,8 @@ ModTable make_table(int nmod, int k) {
     T.magic[i] = static_cast<uint32_t>((1ull << 32) / m);
     T.c21[i] = static_cast<uint32_t>((1ull << 21) % m);
     T.c42[i] = static_cast<uint32_t>((1ull << 42) % m);
+    T.d63[i] = static_cast<uint32_t>((m - (1ull << 63) % m) % m);
+    T.h[i] = (m + 1) / 2;
     const u128 Mi = M / m;
     const uint32_t mi_mod = static_cast<uint32_t>(Mi % m);
     uint32_t inv = 0;
@@ -97,23 +101,23 @@ ModTable make_table(int nmod, int k) {
   return T;
 }
 
-// Symmetric residues of sign * X modulo each modulus, X < 2^63 given as three
-// 21-bit limbs (X mod m = L2 * (2^42 mod m) + L1 * (2^21 mod m) + L0, mod m).
-__device__ __forceinline__ int residue_of(uint32_t L0, uint32_t L1, uint32_t L2, bool neg, const ModTable& T,
-                                          int i) {
-  const uint32_t m = T.m[i];
-  const uint32_t t = L2 * T.c42[i] + L1 * T.c21[i] + L0;  // < 2^31
-  uint32_t r = mod_small(t, m, T.magic[i]);
-  if (neg && r) r = m - r;
-  int v = static_cast<int>(r);
-  if (2 * r >= m) v -= static_cast<int>(m);  // [-(m/2), (m-1)/2]: |v| <= 128
-  return v;
+// The operand integer V = sign * X (X <= 2^62) is handled as V + 2^63, which
+// is non-negative, in three limbs of 21, 21 and 22 bits.
+__device__ __forceinline__ void offset_limbs(uint64_t X, bool neg, uint32_t& L0, uint32_t& L1, uint32_t& L2) {
+  const uint64_t V = (1ull << 63) + (neg ? 0ull - X : X);
+  L0 = static_cast<uint32_t>(V & 0x1FFFFF);
+  L1 = static_cast<uint32_t>((V >> 21) & 0x1FFFFF);
+  L2 = static_cast<uint32_t>(V >> 42);
 }
 
-__device__ __forceinline__ void limbs21(uint64_t X, uint32_t& L0, uint32_t& L1, uint32_t& L2) {
-  L0 = static_cast<uint32_t>(X & 0x1FFFFF);
-  L1 = static_cast<uint32_t>((X >> 21) & 0x1FFFFF);
-  L2 = static_cast<uint32_t>(X >> 42);
+// Symmetric residue of V modulo m_i, |v| <= m_i / 2 <= 128:
+// t = L2 (2^42 mod m) + L1 (2^21 mod m) + L0 + (-2^63 mod m) < 2^31 is
+// congruent to V; t - floor(t * floor(2^32 / m) / 2^32) * m lies in [0, 2m).
+__device__ __forceinline__ int residue_of(uint32_t L0, uint32_t L1, uint32_t L2, const ModTable& T, int i) {
+  const uint32_t m = T.m[i];
+  const uint32_t t = L2 * T.c42[i] + L1 * T.c21[i] + L0 + T.d63[i];
+  const uint32_t r = t - __umulhi(t, T.magic[i]) * m;
+  return static_cast<int>(r) - static_cast<int>(m) * ((r >= T.h[i]) + (r >= m + T.h[i]));
 }
 
 // A residue planes [n][M][ldp]: blockIdx.x = row, each thread 8 consecutive k.
@@ -126,20 +130,19 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
   const int e = ea[row];
   const double* a = A + row * lda;
   uint32_t L0[8], L1[8], L2[8];
-  bool neg[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const uint64_t X = fixed_point(k0 + j < K ? a[k0 + j] : 0.0, e, T.bits, neg[j]);
-    limbs21(X, L0[j], L1[j], L2[j]);
+    bool neg;
+    const uint64_t X = fixed_point(k0 + j < K ? a[k0 + j] : 0.0, e, T.bits, neg);
+    offset_limbs(X, neg, L0[j], L1[j], L2[j]);
   }
   uint16_t* out = planes + row * ldp + k0;
   for (int i = 0; i < T.n; ++i) {
     uint32_t w[4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2)
-      w[j >> 1] = static_cast<uint32_t>(bf16_bits_of_int(residue_of(L0[j], L1[j], L2[j], neg[j], T, i))) |
-                  (static_cast<uint32_t>(bf16_bits_of_int(residue_of(L0[j + 1], L1[j + 1], L2[j + 1], neg[j + 1], T, i)))
-                   << 16);
+      w[j >> 1] = bf16x2_of_small_ints(residue_of(L0[j], L1[j], L2[j], T, i),
+                                       residue_of(L0[j + 1], L1[j + 1], L2[j + 1], T, i));
     *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
@@ -159,14 +162,14 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
   const int64_t col = j0 + j;
   const int e = col < N ? eb[col] : kExpZero;
   uint32_t L0[8], L1[8], L2[8];
-  bool neg[8];
 #pragma unroll
   for (int u = 0; u < 4; ++u) {  // k pairs kp0, kp0 + 4, ...: elements 2u, 2u + 1
     const int64_t k = k0 + 2 * (kp0 + 4 * u);
-    const uint64_t X0 = fixed_point((col < N && k < K) ? B[k * ldb + col] : 0.0, e, T.bits, neg[2 * u]);
-    const uint64_t X1 = fixed_point((col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0, e, T.bits, neg[2 * u + 1]);
-    limbs21(X0, L0[2 * u], L1[2 * u], L2[2 * u]);
-    limbs21(X1, L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1]);
+    bool n0, n1;
+    const uint64_t X0 = fixed_point((col < N && k < K) ? B[k * ldb + col] : 0.0, e, T.bits, n0);
+    const uint64_t X1 = fixed_point((col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0, e, T.bits, n1);
+    offset_limbs(X0, n0, L0[2 * u], L1[2 * u], L2[2 * u]);
+    offset_limbs(X1, n1, L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1]);
   }
   const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;
   const int64_t gj = j0 + wj, gk = k0 + 8 * q;
@@ -175,11 +178,8 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
     for (int p = 0; p < cnt; ++p) {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        st[p][j][kp0 + 4 * u] =
-            static_cast<uint32_t>(bf16_bits_of_int(residue_of(L0[2 * u], L1[2 * u], L2[2 * u], neg[2 * u], T, i0 + p))) |
-            (static_cast<uint32_t>(
-                 bf16_bits_of_int(residue_of(L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1], neg[2 * u + 1], T, i0 + p)))
-             << 16);
+        st[p][j][kp0 + 4 * u] = bf16x2_of_small_ints(residue_of(L0[2 * u], L1[2 * u], L2[2 * u], T, i0 + p),
+                                                     residue_of(L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1], T, i0 + p));
     }
     __syncthreads();
     if (gj < N && gk < ldp)
@@ -200,97 +200,70 @@ __device__ __forceinline__ double add_scaled(double c, double v, int x) {
   return c + ldexp(v, x);
 }
 
-// C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
-__global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
-                                                  int N, const int* __restrict__ ea, const int* __restrict__ eb,
-                                                  const __grid_constant__ ModTable T, double* __restrict__ C,
-                                                  int64_t ldc) {
-  const int64_t row = blockIdx.x;
-  const int64_t col = (int64_t)blockIdx.y * blockDim.x + threadIdx.x;
-  if (row >= M || col >= N) return;
-  // acc = sum r_i W_i: 32-bit limbs accumulated in 64 bits (no overflow: 16 x 2^8 x 2^32 < 2^45)
-  uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-  const uint8_t* rp = R + row * ldr + col;
-  for (int i = 0; i < T.n; ++i) {
-    const uint64_t r = rp[i * rplane];
-    a0 += r * T.W[i][0];
-    a1 += r * T.W[i][1];
-    a2 += r * T.W[i][2];
-    a3 += r * T.W[i][3];
-  }
-  uint32_t l[5];
-  uint64_t t = a0;
-  l[0] = static_cast<uint32_t>(t);
-  t = (t >> 32) + a1;
-  l[1] = static_cast<uint32_t>(t);
-  t = (t >> 32) + a2;
-  l[2] = static_cast<uint32_t>(t);
-  t = (t >> 32) + a3;
-  l[3] = static_cast<uint32_t>(t);
-  l[4] = static_cast<uint32_t>(t >> 32);
-  // q = floor(acc / M) < 2^12 (acc < 16 * 256 * M), estimated in single
-  // precision from the 64 bits at limb qlimb (acc >> 32 qlimb < 2^64), then
-  // corrected by at most one in either direction below
+// The symmetric representative of acc mod M (acc = sum r_i W_i < 2^12 M, as
+// five 32-bit limbs) rounded once to double: returns v and sets shift so that
+// the result is v * 2^shift (v an integer-valued double, 0 for a zero result).
+__device__ __forceinline__ double crt_round(uint32_t (&l)[5], const ModTable& T, int& shift) {
+  // q = floor(acc / M) < 2^12, estimated in single precision from the 64 bits
+  // at limb qlimb (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20: error well
+  // below one), then corrected by at most one in either direction
   const float top = static_cast<float>((static_cast<uint64_t>(l[T.qlimb + 1]) << 32) | l[T.qlimb]);
-  uint32_t q = static_cast<uint32_t>(top / T.Mtop);
-  // r = acc - q M (160-bit, two's complement)
+  const uint32_t q = static_cast<uint32_t>(top / T.Mtop);
   uint32_t rr[5];
-  uint64_t carry = 0, borrow = 0;
-  for (int w = 0; w < 5; ++w) {
+  uint64_t carry = 0;
+  uint32_t borrow = 0;
+#pragma unroll
+  for (int w = 0; w < 5; ++w) {  // r = acc - q M (160-bit two's complement)
     const uint64_t pm = (w < 4 ? static_cast<uint64_t>(T.M[w]) * q : 0) + carry;
     carry = pm >> 32;
     const uint64_t sub = static_cast<uint64_t>(l[w]) - static_cast<uint32_t>(pm) - borrow;
     rr[w] = static_cast<uint32_t>(sub);
-    borrow = (sub >> 63) & 1;
+    borrow = static_cast<uint32_t>(sub >> 63);
   }
-  // negative: add M back (q was one too large)
-  if (rr[4] & 0x80000000u) {
+  if (rr[4] & 0x80000000u) {  // negative: q was one too large, add M back
     uint64_t c2 = 0;
+#pragma unroll
     for (int w = 0; w < 5; ++w) {
-      const uint64_t s = static_cast<uint64_t>(rr[w]) + (w < 4 ? T.M[w] : 0) + c2;
-      rr[w] = static_cast<uint32_t>(s);
-      c2 = s >> 32;
+      const uint64_t t = static_cast<uint64_t>(rr[w]) + (w < 4 ? T.M[w] : 0) + c2;
+      rr[w] = static_cast<uint32_t>(t);
+      c2 = t >> 32;
+    }
+  } else {  // r >= M: q was one too small, subtract M
+    bool ge = rr[4] != 0;
+    if (!ge) {
+      ge = true;
+#pragma unroll
+      for (int w = 3; w >= 0; --w)
+        if (rr[w] != T.M[w]) { ge = rr[w] > T.M[w]; break; }
+    }
+    if (ge) {
+      uint32_t b2 = 0;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint64_t t = static_cast<uint64_t>(rr[w]) - T.M[w] - b2;
+        rr[w] = static_cast<uint32_t>(t);
+        b2 = static_cast<uint32_t>(t >> 63);
+      }
     }
   }
-  // r >= M: subtract M (q was one too small)
-  auto geq_M = [&]() {
-    if (rr[4]) return true;
-    for (int w = 3; w >= 0; --w)
-      if (rr[w] != T.M[w]) return rr[w] > T.M[w];
-    return true;
-  };
-  if (geq_M()) {
-    uint64_t b2 = 0;
-    for (int w = 0; w < 5; ++w) {
-      const uint64_t s = static_cast<uint64_t>(rr[w]) - (w < 4 ? T.M[w] : 0) - b2;
-      rr[w] = static_cast<uint32_t>(s);
-      b2 = (s >> 63) & 1;
-    }
-  }
-  // symmetric representative: r > M/2 -> r - M (negative), magnitude M - r
+  // symmetric representative: r > M/2 -> r - M, magnitude M - r
   bool gt_half = false;
+#pragma unroll
   for (int w = 3; w >= 0; --w)
     if (rr[w] != T.Mhalf[w]) { gt_half = rr[w] > T.Mhalf[w]; break; }
-  bool neg = false;
   uint32_t x[4] = {rr[0], rr[1], rr[2], rr[3]};
   if (gt_half) {
-    neg = true;
-    uint64_t b2 = 0;
+    uint32_t b2 = 0;
+#pragma unroll
     for (int w = 0; w < 4; ++w) {
-      const uint64_t s = static_cast<uint64_t>(T.M[w]) - x[w] - b2;
-      x[w] = static_cast<uint32_t>(s);
-      b2 = (s >> 63) & 1;
+      const uint64_t t = static_cast<uint64_t>(T.M[w]) - x[w] - b2;
+      x[w] = static_cast<uint32_t>(t);
+      b2 = static_cast<uint32_t>(t >> 63);
     }
   }
-  double* cp = C + row * ldc + col;
   const uint64_t hi = (static_cast<uint64_t>(x[3]) << 32) | x[2];
   const uint64_t lo = (static_cast<uint64_t>(x[1]) << 32) | x[0];
-  if (hi == 0 && lo == 0) {
-    *cp = *cp + 0.0;
-    return;
-  }
   double v;
-  int shift;
   if (hi == 0) {
     v = __ull2double_rn(lo);
     shift = 0;
@@ -303,8 +276,58 @@ __global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R,
     v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
     shift = 64 - lz;
   }
-  if (neg) v = -v;
-  *cp = add_scaled(*cp, v, shift + max(ea[row], -20000) + max(eb[col], -20000) - 2 * T.bits);
+  return gt_half ? -v : v;
+}
+
+constexpr int kCrtCols = 4;  // consecutive columns per thread (one 32-bit load per plane)
+
+// C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
+__global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
+                                                  int N, const int* __restrict__ ea, const int* __restrict__ eb,
+                                                  const __grid_constant__ ModTable T, double* __restrict__ C,
+                                                  int64_t ldc) {
+  const int64_t row = blockIdx.x;
+  const int64_t c0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * kCrtCols;
+  if (row >= M || c0 >= N) return;
+  // c0 is a multiple of 4 below N <= ldr (a multiple of 16): the word is in the plane
+  uint32_t rw[kMaxModuli];
+  const uint8_t* rp = R + row * ldr + c0;
+#pragma unroll
+  for (int i = 0; i < kMaxModuli; ++i) rw[i] = i < T.n ? *reinterpret_cast<const uint32_t*>(rp + i * rplane) : 0u;
+  const int e_row = max(ea[row], -20000) - 2 * T.bits;
+  double* cp = C + row * ldc + c0;
+#pragma unroll
+  for (int c = 0; c < kCrtCols; ++c) {
+    if (c0 + c >= N) break;
+    // acc = sum r_i W_i in 32-bit limbs accumulated in 64 bits (16 x 2^8 x 2^32 < 2^45)
+    uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+    for (int i = 0; i < kMaxModuli; ++i) {
+      if (i < T.n) {
+        const uint32_t r = (rw[i] >> (8 * c)) & 0xFFu;
+        a0 += static_cast<uint64_t>(r) * T.W[i][0];
+        a1 += static_cast<uint64_t>(r) * T.W[i][1];
+        a2 += static_cast<uint64_t>(r) * T.W[i][2];
+        a3 += static_cast<uint64_t>(r) * T.W[i][3];
+      }
+    }
+    uint32_t l[5];
+    uint64_t t = a0;
+    l[0] = static_cast<uint32_t>(t);
+    t = (t >> 32) + a1;
+    l[1] = static_cast<uint32_t>(t);
+    t = (t >> 32) + a2;
+    l[2] = static_cast<uint32_t>(t);
+    t = (t >> 32) + a3;
+    l[3] = static_cast<uint32_t>(t);
+    l[4] = static_cast<uint32_t>(t >> 32);
+    int shift;
+    const double v = crt_round(l, T, shift);
+    if (v == 0.0)
+      cp[c] = cp[c] + 0.0;
+    else
+      cp[c] = add_scaled(cp[c], v, shift + e_row + max(eb[c0 + c], -20000));
+  }
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -370,7 +393,7 @@ int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const doubl
                            : launch_tc_slice_gemm<256, kResidue>(pa, pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
                                                                   nullptr, nullptr, stream, R, L.ldr, rplane);
   if (rc != PHPC_OK) return rc;
-  crt_kernel<<<dim3(m, ceil_div(n, 128)), 128, 0, stream>>>(R, L.ldr, rplane, m, n, ea, eb, T, dC, ldc);
+  crt_kernel<<<dim3(m, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(R, L.ldr, rplane, m, n, ea, eb, T, dC, ldc);
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
 }

@@ -82,6 +82,20 @@ __device__ __forceinline__ uint16_t bf16_bits_of_int(int v) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(static_cast<float>(v)));
 }
 
+// float(v) for |v| < 2^22 without a conversion instruction: the bits of
+// 1.5 * 2^23 plus v are the float 1.5 * 2^23 + v (unit spacing there), and
+// subtracting 1.5 * 2^23 is exact.
+__device__ __forceinline__ float float_of_small_int(int v) {
+  return __int_as_float(0x4B400000 + v) - 12582912.0f;
+}
+
+// Two integers with |v| <= 256 as a packed pair of BF16 values (lo in the low
+// half): the floats are exact and their low 16 bits are zero, so their high
+// halves are the BF16 encodings.
+__device__ __forceinline__ uint32_t bf16x2_of_small_ints(int lo, int hi) {
+  return __byte_perm(__float_as_uint(float_of_small_int(lo)), __float_as_uint(float_of_small_int(hi)), 0x7632);
+}
+
 
 // Warp-cooperative scan of one row: *out = max_k e(a[k]); flags inf/NaN.
 __device__ __forceinline__ void scan_row_warp(const double* __restrict__ a, int K, int* out, int* status) {
@@ -107,8 +121,7 @@ __device__ __forceinline__ void split_row_piece(const double* __restrict__ a, in
     split_digits(x1, e, s, d1);
 #pragma unroll
     for (int p = 0; p < 8; ++p)
-      packed[p][j >> 1] = static_cast<uint32_t>(bf16_bits_of_int(d0[p])) |
-                          (static_cast<uint32_t>(bf16_bits_of_int(d1[p])) << 16);
+      packed[p][j >> 1] = bf16x2_of_small_ints(d0[p], d1[p]);
   }
 #pragma unroll
   for (int p = 0; p < 8; ++p)
@@ -138,8 +151,7 @@ __device__ __forceinline__ void split_col_block(const double* __restrict__ B, in
 #pragma unroll
     for (int p = 0; p < 8; ++p)
       if (p < s)
-        st[p][j][kp] = static_cast<uint32_t>(bf16_bits_of_int(d0[p])) |
-                       (static_cast<uint32_t>(bf16_bits_of_int(d1[p])) << 16);
+        st[p][j][kp] = bf16x2_of_small_ints(d0[p], d1[p]);
   }
   __syncthreads();
   const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;  // row j of the block, 16-byte quarter of its 64-byte run

@@ -471,28 +471,32 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if (!fold) continue;
           if (MODE == kResidue) {
             const uint32_t m = pairs.mod[gstart], magic = pairs.magic[gstart];
+            if (!group_end) {  // keep the partial residue; more chunks of this modulus follow
 #pragma unroll
-            for (int u = 0; u < HALF; ++u) acc[u] = static_cast<int32_t>(mod_signed(acc[u], m, magic));
-            if (!group_end) continue;  // keep the partial residue; more chunks of this modulus follow
+              for (int u = 0; u < HALF; ++u) acc[u] = static_cast<int32_t>(mod_signed(acc[u], m, magic));
+              continue;
+            }
             // One byte per element: the thread's row segment of HALF columns is
-            // contiguous in the residue plane, stored as 16-byte vectors.
+            // contiguous in the residue plane, reduced and stored 16 columns
+            // (one 16-byte vector) at a time.
             const int64_t grow = row0 + lane;
-            if (grow < job.M) {
-              uint8_t* rp = args.R + static_cast<int64_t>(pairs.g[gstart]) * args.rplane + grow * args.ldr + col0;
+            uint8_t* rp = args.R + static_cast<int64_t>(pairs.g[gstart]) * args.rplane + grow * args.ldr + col0;
 #pragma unroll
-              for (int u = 0; u < HALF; u += 16) {
+            for (int u = 0; u < HALF; u += 16) {
+              uint32_t w[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                w[q] = 0;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) w[q] |= mod_signed(acc[u + 4 * q + v], m, magic) << (8 * v);
+              }
+              if (grow < job.M) {
                 if (col0 + u + 16 <= job.N) {
-                  uint32_t w[4];
-#pragma unroll
-                  for (int q = 0; q < 4; ++q)
-                    w[q] = static_cast<uint32_t>(acc[u + 4 * q]) | (static_cast<uint32_t>(acc[u + 4 * q + 1]) << 8) |
-                           (static_cast<uint32_t>(acc[u + 4 * q + 2]) << 16) |
-                           (static_cast<uint32_t>(acc[u + 4 * q + 3]) << 24);
                   *reinterpret_cast<uint4*>(rp + u) = make_uint4(w[0], w[1], w[2], w[3]);
                 } else {
 #pragma unroll
                   for (int q = 0; q < 16; ++q)
-                    if (col0 + u + q < job.N) rp[u + q] = static_cast<uint8_t>(acc[u + q]);
+                    if (col0 + u + q < job.N) rp[u + q] = static_cast<uint8_t>(w[q >> 2] >> (8 * (q & 3)));
                 }
               }
             }
