@@ -3,14 +3,17 @@
 
 Workload (one "step"): C += A @ B, square N = 16384, FP64, inputs
 A_ij = u * 2^e with u uniform [-1, 1) and e a uniform integer in [-20, 20]
-(the wide-exponent configuration), computed by the FP64-accurate Ozaki split
-GEMM (exponent scans + integer digit split + exact BF16 slice products on
-tcgen05 + FP64 fold) with the library's default slice count.
+(the wide-exponent configuration), computed by the FP64-accurate Ozaki GEMM
+the library selects for this shape (phpc_default_moduli): the modular scheme
+(exponent scans + residue split modulo q coprime moduli + q exact BF16
+residue GEMMs on tcgen05 + CRT reconstruction) or the digit scheme (digit
+split + exact BF16 slice products + FP64 fold). --moduli / --slices override.
 
 Reported (one JSON line on rank 0):
   value      2 N^3 / (device time per step), inputs resident in HBM, TFLOP/s
              (FP64-equivalent); every step reads 3 x 2 GiB of FP64 operands and
-             writes 7 GiB of digit planes, far larger than the 129 MB L2.
+             writes the split planes (8 GiB per operand at 15 moduli), far
+             larger than the 129 MB L2.
   e2e        the same metric through the reference-facing C ABI call
              phpc_gemm_cublas with pinned host buffers: host->device copies of
              A, B, C and the device->host copy of C inside the timed region.
@@ -18,9 +21,11 @@ Reported (one JSON line on rank 0):
              inputs, and split_vs_dmma = value / dmma_tflops.
   errors     max-abs and Frobenius relative errors of both results against the
              double-double reference (phpc_dgemm_dd_rows_dev) on 64 seeded rows.
-  roofline   the slice GEMM kernel (tc_slice_gemm_kernel), tensor-bound: its
-             BF16 TFLOP/s (pairs x 2 N^3 per launch / CUDA-event duration) vs
-             the measured sustained cuBLAS BF16 rate.
+  roofline   the tensor-core GEMM kernel (tc_slice_gemm_kernel), tensor-bound:
+             its BF16 TFLOP/s (q residue GEMMs, or slice pairs, x 2 N^3 per
+             launch / CUDA-event duration) vs the measured sustained cuBLAS
+             BF16 rate.
+  other_scheme  the digit (or modular) scheme on the same inputs, for context.
   cpu_baseline  the reference's CPU loop (src/iterative.c:8-13, oracle port)
              on all host cores, on a bounded sample of rows of the same product.
 
@@ -49,8 +54,9 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
 # dominant kernel, from a one-pass ncu capture of this workload
-# (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by (N, slices).
-NCU_TRAFFIC_BYTES = {(16384, 7): 426.25e9 + 15.28e9}
+# (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by
+# (N, "slices" | "moduli", count).
+NCU_TRAFFIC_BYTES = {(16384, "slices", 7): 426.25e9 + 15.28e9}
 UNIT = "TFLOP/s"
 
 
@@ -61,7 +67,9 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n", type=int, default=16384, help="matrix order (16384 is the benchmark configuration)")
-    p.add_argument("--slices", type=int, default=0, help="0 = library default")
+    p.add_argument("--moduli", type=int, default=-1,
+                   help="modular scheme with this many moduli (8..16); 0 = digit scheme; -1 = library default")
+    p.add_argument("--slices", type=int, default=0, help="digit scheme slices; 0 = library default")
     p.add_argument("--dmma-steps", type=int, default=1)
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--seed", type=int, default=20241203)
@@ -156,6 +164,53 @@ def ozaki_pairs(s: int) -> int:
     return s * (s + 1) // 2
 
 
+class Scheme:
+    """One FP64-accurate Ozaki GEMM configuration through the library's device
+    entry points: phases prepare (scans + split), multiply (tensor-core GEMM
+    kernel) and, for the modular scheme, reconstruct (CRT into C)."""
+
+    def __init__(self, phpc, n: int, moduli: int, slices: int):
+        self.phpc, self.n = phpc, n
+        self.moduli = moduli
+        self.slices = slices if moduli == 0 else 0
+        if moduli > 0:
+            self.ws_bytes = phpc.ozaki2_workspace_bytes(n, n, n, moduli)
+            self.gemms = moduli
+            self.name = f"modular, {moduli} moduli"
+            self.launches = 7  # scan_rows, residue_rows, fill_int, scan_cols, residue_cols, tc GEMM, crt
+        else:
+            self.ws_bytes = phpc.ozaki_workspace_bytes(n, n, n, slices)
+            self.gemms = ozaki_pairs(slices)
+            self.name = f"digits, {slices} slices"
+            self.launches = 6  # scan_rows, split_rows, fill_int, scan_cols, split_cols, tc GEMM (+ fold)
+
+    def full(self, A, B, C, W, stream):
+        n, p = self.n, self.phpc
+        if self.moduli:
+            p.dgemm_ozaki2_dev(n, n, n, A, n, B, n, C, n, self.moduli, W, self.ws_bytes, stream)
+        else:
+            p.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, self.slices, W, self.ws_bytes, stream)
+
+    def prepare(self, A, B, W, stream):
+        n, p = self.n, self.phpc
+        if self.moduli:
+            p.ozaki2_prepare_dev(n, n, n, A, n, B, n, self.moduli, W, self.ws_bytes, stream)
+        else:
+            p.ozaki_prepare_dev(n, n, n, A, n, B, n, self.slices, W, self.ws_bytes, stream)
+
+    def multiply(self, C, W, stream):
+        n, p = self.n, self.phpc
+        if self.moduli:
+            p.ozaki2_multiply_dev(n, n, n, self.moduli, W, self.ws_bytes, stream)
+        else:
+            p.ozaki_multiply_dev(n, n, n, C, n, self.slices, W, self.ws_bytes, stream)
+
+    def reconstruct(self, C, W, stream):
+        if self.moduli:
+            n = self.n
+            self.phpc.ozaki2_reconstruct_dev(n, n, n, C, n, self.moduli, W, self.ws_bytes, stream)
+
+
 def run_ours(args, world, rank, local):
     import torch
     import phpc
@@ -166,7 +221,8 @@ def run_ours(args, world, rank, local):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     n = args.n
-    s = args.slices or phpc.default_slices(n, n, n)
+    moduli = args.moduli if args.moduli >= 0 else phpc.default_moduli(n, n, n)
+    sch = Scheme(phpc, n, moduli, args.slices or phpc.default_slices(n, n, n))
     flops = 2.0 * n * n * n
     stream = torch.cuda.current_stream()
 
@@ -176,8 +232,7 @@ def run_ours(args, world, rank, local):
     seed = args.seed + 1000 * rank
     phpc.fill_wide_dev(A, n * n, seed, 0, -20, 20, stream)
     phpc.fill_wide_dev(B, n * n, seed + 1, 0, -20, 20, stream)
-    ws_bytes = phpc.ozaki_workspace_bytes(n, n, n, s)
-    W = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    W = torch.empty(sch.ws_bytes, dtype=torch.uint8, device=dev)
 
     def barrier():
         torch.cuda.synchronize()
@@ -202,7 +257,7 @@ def run_ours(args, world, rank, local):
                 "frob": float(np.sqrt(np.sum(d * d) / np.sum(r * r)))}
 
     C.zero_()
-    phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws_bytes, stream)
+    sch.full(A, B, C, W, stream)
     torch.cuda.synchronize()
     status = phpc.device_status()
     if status != 0:
@@ -231,31 +286,54 @@ def run_ours(args, world, rank, local):
 
     # ---- Ozaki timed region: K steps of C += A B, inputs resident in HBM
     for _ in range(args.warmup):
-        phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws_bytes, stream)
+        sch.full(A, B, C, W, stream)
     barrier()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
-            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         barrier()
         t0.record(stream)
-        for e_pre, e_mid, e_end in evs:
-            e_pre.record(stream)
-            phpc.ozaki_prepare_dev(n, n, n, A, n, B, n, s, W, ws_bytes, stream)
-            e_mid.record(stream)
-            phpc.ozaki_multiply_dev(n, n, n, C, n, s, W, ws_bytes, stream)
-            e_end.record(stream)
+        for e in evs:
+            e[0].record(stream)
+            sch.prepare(A, B, W, stream)
+            e[1].record(stream)
+            sch.multiply(C, W, stream)
+            e[2].record(stream)
+            sch.reconstruct(C, W, stream)
+            e[3].record(stream)
         t1.record(stream)
         barrier()
     total_s = max_over_ranks(t0.elapsed_time(t1) / 1e3)
     step_s = total_s / args.steps
-    gemm_ms = statistics.mean(b.elapsed_time(c) for _, b, c in evs)
-    prep_ms = statistics.mean(a.elapsed_time(b) for a, b, _ in evs)
+    prep_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in evs)
+    gemm_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in evs)
+    crt_ms = statistics.mean(e[2].elapsed_time(e[3]) for e in evs)
     status = phpc.device_status()
     if status != 0:
         raise RuntimeError(f"device status {status} after the timed region")
     value = replica_throughput(flops, step_s, world)
+
+    # ---- the other scheme on the same inputs, for context (untimed by the contract)
+    other = Scheme(phpc, n, 0 if sch.moduli else 15, 7)
+    Wo = None
+    other_ms = None
+    try:
+        del W
+        torch.cuda.empty_cache()
+        Wo = torch.empty(other.ws_bytes, dtype=torch.uint8, device=dev)
+        other.full(A, B, C, Wo, stream)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            other.full(A, B, C, Wo, stream)
+        e1.record(stream)
+        e1.synchronize()
+        other_ms = e0.elapsed_time(e1) / 2
+    except torch.OutOfMemoryError:
+        pass
+    del Wo
 
     # ---- end to end through the reference-facing C ABI (pinned host buffers)
     Ah = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
@@ -263,7 +341,7 @@ def run_ours(args, world, rank, local):
     Ch = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)
     Ah.copy_(A)
     Bh.copy_(B)
-    del A, B, C, W
+    del A, B, C
     torch.cuda.empty_cache()
     an, bn, cn = Ah.numpy(), Bh.numpy(), Ch.numpy()
     phpc.gemm_cublas(an, n, bn, n, cn, n, n, n, n)  # warm: allocations, tensor maps
@@ -281,7 +359,10 @@ def run_ours(args, world, rank, local):
     peak_src = "measured sustained cuBLAS bf16 (MEASURED_PEAKS.json)"
     if not peak:
         peak, peak_src = 1700.0, "fallback sustained bf16"
-    achieved = ozaki_pairs(s) * flops / (gemm_ms / 1e3) / 1e12
+    achieved = sch.gemms * flops / (gemm_ms / 1e3) / 1e12
+    mode = "kResidue" if sch.moduli else "kOzaki"
+    key = (n, "moduli", sch.moduli) if sch.moduli else (n, "slices", sch.slices)
+    unit_desc = f"{sch.moduli} residue GEMMs" if sch.moduli else f"{sch.gemms} slice pairs"
 
     result = {
         "metric": METRIC,
@@ -294,12 +375,14 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64 (bf16 digit products, int32/f32 exact accumulation, f64 fold)",
+        "dtype": ("f64 (bf16 residue products, exact f32/int32 accumulation, CRT, f64 rounding)" if sch.moduli
+                  else "f64 (bf16 digit products, int32/f32 exact accumulation, f64 fold)"),
         "data": "synthetic: seeded A_ij = u*2^e, u~U[-1,1), e~U{-20..20} (device generator)",
-        "config": {"workload": f"Ozaki split FP64-accurate GEMM C += A B, N={n}, wide-exponent inputs",
-                   "m": n, "n": n, "k": n, "slices": s, "slice_pairs": ozaki_pairs(s),
+        "config": {"workload": f"Ozaki FP64-accurate GEMM C += A B ({sch.name}), N={n}, wide-exponent inputs",
+                   "m": n, "n": n, "k": n, "scheme": "modular" if sch.moduli else "digits",
+                   "moduli": sch.moduli, "slices": sch.slices, "tensor_core_gemms": sch.gemms,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (3 x 2 GiB FP64 operands + digit planes per step)"},
+                   "l2": "inputs larger than L2 (3 x 2 GiB FP64 operands + split planes per step)"},
         "dmma_tflops": round(flops / dmma_s / 1e12, 4),
         "dmma_ms": round(dmma_s * 1e3, 1),
         "split_vs_dmma": round(value / world / (flops / dmma_s / 1e12), 2),
@@ -308,17 +391,21 @@ def run_ours(args, world, rank, local):
         "dmma_frob_rel_err": err_dmma["frob"],
         "dmma_max_rel_err": err_dmma["max"],
         "error_reference": "double-double GEMM (phpc_dgemm_dd_rows_dev) on 64 seeded rows",
-        "phase_ms": {"scan_split": round(prep_ms, 3), "slice_gemm": round(gemm_ms, 3)},
-        "roofline": {"bound": "tensor", "kernel": "tc_slice_gemm_kernel<256,kOzaki>",
+        "phase_ms": {"scan_split": round(prep_ms, 3), "tc_gemm": round(gemm_ms, 3), "crt": round(crt_ms, 3)},
+        "other_scheme": {"scheme": other.name,
+                         "ms": round(other_ms, 3) if other_ms else None,
+                         "tflops": round(flops / other_ms / 1e9, 3) if other_ms else None},
+        "roofline": {"bound": "tensor", "kernel": f"tc_slice_gemm_kernel (mode {mode})",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "TFLOP/s",
-                     "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get((n, s)),
+                     "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get(key),
                      "traffic_unit": "DRAM bytes per launch (ncu)",
                      "peak_source": peak_src,
-                     "work_per_launch": f"{ozaki_pairs(s)} slice pairs x 2 N^3 = {ozaki_pairs(s) * flops:.4e} bf16 flop"},
+                     "work_per_launch": f"{unit_desc} x 2 N^3 = {sch.gemms * flops:.4e} bf16 flop"},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * n * n * 8,
                 "d2h_bytes_per_step": n * n * 8, "api": "phpc_gemm_cublas (host pointers)",
+                "scheme": "modular" if phpc.default_moduli(n, n, n) else "digits",
                 "ms_per_step": round(e2e_step * 1e3, 1)},
-        "gpu_launches": 6 * args.steps,
+        "gpu_launches": sch.launches * args.steps,
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1:

@@ -1,6 +1,7 @@
-"""Autotuner for the FP64-accurate Ozaki GEMM: slice count, tile width, L2 raster.
+"""Autotuner for the FP64-accurate Ozaki GEMMs: scheme, tile width, L2 raster.
 
-For each square size N it sweeps slices s, output tile width BN (128 or 256),
+For each square size N it sweeps the scheme (the modular scheme with q
+moduli, or the digit scheme with s slices), output tile width BN (128 or 256),
 the raster height of the persistent tile order (group_rows) and the CTA
 grouping (1 = one CTA per 128 x BN tile, 2 = CTA pairs computing 256 x BN
 tiles with M = 256 tcgen05 MMAs), times the
@@ -36,7 +37,8 @@ def main() -> int:
     p = argparse.ArgumentParser()
     p.add_argument("--sizes", default="1024,2048,4096,8192,16384")
     p.add_argument("--max-n", type=int, default=16384)
-    p.add_argument("--slices", default="6,7,8")
+    p.add_argument("--slices", default="7", help="digit-scheme slice counts to try")
+    p.add_argument("--moduli", default="14,15,16", help="modular-scheme moduli counts to try")
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--target", type=float, default=1e-14)
     p.add_argument("--margin", type=float, default=4.0)
@@ -52,7 +54,8 @@ def main() -> int:
 
     st = torch.cuda.current_stream()
     sizes = [n for n in (int(x) for x in a.sizes.split(",")) if n <= a.max_n]
-    slices = [int(x) for x in a.slices.split(",")]
+    schemes = [("moduli", int(x)) for x in a.moduli.split(",") if x] + \
+              [("slices", int(x)) for x in a.slices.split(",") if x]
     table, report = [], []
 
     clusters = [int(x) for x in a.clusters.split(",")]
@@ -81,14 +84,23 @@ def main() -> int:
         C = torch.zeros((n, n), dtype=torch.float64, device="cuda")
         grs = [4, 8, 16] if n >= 8192 else [8]
         cands = []
-        for s in slices:
-            ws = phpc.ozaki_workspace_bytes(n, n, n, s)
+        for kind, cnt in schemes:
+            if kind == "moduli":
+                ws = phpc.ozaki2_workspace_bytes(n, n, n, cnt)
+
+                def run(A, B, C, W, ws=ws, q=cnt):
+                    phpc.dgemm_ozaki2_dev(n, n, n, A, n, B, n, C, n, q, W, ws, st)
+            else:
+                ws = phpc.ozaki_workspace_bytes(n, n, n, cnt)
+
+                def run(A, B, C, W, ws=ws, s=cnt):
+                    phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
             W = torch.empty(ws, dtype=torch.uint8, device="cuda")
             set_cfg(256, 8)
             errs = {}
             for name, (A, B, d_rows, R) in classes.items():
                 C.zero_()
-                phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
+                run(A, B, C, W)
                 got = C.index_select(0, d_rows.long())
                 errs[name] = float((got - R).norm() / R.norm())
             ok = all(e <= a.target / a.margin for e in errs.values())
@@ -97,18 +109,20 @@ def main() -> int:
                 for gr in grs:
                     for cl in clusters:
                         set_cfg(bn, gr, cl)
-                        phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)  # warm
+                        run(A, B, C, W)  # warm
                         ts = []
                         for _ in range(a.reps):
                             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                             e0.record(st)
-                            phpc.dgemm_ozaki_dev(n, n, n, A, n, B, n, C, n, s, W, ws, st)
+                            run(A, B, C, W)
                             e1.record(st)
                             e1.synchronize()
                             ts.append(e0.elapsed_time(e1))
                         ms = statistics.median(ts)
-                        rec = {"n": n, "slices": s, "bn": bn, "group_rows": gr, "cluster": cl, "ms": round(ms, 3),
-                               "tflops": round(2.0 * n ** 3 / ms / 1e9, 3), "err": errs, "qualifies": ok}
+                        rec = {"n": n, "moduli": cnt if kind == "moduli" else 0,
+                               "slices": cnt if kind == "slices" else 7, "bn": bn, "group_rows": gr,
+                               "cluster": cl, "ms": round(ms, 3), "tflops": round(2.0 * n ** 3 / ms / 1e9, 3),
+                               "err": errs, "qualifies": ok}
                         report.append(rec)
                         print(json.dumps(rec), flush=True)
                         if ok:
@@ -133,7 +147,7 @@ def main() -> int:
             phpc.fill_uniform_dev(A, m * k, 1000 + 2 * i, 0, st)
             phpc.fill_uniform_dev(B, k * n, 1001 + 2 * i, 0, st)
             mats.append((A, B, torch.zeros((m, n), dtype=torch.float64, device="cuda")))
-        s = table[-1]["slices"] if table else 7
+        s = 7  # the grouped call uses the digit scheme
         probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B, C) in zip(shapes, mats)]
         best_ms = None
         for bn in (128, 256):
@@ -164,13 +178,13 @@ def main() -> int:
     assert phpc.device_status() == 0
     lines = [f"# written by autotune.py on {torch.cuda.get_device_name()} ({time.strftime('%Y-%m-%d %H:%M UTC', time.gmtime())})",
              f"# target Frobenius error {a.target} / margin {a.margin}, uniform and wide-exponent inputs",
-             "# max_mnk slices bn group_rows cluster   (chosen: ms, FP64-equivalent TFLOP/s, errors)"]
+             "# max_mnk slices bn group_rows cluster moduli   (moduli 0 = digit scheme with `slices`)"]
     for i, b in enumerate(table):
         nxt = table[i + 1]["n"] if i + 1 < len(table) else None
         bound = int((b["n"] ** 3 * nxt ** 3) ** 0.5) if nxt else 2 ** 62
         lines.append(f"# N={b['n']}: {b['ms']} ms, {b['tflops']} TFLOP/s, err {b['err']}")
-        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']} {b['cluster']}")
-    lines.append(f"grouped {2 ** 62} {table[-1]['slices'] if table else 7} {grouped_bn}")
+        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']} {b['cluster']} {b['moduli']}")
+    lines.append(f"grouped {2 ** 62} 7 {grouped_bn}")
     Path(a.out).write_text("\n".join(lines) + "\n")
     print(f"wrote {a.out}")
     return 0

@@ -10,7 +10,9 @@
 //  - the device copies use leading dimensions padded to an even number of
 //    doubles so that TMA can address every row;
 //  - buffers that are already page-locked are not registered again;
-//  - the copies of A, B and C and the digit splits overlap on three streams,
+//  - the FP64 product of phpc_gemm_cublas is the FP64-accurate Ozaki GEMM on
+//    the BF16 tensor cores (modular or digit scheme, per the tuning table);
+//  - the copies of A, B and C and the operand splits overlap on three streams,
 //    and device buffers come from a grow-only library pool (PHPC_POOL_KEEP=0
 //    returns them to the system after every call, as the reference did);
 //  - every CUDA call is checked; the outcome is kept for phpc_last_error().
@@ -84,7 +86,7 @@ float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
 
 // Copies and compute of one call overlap across three streams: A (stream 0),
 // B (stream 1) and C (stream 2) travel to the device concurrently; A's and
-// B's digit splits start as soon as their operand has arrived; the GEMM runs
+// B's splits (residues or digits) start as soon as their operand has arrived; the GEMM runs
 // on stream 0 once B's split and C's copy are done; C returns on stream 0.
 // Device buffers come from the library's grow-only pool, so repeated calls of
 // one size allocate no new memory. *seconds = sum of the kernels' device time.
@@ -118,11 +120,16 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
     // events: 0 allocated, 1 B ready (split done / copied), 2 C copied,
     //         3/4 A-side kernels, 5/6 B-side kernels, 7 GEMM start
     cudaStream_t s0 = r.st[0], s1 = r.st[1], s2 = r.st[2];
-    int slices = 0;
+    int slices = 0, moduli = 0;
     size_t ws_bytes = 0;
     if (method == kOzakiMethod) {
-      slices = default_slices(m, k, n);
-      ws_bytes = ozaki_workspace_bytes(m, k, n, slices);
+      moduli = default_moduli(m, k, n);
+      if (moduli > 0) {
+        ws_bytes = ozaki2_workspace_bytes(m, k, n, moduli);
+      } else {
+        slices = default_slices(m, k, n);
+        ws_bytes = ozaki_workspace_bytes(m, k, n, slices);
+      }
     }
     if (rc == PHPC_OK &&
         (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, pool, s0) !=
@@ -151,7 +158,8 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
       if (method == kOzakiMethod) {
         cudaEventRecord(r.ev[3], s0);
         cudaEventRecord(r.ev[5], s1);
-        rc = ozaki_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, slices, r.ws, ws_bytes, s0, s1);
+        rc = moduli > 0 ? ozaki2_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, moduli, r.ws, ws_bytes, s0, s1)
+                        : ozaki_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, slices, r.ws, ws_bytes, s0, s1);
         cudaEventRecord(r.ev[4], s0);
         cudaEventRecord(r.ev[6], s1);
       }
@@ -160,10 +168,14 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
       cudaStreamWaitEvent(s0, r.ev[2], 0);
       cudaEventRecord(r.ev[7], s0);
       if (rc == PHPC_OK) {
-        if (method == kDmma)
+        if (method == kDmma) {
           rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, gw, gh, 256, s0);
-        else
+        } else if (moduli > 0) {
+          rc = ozaki2_multiply(m, k, n, moduli, r.ws, ws_bytes, s0, default_bn(m, k, n));
+          if (rc == PHPC_OK) rc = ozaki2_reconstruct(m, k, n, r.dC, dldc, moduli, r.ws, ws_bytes, s0);
+        } else {
           rc = ozaki_multiply(m, k, n, r.dC, dldc, slices, r.ws, ws_bytes, s0, default_bn(m, k, n));
+        }
       }
     }
     cudaEvent_t end_ev = nullptr;
@@ -178,7 +190,7 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
       if (method == kOzakiMethod) kernel_ms += elapsed_ms(r.ev[3], r.ev[4]) + elapsed_ms(r.ev[5], r.ev[6]);
     }
     if (rc == PHPC_OK && method == kOzakiMethod && (dstatus & 0xFF) == PHPC_ERR_NONFINITE) {
-      // inf/NaN cannot be carried by integer digits: redo this call in IEEE
+      // inf/NaN cannot be carried by integers: redo this call in IEEE
       // FP64 (DMMA) from the original C so that inf/NaN propagate exactly.
       dstatus = 0;
       if (cudaMemsetAsync(status, 0, sizeof(int), s0) != cudaSuccess ||

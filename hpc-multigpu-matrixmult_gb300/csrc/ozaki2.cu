@@ -350,34 +350,62 @@ Ozaki2Layout ozaki2_layout(int m, int k, int n, int nmod) {
   return L;
 }
 
+struct Ozaki2Views {
+  int* ea;
+  int* eb;
+  uint16_t* pa;
+  uint16_t* pb;
+  uint8_t* R;
+};
+
+int ozaki2_views(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, Ozaki2Layout& L, Ozaki2Views& V) {
+  const DeviceInfo* dev = current_device();
+  if (!dev) return PHPC_ERR_CUDA;
+  if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
+  L = ozaki2_layout(m, k, n, nmod);
+  if (!ws || ws_bytes < L.total || !aligned16(ws)) return PHPC_ERR_WORKSPACE;
+  uint8_t* base = static_cast<uint8_t*>(const_cast<void*>(ws));
+  V.ea = reinterpret_cast<int*>(base + L.off_ea);
+  V.eb = reinterpret_cast<int*>(base + L.off_eb);
+  V.pa = reinterpret_cast<uint16_t*>(base + L.off_pa);
+  V.pb = reinterpret_cast<uint16_t*>(base + L.off_pb);
+  V.R = base + L.off_r;
+  return PHPC_OK;
+}
+
 }  // namespace
 
 size_t ozaki2_workspace_bytes(int m, int k, int n, int nmod) { return ozaki2_layout(m, k, n, nmod).total; }
 
-int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
-                 int64_t ldc, int nmod, void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
-  const DeviceInfo* dev = current_device();
-  if (!dev) return PHPC_ERR_CUDA;
-  if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
-  const Ozaki2Layout L = ozaki2_layout(m, k, n, nmod);
-  if (!ws || ws_bytes < L.total || !aligned16(ws)) return PHPC_ERR_WORKSPACE;
-  const ModTable T = make_table(nmod, k);
-  uint8_t* base = static_cast<uint8_t*>(ws);
-  int* ea = reinterpret_cast<int*>(base + L.off_ea);
-  int* eb = reinterpret_cast<int*>(base + L.off_eb);
-  uint16_t* pa = reinterpret_cast<uint16_t*>(base + L.off_pa);
-  uint16_t* pb = reinterpret_cast<uint16_t*>(base + L.off_pb);
-  uint8_t* R = base + L.off_r;
-  int* status = device_status_ptr();
+int ozaki2_bits(int nmod, int k) { return make_table(nmod, k).bits; }
 
-  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream>>>(dA, lda, m, k, ea, status);
-  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(eb, n, kExpZero);
-  scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream>>>(dB, ldb, k, n, 256, eb, status);
-  residue_rows_kernel<<<dim3(m, ceil_div(L.ldp / 8, 128)), 128, 0, stream>>>(dA, lda, m, k, ea, T, pa, L.ldp,
-                                                                              (int64_t)m * L.ldp);
-  residue_cols_kernel<<<dim3(ceil_div(n, 64), ceil_div(k, 32)), 256, 0, stream>>>(dB, ldb, k, n, eb, T, pb, L.ldp,
-                                                                                  (int64_t)n * L.ldp);
+// Exponent scans and residue splits: A's on stream_a, B's on stream_b.
+int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int nmod,
+                    void* ws, size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b) {
+  Ozaki2Layout L;
+  Ozaki2Views V;
+  const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
+  if (rc != PHPC_OK) return rc;
+  const ModTable T = make_table(nmod, k);
+  int* status = device_status_ptr();
+  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream_a>>>(dA, lda, m, k, V.ea, status);
+  residue_rows_kernel<<<dim3(m, ceil_div(L.ldp / 8, 128)), 128, 0, stream_a>>>(dA, lda, m, k, V.ea, T, V.pa, L.ldp,
+                                                                                (int64_t)m * L.ldp);
+  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream_b>>>(V.eb, n, kExpZero);
+  scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream_b>>>(dB, ldb, k, n, 256, V.eb, status);
+  residue_cols_kernel<<<dim3(ceil_div(n, 64), ceil_div(k, 32)), 256, 0, stream_b>>>(dB, ldb, k, n, V.eb, T, V.pb,
+                                                                                    L.ldp, (int64_t)n * L.ldp);
   PHPC_CUDA_TRY(cudaGetLastError());
+  return PHPC_OK;
+}
+
+// The residue GEMMs: plane i of R = (A_i * B_i^T) mod m_i, one byte per element.
+int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
+  Ozaki2Layout L;
+  Ozaki2Views V;
+  const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
+  if (rc != PHPC_OK) return rc;
+  const ModTable T = make_table(nmod, k);
   PairList pl{};
   pl.n = nmod;
   for (int i = 0; i < nmod; ++i) {
@@ -388,14 +416,32 @@ int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const doubl
     pl.magic[i] = T.magic[i];
   }
   const int64_t rplane = (int64_t)m * L.ldr;
-  const int rc = bn == 128 ? launch_tc_slice_gemm<128, kResidue>(pa, pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
-                                                                  nullptr, nullptr, stream, R, L.ldr, rplane)
-                           : launch_tc_slice_gemm<256, kResidue>(pa, pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
-                                                                  nullptr, nullptr, stream, R, L.ldr, rplane);
+  return bn == 128 ? launch_tc_slice_gemm<128, kResidue>(V.pa, V.pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
+                                                          nullptr, nullptr, stream, V.R, L.ldr, rplane)
+                   : launch_tc_slice_gemm<256, kResidue>(V.pa, V.pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
+                                                          nullptr, nullptr, stream, V.R, L.ldr, rplane);
+}
+
+// C += CRT(R) * 2^(ea + eb - 2b).
+int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,
+                       cudaStream_t stream) {
+  Ozaki2Layout L;
+  Ozaki2Views V;
+  const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
   if (rc != PHPC_OK) return rc;
-  crt_kernel<<<dim3(m, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(R, L.ldr, rplane, m, n, ea, eb, T, dC, ldc);
+  const ModTable T = make_table(nmod, k);
+  crt_kernel<<<dim3(m, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(V.R, L.ldr, (int64_t)m * L.ldr, m, n, V.ea,
+                                                                        V.eb, T, dC, ldc);
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
+}
+
+int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
+                 int64_t ldc, int nmod, void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
+  int rc = ozaki2_prepare2(m, k, n, dA, lda, dB, ldb, nmod, ws, ws_bytes, stream, stream);
+  if (rc == PHPC_OK) rc = ozaki2_multiply(m, k, n, nmod, ws, ws_bytes, stream, bn);
+  if (rc == PHPC_OK) rc = ozaki2_reconstruct(m, k, n, dC, ldc, nmod, ws, ws_bytes, stream);
+  return rc;
 }
 
 }  // namespace phpc
@@ -405,21 +451,64 @@ extern "C" size_t phpc_ozaki2_workspace_bytes(int m, int k, int n, int moduli) {
   return phpc::ozaki2_workspace_bytes(m, k, n, moduli);
 }
 
+namespace {
+
+// Shared argument checks of the device entry points: PHPC_OK when the call
+// may proceed (the callers skip empty problems).
+int ozaki2_args(int m, int k, int n, int moduli, bool need_a, const double* dA, int64_t lda, bool need_b,
+                const double* dB, int64_t ldb, bool need_c, const double* dC, int64_t ldc) {
+  using namespace phpc;
+  if (m < 0 || k < 0 || n < 0 || moduli < kMinModuli || moduli > kMaxModuli) return PHPC_ERR_ARG;
+  if (m == 0 || n == 0 || k == 0) return PHPC_OK;
+  if ((need_a && (!dA || lda < k)) || (need_b && (!dB || ldb < n)) || (need_c && (!dC || ldc < n)))
+    return PHPC_ERR_ARG;
+  if (m > 65535 * 128 || k > 65535 * 32) return PHPC_ERR_ARG;  // launch-grid limits of the split kernels
+  return PHPC_OK;
+}
+
+}  // namespace
+
+extern "C" int phpc_default_moduli(int m, int k, int n) { return phpc::default_moduli(m, k, n); }
+
+extern "C" int phpc_ozaki2_prepare_dev(int m, int k, int n, const double* dA, int64_t lda, const double* dB,
+                                       int64_t ldb, int moduli, void* workspace, size_t workspace_bytes,
+                                       void* stream) {
+  int rc = ozaki2_args(m, k, n, moduli, true, dA, lda, true, dB, ldb, false, nullptr, 0);
+  if (rc == PHPC_OK && m > 0 && n > 0 && k > 0) {
+    const cudaStream_t st = static_cast<cudaStream_t>(stream);
+    rc = phpc::ozaki2_prepare2(m, k, n, dA, lda, dB, ldb, moduli, workspace, workspace_bytes, st, st);
+  }
+  phpc::set_last_error(rc);
+  return rc;
+}
+
+extern "C" int phpc_ozaki2_multiply_dev(int m, int k, int n, int moduli, void* workspace, size_t workspace_bytes,
+                                        void* stream) {
+  int rc = ozaki2_args(m, k, n, moduli, false, nullptr, 0, false, nullptr, 0, false, nullptr, 0);
+  if (rc == PHPC_OK && m > 0 && n > 0 && k > 0)
+    rc = phpc::ozaki2_multiply(m, k, n, moduli, workspace, workspace_bytes, static_cast<cudaStream_t>(stream),
+                               phpc::default_bn(m, k, n));
+  phpc::set_last_error(rc);
+  return rc;
+}
+
+extern "C" int phpc_ozaki2_reconstruct_dev(int m, int k, int n, double* dC, int64_t ldc, int moduli, void* workspace,
+                                           size_t workspace_bytes, void* stream) {
+  int rc = ozaki2_args(m, k, n, moduli, false, nullptr, 0, false, nullptr, 0, true, dC, ldc);
+  if (rc == PHPC_OK && m > 0 && n > 0 && k > 0)
+    rc = phpc::ozaki2_reconstruct(m, k, n, dC, ldc, moduli, workspace, workspace_bytes,
+                                  static_cast<cudaStream_t>(stream));
+  phpc::set_last_error(rc);
+  return rc;
+}
+
 extern "C" int phpc_dgemm_ozaki2_dev(int m, int k, int n, const double* dA, int64_t lda, const double* dB,
                                      int64_t ldb, double* dC, int64_t ldc, int moduli, void* workspace,
                                      size_t workspace_bytes, void* stream) {
-  using namespace phpc;
-  int rc;
-  if (m < 0 || k < 0 || n < 0 || moduli < kMinModuli || moduli > kMaxModuli) {
-    rc = PHPC_ERR_ARG;
-  } else if (m == 0 || n == 0 || k == 0) {
-    rc = PHPC_OK;
-  } else if (!dA || !dB || !dC || lda < k || ldb < n || ldc < n || m > 65535 * 128) {
-    rc = PHPC_ERR_ARG;
-  } else {
-    rc = dgemm_ozaki2(m, k, n, dA, lda, dB, ldb, dC, ldc, moduli, workspace, workspace_bytes,
-                      static_cast<cudaStream_t>(stream), default_bn(m, k, n));
-  }
-  set_last_error(rc);
+  int rc = ozaki2_args(m, k, n, moduli, true, dA, lda, true, dB, ldb, true, dC, ldc);
+  if (rc == PHPC_OK && m > 0 && n > 0 && k > 0)
+    rc = phpc::dgemm_ozaki2(m, k, n, dA, lda, dB, ldb, dC, ldc, moduli, workspace, workspace_bytes,
+                            static_cast<cudaStream_t>(stream), phpc::default_bn(m, k, n));
+  phpc::set_last_error(rc);
   return rc;
 }

@@ -53,6 +53,12 @@ size_t ozaki_workspace_bytes(int m, int k, int n, int s);
 size_t ozaki2_workspace_bytes(int m, int k, int n, int nmod);
 int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
                  int64_t ldc, int nmod, void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
+int ozaki2_bits(int nmod, int k);
+int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int nmod,
+                    void* ws, size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b);
+int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
+int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,
+                       cudaStream_t stream);
 int ozaki_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
                    size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b);
 int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const void* ws, size_t ws_bytes,
@@ -61,6 +67,9 @@ int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const vo
 // unless PHPC_POOL_KEEP=0): buffers of one call are reused by the next.
 cudaMemPool_t host_api_pool();
 int default_slices(int m, int k, int n);
+// Number of moduli of the modular scheme for this shape, or 0 for the digit
+// scheme (default_slices slices).
+int default_moduli(int m, int k, int n);
 int default_bn(int m, int k, int n);
 int default_grouped_bn(const phpc_gemm_problem* problems, int count);
 int default_group_rows(int m, int k, int n);

@@ -1,10 +1,13 @@
-// Slice-count selection for the Ozaki GEMM.
+// Scheme and tile selection for the FP64-accurate Ozaki GEMMs.
 //
-// Order of precedence: the PHPC_SLICES environment variable (2..8), then the
+// Order of precedence for each choice: an environment variable, then the
 // tuning table written by the autotuner (PHPC_TUNE_TABLE, or tune_table.txt
-// next to the library), then the built-in default of 7 slices (55-bit digit
-// grids: Frobenius error well below 1e-14 even for inputs whose exponents
-// spread over 2^+-20 inside a row).
+// next to the library), then a built-in default. Schemes: the modular one
+// (PHPC_MODULI = 8..16 residue GEMMs; built-in default: the fewest moduli
+// whose operand grid has at least 51 bits, Frobenius error about 2e-15 on
+// inputs whose exponents spread over 2^+-20 inside a row) or, with
+// PHPC_MODULI=0 or a table entry of 0 moduli, the digit scheme (PHPC_SLICES =
+// 2..8 slices, default 7: 55-bit digit grids).
 #include <dlfcn.h>
 
 #include <cstdio>
@@ -19,12 +22,15 @@
 namespace phpc {
 namespace {
 
+constexpr int kMinModuliCount = 8, kMaxModuliCount = 16;  // range of the modular scheme
+
 struct TuneEntry {
   long long max_mnk;  // entry applies to problems with m*n*k <= max_mnk (first match wins)
   int slices;
   int bn;
   int group_rows;     // L2 raster height of the persistent tile order (0 = default 8)
   int cluster;        // CTAs per cluster sharing B (1 or 2; 0 = default 1)
+  int moduli;         // modular scheme with this many moduli; 0 = digit scheme; -1 = built-in rule
 };
 
 std::once_flag g_once;
@@ -41,7 +47,7 @@ std::string library_dir() {
   return ".";
 }
 
-// Table format (text): one entry per line, "max_mnk slices bn [group_rows [cluster]]"
+// Table format (text): one entry per line, "max_mnk slices bn [group_rows [cluster [moduli]]]"
 // for single problems or "grouped max_mean_mnk slices bn" for grouped calls;
 // '#' starts a comment line. Written by autotune.py.
 void load_table() {
@@ -59,10 +65,12 @@ void load_table() {
         g_grouped.push_back(e);
       continue;
     }
-    const int got = sscanf(line, "%lld %d %d %d %d", &e.max_mnk, &e.slices, &e.bn, &e.group_rows, &e.cluster);
+    const int got = sscanf(line, "%lld %d %d %d %d %d", &e.max_mnk, &e.slices, &e.bn, &e.group_rows, &e.cluster,
+                           &e.moduli);
     if (got >= 3 && e.slices >= 2 && e.slices <= 8 && (e.bn == 128 || e.bn == 256)) {
       if (got < 4 || e.group_rows < 1 || e.group_rows > 64) e.group_rows = 0;
       if (got < 5 || (e.cluster != 1 && e.cluster != 2)) e.cluster = 0;
+      if (got < 6 || (e.moduli != 0 && (e.moduli < kMinModuliCount || e.moduli > kMaxModuliCount))) e.moduli = -1;
       g_table.push_back(e);
     }
   }
@@ -87,6 +95,19 @@ int default_slices(int m, int k, int n) {
   }
   if (const TuneEntry* e = lookup(m, k, n)) return e->slices;
   return 7;
+}
+
+int default_moduli(int m, int k, int n) {
+  const char* env = getenv("PHPC_MODULI");
+  if (env) {
+    const int q = atoi(env);
+    if (q == 0 || (q >= kMinModuliCount && q <= kMaxModuliCount)) return q;
+  }
+  if (const TuneEntry* e = lookup(m, k, n))
+    if (e->moduli >= 0) return e->moduli;
+  for (int q = kMinModuliCount; q < kMaxModuliCount; ++q)
+    if (ozaki2_bits(q, k) >= 51) return q;
+  return kMaxModuliCount;
 }
 
 int default_bn(int m, int k, int n) {

@@ -80,6 +80,17 @@ _lib.phpc_dgemm_ozaki2_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p
                                        ct.c_int64, ct.c_void_p, ct.c_int64, ct.c_int, ct.c_void_p, ct.c_size_t,
                                        ct.c_void_p]
 _lib.phpc_dgemm_ozaki2_dev.restype = ct.c_int
+_lib.phpc_ozaki2_prepare_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_void_p,
+                                         ct.c_int64, ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_ozaki2_prepare_dev.restype = ct.c_int
+_lib.phpc_ozaki2_multiply_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t,
+                                          ct.c_void_p]
+_lib.phpc_ozaki2_multiply_dev.restype = ct.c_int
+_lib.phpc_ozaki2_reconstruct_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_int,
+                                             ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_ozaki2_reconstruct_dev.restype = ct.c_int
+_lib.phpc_default_moduli.argtypes = [ct.c_int, ct.c_int, ct.c_int]
+_lib.phpc_default_moduli.restype = ct.c_int
 
 
 class GemmProblem(ct.Structure):
@@ -184,6 +195,11 @@ def default_slices(m, k, n) -> int:
     return int(_lib.phpc_default_slices(m, k, n))
 
 
+def default_moduli(m, k, n) -> int:
+    """Moduli of the modular scheme the host entry points use (0 = digit scheme)."""
+    return int(_lib.phpc_default_moduli(m, k, n))
+
+
 def dgemm_ozaki_dev(m, k, n, A, lda, B, ldb, C, ldc, slices, workspace, workspace_bytes, stream=None) -> None:
     _check(_lib.phpc_dgemm_ozaki_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, slices,
                                      _dptr(workspace), workspace_bytes, _stream(stream)), "phpc_dgemm_ozaki_dev")
@@ -197,6 +213,21 @@ def dgemm_ozaki2_dev(m, k, n, A, lda, B, ldb, C, ldc, moduli, workspace, workspa
     """FP64-accurate C += A @ B by the modular (CRT) Ozaki scheme with `moduli` residue GEMMs."""
     _check(_lib.phpc_dgemm_ozaki2_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc, moduli,
                                       _dptr(workspace), workspace_bytes, _stream(stream)), "phpc_dgemm_ozaki2_dev")
+
+
+def ozaki2_prepare_dev(m, k, n, A, lda, B, ldb, moduli, workspace, workspace_bytes, stream=None) -> None:
+    _check(_lib.phpc_ozaki2_prepare_dev(m, k, n, _dptr(A), lda, _dptr(B), ldb, moduli, _dptr(workspace),
+                                        workspace_bytes, _stream(stream)), "phpc_ozaki2_prepare_dev")
+
+
+def ozaki2_multiply_dev(m, k, n, moduli, workspace, workspace_bytes, stream=None) -> None:
+    _check(_lib.phpc_ozaki2_multiply_dev(m, k, n, moduli, _dptr(workspace), workspace_bytes, _stream(stream)),
+           "phpc_ozaki2_multiply_dev")
+
+
+def ozaki2_reconstruct_dev(m, k, n, C, ldc, moduli, workspace, workspace_bytes, stream=None) -> None:
+    _check(_lib.phpc_ozaki2_reconstruct_dev(m, k, n, _dptr(C), ldc, moduli, _dptr(workspace), workspace_bytes,
+                                            _stream(stream)), "phpc_ozaki2_reconstruct_dev")
 
 
 def ozaki_prepare_dev(m, k, n, A, lda, B, ldb, slices, workspace, workspace_bytes, stream=None) -> None:

@@ -94,6 +94,16 @@ size_t phpc_ozaki2_workspace_bytes(int m, int k, int n, int moduli);
 int phpc_dgemm_ozaki2_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
                           double *dC, int64_t ldc, int moduli, void *workspace, size_t workspace_bytes, void *stream);
 
+/* The three phases of phpc_dgemm_ozaki2_dev (same workspace):
+ * prepare = exponent scans + residue split of A and B;
+ * multiply = the residue GEMMs (one byte per element and modulus, in the
+ * workspace); reconstruct = CRT, rounding and C += result * 2^(ea + eb - 2b). */
+int phpc_ozaki2_prepare_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
+                            int moduli, void *workspace, size_t workspace_bytes, void *stream);
+int phpc_ozaki2_multiply_dev(int m, int k, int n, int moduli, void *workspace, size_t workspace_bytes, void *stream);
+int phpc_ozaki2_reconstruct_dev(int m, int k, int n, double *dC, int64_t ldc, int moduli, void *workspace,
+                                size_t workspace_bytes, void *stream);
+
 /* The two phases of phpc_dgemm_ozaki_dev, for callers that reuse the digit
  * planes of A and B or time the phases separately:
  * prepare = exponent scans + digit split of A and B into the workspace;
@@ -171,6 +181,12 @@ void phpc_grouped_plan_destroy(phpc_grouped_plan *plan);
 /* Slice count the host entry points use for an m x k x n problem
  * (PHPC_SLICES, else the autotuner's table, else 7). */
 int phpc_default_slices(int m, int k, int n);
+
+/* Scheme phpc_gemm_cublas uses for an m x k x n problem: the number of moduli
+ * of the modular scheme (8..16), or 0 for the digit scheme with
+ * phpc_default_slices slices (PHPC_MODULI, else the autotuner's table, else
+ * the fewest moduli giving a grid of at least 51 bits). */
+int phpc_default_moduli(int m, int k, int n);
 
 /* ------------------------------------------------------------------ utils */
 

@@ -57,8 +57,14 @@ def test_extreme_digits_exact_accumulation(phpc, torch_cuda):
     np.testing.assert_array_equal(got, ozaki_model.gemm(a, b, None, 7))
 
 
+# The host entry point phpc_gemm_cublas under both FP64-accurate schemes.
+SCHEMES = pytest.mark.parametrize("scheme", ["0", "15"], ids=["digits", "modular15"])
+
+
+@SCHEMES
 @pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] == "index"], ids=lambda c: c["name"])
-def test_index_inputs_exact(case, phpc, oracle):
+def test_index_inputs_exact(case, phpc, oracle, monkeypatch, scheme):
+    monkeypatch.setenv("PHPC_MODULI", scheme)
     a, b, c = golden_inputs(case)
     ref = c.copy()
     oracle.gemm_iterative(a, b, ref)
@@ -66,8 +72,10 @@ def test_index_inputs_exact(case, phpc, oracle):
     np.testing.assert_array_equal(c, ref)
 
 
+@SCHEMES
 @pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] != "index"], ids=lambda c: c["name"])
-def test_golden_within_tolerance(case, phpc, oracle):
+def test_golden_within_tolerance(case, phpc, oracle, monkeypatch, scheme):
+    monkeypatch.setenv("PHPC_MODULI", scheme)
     a, b, c = golden_inputs(case)
     ref = oracle.gemm_dd(a, b, c)
     phpc.gemm_host("ozaki", a, b, c)
@@ -75,7 +83,9 @@ def test_golden_within_tolerance(case, phpc, oracle):
     assert err["frob"] <= 1e-14, err
 
 
-def test_index_n1024_exact(phpc):
+@SCHEMES
+def test_index_n1024_exact(phpc, monkeypatch, scheme):
+    monkeypatch.setenv("PHPC_MODULI", scheme)
     n = 1024
     a = np.arange(n * n, dtype=np.float64).reshape(n, n)
     c = np.zeros((n, n))
@@ -88,8 +98,10 @@ def test_index_n1024_exact(phpc):
     np.testing.assert_array_equal(c, exact)
 
 
+@SCHEMES
 @pytest.mark.parametrize("dist", ["uniform", "wide"])
-def test_n1024_frobenius_1e14(phpc, oracle, dist):
+def test_n1024_frobenius_1e14(phpc, oracle, dist, monkeypatch, scheme):
+    monkeypatch.setenv("PHPC_MODULI", scheme)
     rng = np.random.default_rng(17)
     n = 1024
     a = rng.uniform(-1, 1, (n, n))
@@ -121,7 +133,9 @@ def test_zero_rows_and_columns(phpc, torch_cuda):
     np.testing.assert_array_equal(got[:, 9], c0[:, 9])
 
 
-def test_nonfinite_inputs_follow_ieee(phpc):
+@SCHEMES
+def test_nonfinite_inputs_follow_ieee(phpc, monkeypatch, scheme):
+    monkeypatch.setenv("PHPC_MODULI", scheme)
     a = np.ones((16, 16))
     b = np.ones((16, 16))
     a[2, 3] = np.inf

@@ -93,3 +93,37 @@ def test_zero_rows_columns_and_argument_errors(phpc, torch_cuda):
     with pytest.raises(phpc.PhpcError) as e:
         phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 17, W, 16)
     assert e.value.code == 1
+
+
+def test_phases_equal_one_call(phpc, torch_cuda):
+    """prepare + multiply + reconstruct on one workspace == phpc_dgemm_ozaki2_dev."""
+    torch = torch_cuda
+    rng = np.random.default_rng(9)
+    m, k, n = 260, 700, 390
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+    b = rng.uniform(-1, 1, (k, n))
+    c0 = rng.uniform(-1, 1, (m, n))
+    want = run_dev(phpc, torch, a, b, c0, 15)
+    A, B, C = (torch.from_numpy(x).cuda() for x in (a, b, c0))
+    ws = phpc.ozaki2_workspace_bytes(m, k, n, 15)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    phpc.ozaki2_prepare_dev(m, k, n, A, k, B, n, 15, W, ws)
+    phpc.ozaki2_multiply_dev(m, k, n, 15, W, ws)
+    phpc.ozaki2_reconstruct_dev(m, k, n, C, n, 15, W, ws)
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    np.testing.assert_array_equal(C.cpu().numpy(), want)
+
+
+def test_host_entry_uses_modular_scheme(phpc, monkeypatch):
+    """phpc_gemm_cublas with PHPC_MODULI=q computes the modular scheme's bits."""
+    rng = np.random.default_rng(10)
+    a = rng.uniform(-1, 1, (150, 333)) * np.exp2(rng.integers(-20, 21, (150, 333)))
+    b = rng.uniform(-1, 1, (333, 170))
+    c = rng.uniform(-1, 1, (150, 170))
+    want = ozaki2_model.gemm(a, b, c, 13)
+    monkeypatch.setenv("PHPC_MODULI", "13")
+    assert phpc.default_moduli(150, 333, 170) == 13
+    phpc.gemm_host("ozaki", a, b, c)
+    np.testing.assert_array_equal(c, want)
+

@@ -11,18 +11,20 @@ PKG = ROOT / "hpc-multigpu-matrixmult_gb300"
 PROBE = """
 import sys, ctypes as ct
 L = ct.CDLL(sys.argv[1])
-L.phpc_default_slices.argtypes = [ct.c_int] * 3
-print(",".join(str(L.phpc_default_slices(n, n, n)) for n in (256, 1024, 4096, 16384)))
+f = getattr(L, sys.argv[2])
+f.argtypes = [ct.c_int] * 3
+print(",".join(str(f(n, n, n)) for n in (256, 1024, 4096, 16384)))
 """
 
 
-def _probe(built, env_extra):
+def _probe(built, env_extra, fn="phpc_default_slices"):
     import os
 
     env = dict(os.environ)
     env.pop("PHPC_SLICES", None)
+    env.pop("PHPC_MODULI", None)
     env.update(env_extra)
-    r = subprocess.run([sys.executable, "-c", PROBE, str(PKG / "lib" / "libphpc_gemm.so")], env=env,
+    r = subprocess.run([sys.executable, "-c", PROBE, str(PKG / "lib" / "libphpc_gemm.so"), fn], env=env,
                        capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr
     return [int(x) for x in r.stdout.strip().split(",")]
@@ -40,6 +42,22 @@ def test_env_overrides_and_default(built, tmp_path):
     assert _probe(built, {"PHPC_TUNE_TABLE": str(tmp_path / "missing.txt"), "PHPC_SLICES": "4"}) == [4, 4, 4, 4]
 
 
+def test_scheme_selection(built, tmp_path):
+    """Sixth column: moduli of the modular scheme (0 = digit scheme); without it
+    the built-in rule picks the fewest moduli with a grid of >= 51 bits."""
+    import ozaki2_model
+
+    t = tmp_path / "table.txt"
+    t.write_text(f"{1024**3} 7 128 8 1 0\n" + f"{4096**3} 7 256 8 2 14\n" + f"{2**62} 7 256 8 1\n")
+    rule = [min(q for q in range(8, 17) if ozaki2_model.bits_for(q, n) >= 51) for n in (256, 1024, 4096, 16384)]
+    assert rule == [15, 15, 15, 15]
+    assert _probe(built, {"PHPC_TUNE_TABLE": str(t)}, "phpc_default_moduli") == [0, 0, 14, rule[3]]
+    missing = str(tmp_path / "missing.txt")
+    assert _probe(built, {"PHPC_TUNE_TABLE": missing}, "phpc_default_moduli") == rule
+    assert _probe(built, {"PHPC_TUNE_TABLE": missing, "PHPC_MODULI": "16"}, "phpc_default_moduli") == [16] * 4
+    assert _probe(built, {"PHPC_TUNE_TABLE": str(t), "PHPC_MODULI": "0"}, "phpc_default_moduli") == [0] * 4
+
+
 def test_committed_table_is_well_formed():
     lines = [ln for ln in (PKG / "tune_table.txt").read_text().splitlines() if ln and not ln.startswith("#")]
     assert lines[-1].startswith("grouped ")
@@ -48,3 +66,4 @@ def test_committed_table_is_well_formed():
         mnk, s, bn, gr = f[:4]
         assert 2 <= s <= 8 and bn in (128, 256) and 1 <= gr <= 64
         assert len(f) == 4 or f[4] in (1, 2)
+        assert len(f) <= 5 or f[5] == 0 or 8 <= f[5] <= 16
