@@ -22,11 +22,6 @@
 
 namespace phpc {
 
-template <int BN, int MODE>
-int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
-                         int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane);
-
 namespace {
 
 __device__ __forceinline__ void split3(float x, uint16_t& h1, uint16_t& h2, uint16_t& h3) {

@@ -16,8 +16,11 @@
 //    and device buffers come from a grow-only library pool (PHPC_POOL_KEEP=0
 //    returns them to the system after every call, as the reference did);
 //  - every CUDA call is checked; the outcome is kept for phpc_last_error().
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <numeric>
+#include <vector>
 
 #include "phpc_host.hpp"
 
@@ -84,6 +87,10 @@ float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
   return cudaEventElapsedTime(&ms, a, b) == cudaSuccess ? ms : 0.f;
 }
 
+int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k, int n,
+                      int nmod, float* seconds);
+
+// DMMA and digit-scheme calls (the modular scheme goes to host_gemm_modular).
 // Copies and compute of one call overlap across three streams: A (stream 0),
 // B (stream 1) and C (stream 2) travel to the device concurrently; A's and
 // B's splits (residues or digits) start as soon as their operand has arrived; the GEMM runs
@@ -100,6 +107,10 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
   const DeviceInfo* dev = current_device();
   if (!dev) return PHPC_ERR_CUDA;
   if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
+  if (method == kOzakiMethod) {
+    const int nmod = default_moduli(m, k, n);
+    if (nmod > 0) return host_gemm_modular(a, lda, b, ldb, c, ldc, m, k, n, nmod, seconds);
+  }
   cudaMemPool_t pool = host_api_pool();
   int* status = device_status_ptr();
   if (!pool || !status) return PHPC_ERR_CUDA;
@@ -120,16 +131,11 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
     // events: 0 allocated, 1 B ready (split done / copied), 2 C copied,
     //         3/4 A-side kernels, 5/6 B-side kernels, 7 GEMM start
     cudaStream_t s0 = r.st[0], s1 = r.st[1], s2 = r.st[2];
-    int slices = 0, moduli = 0;
+    int slices = 0;
     size_t ws_bytes = 0;
     if (method == kOzakiMethod) {
-      moduli = default_moduli(m, k, n);
-      if (moduli > 0) {
-        ws_bytes = ozaki2_workspace_bytes(m, k, n, moduli);
-      } else {
-        slices = default_slices(m, k, n);
-        ws_bytes = ozaki_workspace_bytes(m, k, n, slices);
-      }
+      slices = default_slices(m, k, n);
+      ws_bytes = ozaki_workspace_bytes(m, k, n, slices);
     }
     if (rc == PHPC_OK &&
         (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, pool, s0) !=
@@ -158,8 +164,7 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
       if (method == kOzakiMethod) {
         cudaEventRecord(r.ev[3], s0);
         cudaEventRecord(r.ev[5], s1);
-        rc = moduli > 0 ? ozaki2_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, moduli, r.ws, ws_bytes, s0, s1)
-                        : ozaki_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, slices, r.ws, ws_bytes, s0, s1);
+        rc = ozaki_prepare2(m, k, n, r.dA, dlda, r.dB, dldb, slices, r.ws, ws_bytes, s0, s1);
         cudaEventRecord(r.ev[4], s0);
         cudaEventRecord(r.ev[6], s1);
       }
@@ -170,9 +175,6 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
       if (rc == PHPC_OK) {
         if (method == kDmma) {
           rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, gw, gh, 256, s0);
-        } else if (moduli > 0) {
-          rc = ozaki2_multiply(m, k, n, moduli, r.ws, ws_bytes, s0, default_bn(m, k, n));
-          if (rc == PHPC_OK) rc = ozaki2_reconstruct(m, k, n, r.dC, dldc, moduli, r.ws, ws_bytes, s0);
         } else {
           rc = ozaki_multiply(m, k, n, r.dC, dldc, slices, r.ws, ws_bytes, s0, default_bn(m, k, n));
         }
@@ -216,6 +218,184 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
         rc = PHPC_ERR_CUDA;
     }
     if (rc == PHPC_OK && seconds) *seconds = kernel_ms / 1000.f;
+  }
+  unpin(pc);
+  unpin(pb);
+  unpin(pa);
+  return rc;
+}
+
+// Row-panel height of the pipelined modular path: a whole number of waves
+// of output tiles per panel (tile rows x tiles per row a multiple of the
+// concurrent tiles, SMs / cluster size), at most 8 panels; problems too small
+// for two such panels use four panels of whole tile rows (or one below 2048
+// rows).
+int panel_rows(int m, int k, int n, int sms) {
+  const int bn = default_bn(m, k, n), cl = default_cluster(m, k, n);
+  const int64_t tn = ceil_div(n, bn), units = std::max(1, sms / cl);
+  const int64_t unit_rows = units / std::gcd(units, tn) * 128 * cl;
+  int64_t pr;
+  if (2 * unit_rows <= m)
+    pr = unit_rows * std::max<int64_t>(1, ceil_div(m, unit_rows * 8));
+  else if (m >= 2048)
+    pr = ceil_div(ceil_div(m, 4), 128 * cl) * (int64_t)(128 * cl);
+  else
+    pr = m;
+  return static_cast<int>(std::min<int64_t>(pr, m));
+}
+
+// phpc_gemm_cublas on the modular scheme, pipelined over row panels of A and
+// C: B travels and is split on stream sB while A's panels travel and are
+// split on sA and C's panels travel on sC; panel p's residue GEMMs and CRT
+// run on sG as soon as B and A_p (C_p for the CRT) are ready, and C_p returns
+// on sO while later panels compute. Only B's copy and split, the first
+// panel's GEMM and the last panel's copy-out are not overlapped. Inputs with
+// inf/NaN are detected after the scans, before any of C is copied back, and
+// the call is redone in IEEE FP64 (DMMA) from the original C.
+int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k, int n,
+                      int nmod, float* seconds) {
+  const DeviceInfo* dev = current_device();
+  cudaMemPool_t pool = host_api_pool();
+  int* status = device_status_ptr();
+  if (!dev || !pool || !status) return PHPC_ERR_CUDA;
+  Pinned pa, pb, pc;
+  pin(pa, a, ((size_t)(m - 1) * lda + k) * sizeof(double));
+  pin(pb, b, ((size_t)(k - 1) * ldb + n) * sizeof(double));
+  pin(pc, c, ((size_t)(m - 1) * ldc + n) * sizeof(double));
+
+  const int pr = panel_rows(m, k, n, dev->sm_count);
+  const int np = ceil_div(m, pr);
+  const int bn = default_bn(m, k, n);
+  const size_t ws_bytes = ozaki2_workspace_bytes(m, k, n, nmod);
+  int rc = PHPC_OK;
+  {
+    CallResources r;
+    cudaStream_t sx[2] = {nullptr, nullptr};  // sC (C panels in), sO (C panels out)
+    std::vector<cudaEvent_t> evs;
+    auto new_event = [&](cudaEvent_t& e) {
+      if (rc == PHPC_OK && cudaEventCreate(&e) != cudaSuccess) rc = PHPC_ERR_CUDA;
+      evs.push_back(e);
+    };
+    const int64_t dlda = (k + 1) & ~1, dldb = (n + 1) & ~1, dldc = (n + 1) & ~1;
+    for (auto& x : r.st)
+      if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    for (auto& x : sx)
+      if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    cudaStream_t sB = r.st[0], sA = r.st[1], sG = r.st[2], sC = sx[0], sO = sx[1];
+    cudaEvent_t ev_alloc{}, ev_bcopy{}, ev_b0{}, ev_b1{}, ev_g0{}, ev_g1{};
+    std::vector<cudaEvent_t> ev_a0(np), ev_a1(np), ev_c(np), ev_g(np);
+    for (cudaEvent_t* e : {&ev_alloc, &ev_bcopy, &ev_b0, &ev_b1, &ev_g0, &ev_g1}) new_event(*e);
+    for (int p = 0; p < np; ++p) {
+      new_event(ev_a0[p]);
+      new_event(ev_a1[p]);
+      new_event(ev_c[p]);
+      new_event(ev_g[p]);
+    }
+    if (rc == PHPC_OK &&
+        (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, pool, sB) !=
+             cudaSuccess ||
+         cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dB), sizeof(double) * k * dldb, pool, sB) !=
+             cudaSuccess ||
+         cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dC), sizeof(double) * m * dldc, pool, sB) !=
+             cudaSuccess ||
+         cudaMallocFromPoolAsync(&r.ws, ws_bytes, pool, sB) != cudaSuccess))
+      rc = PHPC_ERR_NOMEM;
+    if (rc == PHPC_OK) {
+      cudaMemsetAsync(status, 0, sizeof(int), sB);
+      cudaEventRecord(ev_alloc, sB);
+      for (cudaStream_t st : {sA, sG, sC, sO}) cudaStreamWaitEvent(st, ev_alloc, 0);
+      // B: copy, then exponent scan and residue split
+      if (cudaMemcpy2DAsync(r.dB, dldb * 8, b, (size_t)ldb * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, sB) !=
+          cudaSuccess)
+        rc = PHPC_ERR_CUDA;
+      cudaEventRecord(ev_bcopy, sB);
+      cudaEventRecord(ev_b0, sB);
+      if (rc == PHPC_OK) rc = ozaki2_prepare_b(m, k, n, r.dB, dldb, nmod, r.ws, ws_bytes, sB);
+      cudaEventRecord(ev_b1, sB);
+      // A panels: copy, scan and split; C panels: copy (after B's copy)
+      cudaStreamWaitEvent(sC, ev_bcopy, 0);
+      for (int p = 0; p < np && rc == PHPC_OK; ++p) {
+        const int r0 = p * pr, rows = std::min(pr, m - r0);
+        if (cudaMemcpy2DAsync(r.dA + (int64_t)r0 * dlda, dlda * 8, a + (int64_t)r0 * lda, (size_t)lda * 8,
+                              (size_t)k * 8, rows, cudaMemcpyHostToDevice, sA) != cudaSuccess ||
+            cudaMemcpy2DAsync(r.dC + (int64_t)r0 * dldc, dldc * 8, c + (int64_t)r0 * ldc, (size_t)ldc * 8,
+                              (size_t)n * 8, rows, cudaMemcpyHostToDevice, sC) != cudaSuccess) {
+          rc = PHPC_ERR_CUDA;
+          break;
+        }
+        cudaEventRecord(ev_c[p], sC);
+        cudaEventRecord(ev_a0[p], sA);
+        rc = ozaki2_prepare_a_rows(m, r0, rows, k, n, r.dA, dlda, nmod, r.ws, ws_bytes, sA);
+        cudaEventRecord(ev_a1[p], sA);
+      }
+      // residue GEMMs and CRT per panel
+      cudaStreamWaitEvent(sG, ev_b1, 0);
+      for (int p = 0; p < np && rc == PHPC_OK; ++p) {
+        const int r0 = p * pr, rows = std::min(pr, m - r0);
+        cudaStreamWaitEvent(sG, ev_a1[p], 0);
+        if (p == 0) cudaEventRecord(ev_g0, sG);
+        rc = ozaki2_multiply_rows(m, r0, rows, k, n, nmod, r.ws, ws_bytes, sG, bn);
+        cudaStreamWaitEvent(sG, ev_c[p], 0);
+        if (rc == PHPC_OK) rc = ozaki2_reconstruct_rows(m, r0, rows, k, n, r.dC, dldc, nmod, r.ws, ws_bytes, sG);
+        cudaEventRecord(ev_g[p], sG);
+      }
+      cudaEventRecord(ev_g1, sG);
+    }
+    // The scans have flagged inf/NaN (if any) once B's and the last A panel's
+    // preparation are done: check before any of C returns to the host.
+    int dstatus = 0;
+    if (rc == PHPC_OK && (cudaEventSynchronize(ev_b1) != cudaSuccess ||
+                          cudaEventSynchronize(ev_a1[np - 1]) != cudaSuccess ||
+                          cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+      rc = PHPC_ERR_CUDA;
+    const bool nonfinite = rc == PHPC_OK && (dstatus & 0xFF) == PHPC_ERR_NONFINITE;
+    if (rc == PHPC_OK && !nonfinite) {
+      for (int p = 0; p < np; ++p) {
+        const int r0 = p * pr, rows = std::min(pr, m - r0);
+        cudaStreamWaitEvent(sO, ev_g[p], 0);
+        if (cudaMemcpy2DAsync(c + (int64_t)r0 * ldc, (size_t)ldc * 8, r.dC + (int64_t)r0 * dldc, dldc * 8,
+                              (size_t)n * 8, rows, cudaMemcpyDeviceToHost, sO) != cudaSuccess) {
+          rc = PHPC_ERR_CUDA;
+          break;
+        }
+      }
+    }
+    for (cudaStream_t st : {sB, sA, sC, sG, sO})
+      if (cudaStreamSynchronize(st) != cudaSuccess && rc == PHPC_OK) rc = PHPC_ERR_CUDA;
+    if (rc == PHPC_OK && cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = PHPC_ERR_CUDA;
+    float kernel_ms = 0.f;
+    if (rc == PHPC_OK) {
+      kernel_ms = elapsed_ms(ev_b0, ev_b1) + elapsed_ms(ev_g0, ev_g1);
+      for (int p = 0; p < np; ++p) kernel_ms += elapsed_ms(ev_a0[p], ev_a1[p]);
+    }
+    if (rc == PHPC_OK && nonfinite) {
+      // inf/NaN cannot be carried by integers: redo the call in IEEE FP64
+      // (DMMA) from the original C, which has not been copied back.
+      dstatus = 0;
+      if (cudaMemsetAsync(status, 0, sizeof(int), sB) != cudaSuccess ||
+          cudaMemcpy2DAsync(r.dC, dldc * 8, c, (size_t)ldc * 8, (size_t)n * 8, m, cudaMemcpyHostToDevice, sB) !=
+              cudaSuccess)
+        rc = PHPC_ERR_CUDA;
+      cudaEventRecord(ev_g0, sB);
+      if (rc == PHPC_OK) rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, 1, 1, 256, sB);
+      cudaEventRecord(ev_g1, sB);
+      if (rc == PHPC_OK &&
+          (cudaMemcpy2DAsync(c, (size_t)ldc * 8, r.dC, dldc * 8, (size_t)n * 8, m, cudaMemcpyDeviceToHost, sB) !=
+               cudaSuccess ||
+           cudaStreamSynchronize(sB) != cudaSuccess ||
+           cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
+        rc = PHPC_ERR_CUDA;
+      if (rc == PHPC_OK) kernel_ms = elapsed_ms(ev_g0, ev_g1);
+    }
+    if (rc == PHPC_OK && dstatus != 0) rc = dstatus;
+    if (rc == PHPC_OK && seconds) *seconds = kernel_ms / 1000.f;
+    // the pool allocations are released on sB by ~CallResources; the other
+    // streams are idle (synchronised above)
+    for (cudaStream_t st : sx)
+      if (st) cudaStreamDestroy(st);
+    for (cudaEvent_t e : evs)
+      if (e) cudaEventDestroy(e);
   }
   unpin(pc);
   unpin(pb);

@@ -92,21 +92,25 @@ PairList ozaki_pairs(int s) {
 
 }  // namespace
 
-// Launches the tcgen05 slice GEMM over bf16 planes (shared with the 3xBF16 path).
+// Launches the tcgen05 slice GEMM over bf16 planes (shared with the 3xBF16
+// and modular paths).
 template <int BN, int MODE>
 int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
                          int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane) {
+                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane, const TcGemmOpts& opt) {
   using Cfg = TcCfg<BN>;
   const DeviceInfo* dev = current_device();
   if (!dev) return PHPC_ERR_CUDA;
   CUtensorMap tmA, tmB;
   const uint64_t dA[3] = {(uint64_t)k, (uint64_t)m, (uint64_t)nplanesA};
-  const uint64_t sA[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * m};
+  const int64_t a_plane_rows = opt.a_plane_rows > 0 ? opt.a_plane_rows : m;
+  const uint64_t sA[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * a_plane_rows};
   const uint32_t bA[3] = {kTcBK, kTcBM, 1};
   const uint64_t dB[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)nplanesB};
   const uint64_t sB[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * n};
-  const int cluster = default_cluster(m, k, n);
+  const int cm = opt.cfg_m > 0 ? opt.cfg_m : m, cn = opt.cfg_n > 0 ? opt.cfg_n : n,
+            ck = opt.cfg_k > 0 ? opt.cfg_k : k;
+  const int cluster = default_cluster(cm, ck, cn);
   const uint32_t bB[3] = {kTcBK, (uint32_t)(BN / cluster), 1};  // with a 2-CTA cluster each CTA loads half of B
   if (!encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesA, dA, sA, bA, CU_TENSOR_MAP_SWIZZLE_128B) ||
       !encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesB, dB, sB, bB, CU_TENSOR_MAP_SWIZZLE_128B))
@@ -117,7 +121,7 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.K = k;
   a.tm = ceil_div(m, kTcBM);
   a.tn = ceil_div(n, BN);
-  a.group_rows = default_group_rows(m, k, n);
+  a.group_rows = default_group_rows(cm, ck, cn);
   a.C = C;
   a.ldc = ldc;
   a.ea = ea;
@@ -165,7 +169,7 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
 #define PHPC_INSTANTIATE_TC(BN, MODE)                                                                         \
   template int launch_tc_slice_gemm<BN, MODE>(const void*, const void*, int, int, int64_t, int, int, int,         \
                                               const PairList&, void*, int64_t, const int*, const int*, cudaStream_t, \
-                                              uint8_t*, int64_t, int64_t);
+                                              uint8_t*, int64_t, int64_t, const TcGemmOpts&);
 PHPC_INSTANTIATE_TC(256, kF32)
 PHPC_INSTANTIATE_TC(128, kF32)
 PHPC_INSTANTIATE_TC(256, kResidue)

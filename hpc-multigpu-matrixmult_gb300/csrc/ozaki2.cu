@@ -31,11 +31,6 @@
 
 namespace phpc {
 
-template <int BN, int MODE>
-int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
-                         int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane);
-
 namespace {
 
 constexpr int kMaxModuli = 16;  // M < 2^126: weights in four 32-bit limbs, sums in five
@@ -49,15 +44,14 @@ struct ModTable {
   int bits;  // b: operands are integers of magnitude <= 2^b
   uint32_t m[kMaxModuli];
   uint32_t magic[kMaxModuli];  // floor(2^32 / m)
-  uint32_t c21[kMaxModuli];    // 2^21 mod m
-  uint32_t c42[kMaxModuli];    // 2^42 mod m
-  uint32_t d63[kMaxModuli];    // -2^63 mod m (removes the 2^63 offset of the operands)
-  uint32_t h[kMaxModuli];      // (m + 1) / 2: residues at or above it map to r - m
+  float cf[kMaxModuli][3];     // symmetric residues of 2^16, 2^32, 2^48 mod m (|c| <= 127)
+  float invm[kMaxModuli];      // 1 / m rounded to float
+  float mf[kMaxModuli];        // m as a float
   uint32_t W[kMaxModuli][4];   // CRT weights, little-endian 32-bit limbs
   uint32_t M[4];               // product of the moduli
   uint32_t Mhalf[4];           // floor(M / 2)
   int qlimb;                   // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
-  float Mtop;                  // (M >> 32 qlimb) as a float
+  float Minv;                  // 1 / (M >> 32 qlimb) rounded to float
 };
 
 using u128 = unsigned __int128;
@@ -78,10 +72,12 @@ ModTable make_table(int nmod, int k) {
     const uint32_t m = kModuli[i];
     T.m[i] = m;
     T.magic[i] = static_cast<uint32_t>((1ull << 32) / m);
-    T.c21[i] = static_cast<uint32_t>((1ull << 21) % m);
-    T.c42[i] = static_cast<uint32_t>((1ull << 42) % m);
-    T.d63[i] = static_cast<uint32_t>((m - (1ull << 63) % m) % m);
-    T.h[i] = (m + 1) / 2;
+    for (int j = 0; j < 3; ++j) {
+      const int64_t c = static_cast<int64_t>((1ull << (16 * (j + 1))) % m);
+      T.cf[i][j] = static_cast<float>(2 * c > static_cast<int64_t>(m) ? c - m : c);
+    }
+    T.invm[i] = 1.0f / static_cast<float>(m);
+    T.mf[i] = static_cast<float>(m);
     const u128 Mi = M / m;
     const uint32_t mi_mod = static_cast<uint32_t>(Mi % m);
     uint32_t inv = 0;
@@ -97,27 +93,42 @@ ModTable make_table(int nmod, int k) {
   int bitlen = 0;
   while (bitlen < 128 && (M >> bitlen) != 0) ++bitlen;
   T.qlimb = std::max(0, (bitlen - 20) / 32);
-  T.Mtop = static_cast<float>(static_cast<double>(static_cast<uint64_t>(M >> (32 * T.qlimb))));
+  T.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.qlimb))));
   return T;
 }
 
-// The operand integer V = sign * X (X <= 2^62) is handled as V + 2^63, which
-// is non-negative, in three limbs of 21, 21 and 22 bits.
-__device__ __forceinline__ void offset_limbs(uint64_t X, bool neg, uint32_t& L0, uint32_t& L1, uint32_t& L2) {
-  const uint64_t V = (1ull << 63) + (neg ? 0ull - X : X);
-  L0 = static_cast<uint32_t>(V & 0x1FFFFF);
-  L1 = static_cast<uint32_t>((V >> 21) & 0x1FFFFF);
-  L2 = static_cast<uint32_t>(V >> 42);
+// The operand integer V = sign * X (X <= 2^62) as four balanced 16-bit limbs
+// held in floats: V = sum L_j 2^(16 j), |L_j| <= 2^15 (|L_3| <= 2^14 + 1).
+__device__ __forceinline__ void balanced_limbs(uint64_t X, bool neg, float (&L)[4]) {
+  uint64_t x = X;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const int d = static_cast<int>(x & 0xFFFFu);
+    const int c = d >= 0x8000;
+    const int l = d - (c << 16);
+    L[j] = float_of_small_int(neg ? -l : l);
+    x = (x >> 16) + static_cast<uint64_t>(c);
+  }
+  const int l3 = static_cast<int>(x);
+  L[3] = float_of_small_int(neg ? -l3 : l3);
 }
 
-// Symmetric residue of V modulo m_i, |v| <= m_i / 2 <= 128:
-// t = L2 (2^42 mod m) + L1 (2^21 mod m) + L0 + (-2^63 mod m) < 2^31 is
-// congruent to V; t - floor(t * floor(2^32 / m) / 2^32) * m lies in [0, 2m).
-__device__ __forceinline__ int residue_of(uint32_t L0, uint32_t L1, uint32_t L2, const ModTable& T, int i) {
-  const uint32_t m = T.m[i];
-  const uint32_t t = L2 * T.c42[i] + L1 * T.c21[i] + L0 + T.d63[i];
-  const uint32_t r = t - __umulhi(t, T.magic[i]) * m;
-  return static_cast<int>(r) - static_cast<int>(m) * ((r >= T.h[i]) + (r >= m + T.h[i]));
+// Residue of V modulo m_i with |r| <= 128, in single precision, exactly:
+// t = L_0 + sum_j L_j (2^(16 j) mod m) is an integer with |t| < 2^24 (exact in
+// float at every step); q = round(t * fl(1/m)) through the 1.5 * 2^23 rounding
+// constant is round(t / m) except within 0.004 of a tie, so r = t - q m (one
+// exact FMA) satisfies |r| <= 0.504 m, i.e. |r| <= 128 for m <= 255 (and r
+// is the symmetric residue exactly for m = 256, where 1/m is exact).
+__device__ __forceinline__ float residue_of(const float (&L)[4], const ModTable& T, int i) {
+  const float t = fmaf(L[3], T.cf[i][2], fmaf(L[2], T.cf[i][1], fmaf(L[1], T.cf[i][0], L[0])));
+  const float q = fmaf(t, T.invm[i], 12582912.0f) - 12582912.0f;
+  return fmaf(-q, T.mf[i], t);
+}
+
+// Two residues as a packed BF16 pair (lo in the low half): integer-valued
+// floats of magnitude <= 128 have zero low 16 bits.
+__device__ __forceinline__ uint32_t bf16x2_of_float_ints(float lo, float hi) {
+  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
 }
 
 // A residue planes [n][M][ldp]: blockIdx.x = row, each thread 8 consecutive k.
@@ -129,20 +140,18 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
   if (row >= M || k0 >= ldp) return;
   const int e = ea[row];
   const double* a = A + row * lda;
-  uint32_t L0[8], L1[8], L2[8];
+  float L[8][4];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     bool neg;
     const uint64_t X = fixed_point(k0 + j < K ? a[k0 + j] : 0.0, e, T.bits, neg);
-    offset_limbs(X, neg, L0[j], L1[j], L2[j]);
+    balanced_limbs(X, neg, L[j]);
   }
   uint16_t* out = planes + row * ldp + k0;
   for (int i = 0; i < T.n; ++i) {
     uint32_t w[4];
 #pragma unroll
-    for (int j = 0; j < 8; j += 2)
-      w[j >> 1] = bf16x2_of_small_ints(residue_of(L0[j], L1[j], L2[j], T, i),
-                                       residue_of(L0[j + 1], L1[j + 1], L2[j + 1], T, i));
+    for (int j = 0; j < 8; j += 2) w[j >> 1] = bf16x2_of_float_ints(residue_of(L[j], T, i), residue_of(L[j + 1], T, i));
     *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
@@ -161,15 +170,15 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
   const int64_t j0 = (int64_t)blockIdx.x * 64;
   const int64_t col = j0 + j;
   const int e = col < N ? eb[col] : kExpZero;
-  uint32_t L0[8], L1[8], L2[8];
+  float L[8][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) {  // k pairs kp0, kp0 + 4, ...: elements 2u, 2u + 1
     const int64_t k = k0 + 2 * (kp0 + 4 * u);
     bool n0, n1;
     const uint64_t X0 = fixed_point((col < N && k < K) ? B[k * ldb + col] : 0.0, e, T.bits, n0);
     const uint64_t X1 = fixed_point((col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0, e, T.bits, n1);
-    offset_limbs(X0, n0, L0[2 * u], L1[2 * u], L2[2 * u]);
-    offset_limbs(X1, n1, L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1]);
+    balanced_limbs(X0, n0, L[2 * u]);
+    balanced_limbs(X1, n1, L[2 * u + 1]);
   }
   const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;
   const int64_t gj = j0 + wj, gk = k0 + 8 * q;
@@ -178,8 +187,7 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
     for (int p = 0; p < cnt; ++p) {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        st[p][j][kp0 + 4 * u] = bf16x2_of_small_ints(residue_of(L0[2 * u], L1[2 * u], L2[2 * u], T, i0 + p),
-                                                     residue_of(L0[2 * u + 1], L1[2 * u + 1], L2[2 * u + 1], T, i0 + p));
+        st[p][j][kp0 + 4 * u] = bf16x2_of_float_ints(residue_of(L[2 * u], T, i0 + p), residue_of(L[2 * u + 1], T, i0 + p));
     }
     __syncthreads();
     if (gj < N && gk < ldp)
@@ -208,7 +216,7 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const ModTable& T,
   // at limb qlimb (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20: error well
   // below one), then corrected by at most one in either direction
   const float top = static_cast<float>((static_cast<uint64_t>(l[T.qlimb + 1]) << 32) | l[T.qlimb]);
-  const uint32_t q = static_cast<uint32_t>(top / T.Mtop);
+  const uint32_t q = static_cast<uint32_t>(top * T.Minv);
   uint32_t rr[5];
   uint64_t carry = 0;
   uint32_t borrow = 0;
@@ -379,32 +387,59 @@ size_t ozaki2_workspace_bytes(int m, int k, int n, int nmod) { return ozaki2_lay
 
 int ozaki2_bits(int nmod, int k) { return make_table(nmod, k).bits; }
 
-// Exponent scans and residue splits: A's on stream_a, B's on stream_b.
-int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int nmod,
-                    void* ws, size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b) {
+// Rows [r0, r0 + rows) of A (an m x k operand, dA its row 0): exponent scan
+// and residue split into the planes of the full problem.
+int ozaki2_prepare_a_rows(int m, int r0, int rows, int k, int n, const double* dA, int64_t lda, int nmod, void* ws,
+                          size_t ws_bytes, cudaStream_t stream) {
+  Ozaki2Layout L;
+  Ozaki2Views V;
+  const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
+  if (rc != PHPC_OK) return rc;
+  if (r0 < 0 || rows <= 0 || r0 + rows > m) return PHPC_ERR_ARG;
+  const ModTable T = make_table(nmod, k);
+  const double* a = dA + (int64_t)r0 * lda;
+  scan_rows_kernel<<<ceil_div(rows, 8), 256, 0, stream>>>(a, lda, rows, k, V.ea + r0, device_status_ptr());
+  residue_rows_kernel<<<dim3(rows, ceil_div(L.ldp / 8, 128)), 128, 0, stream>>>(
+      a, lda, rows, k, V.ea + r0, T, V.pa + (int64_t)r0 * L.ldp, L.ldp, (int64_t)m * L.ldp);
+  PHPC_CUDA_TRY(cudaGetLastError());
+  return PHPC_OK;
+}
+
+// B (k x n): exponent scan and residue split.
+int ozaki2_prepare_b(int m, int k, int n, const double* dB, int64_t ldb, int nmod, void* ws, size_t ws_bytes,
+                     cudaStream_t stream) {
   Ozaki2Layout L;
   Ozaki2Views V;
   const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
   if (rc != PHPC_OK) return rc;
   const ModTable T = make_table(nmod, k);
-  int* status = device_status_ptr();
-  scan_rows_kernel<<<ceil_div(m, 8), 256, 0, stream_a>>>(dA, lda, m, k, V.ea, status);
-  residue_rows_kernel<<<dim3(m, ceil_div(L.ldp / 8, 128)), 128, 0, stream_a>>>(dA, lda, m, k, V.ea, T, V.pa, L.ldp,
-                                                                                (int64_t)m * L.ldp);
-  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream_b>>>(V.eb, n, kExpZero);
-  scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream_b>>>(dB, ldb, k, n, 256, V.eb, status);
-  residue_cols_kernel<<<dim3(ceil_div(n, 64), ceil_div(k, 32)), 256, 0, stream_b>>>(dB, ldb, k, n, V.eb, T, V.pb,
-                                                                                    L.ldp, (int64_t)n * L.ldp);
+  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(V.eb, n, kExpZero);
+  scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream>>>(dB, ldb, k, n, 256, V.eb,
+                                                                                  device_status_ptr());
+  residue_cols_kernel<<<dim3(ceil_div(n, 64), ceil_div(k, 32)), 256, 0, stream>>>(dB, ldb, k, n, V.eb, T, V.pb,
+                                                                                  L.ldp, (int64_t)n * L.ldp);
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
 }
 
-// The residue GEMMs: plane i of R = (A_i * B_i^T) mod m_i, one byte per element.
-int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
+// Exponent scans and residue splits: A's on stream_a, B's on stream_b.
+int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int nmod,
+                    void* ws, size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b) {
+  int rc = ozaki2_prepare_a_rows(m, 0, m, k, n, dA, lda, nmod, ws, ws_bytes, stream_a);
+  if (rc == PHPC_OK) rc = ozaki2_prepare_b(m, k, n, dB, ldb, nmod, ws, ws_bytes, stream_b);
+  return rc;
+}
+
+// The residue GEMMs of rows [r0, r0 + rows): plane i of R = (A_i * B_i^T) mod
+// m_i, one byte per element. Tile width, cluster and raster are those of the
+// full m x k x n problem.
+int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const void* ws, size_t ws_bytes,
+                         cudaStream_t stream, int bn) {
   Ozaki2Layout L;
   Ozaki2Views V;
   const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
   if (rc != PHPC_OK) return rc;
+  if (r0 < 0 || rows <= 0 || r0 + rows > m) return PHPC_ERR_ARG;
   const ModTable T = make_table(nmod, k);
   PairList pl{};
   pl.n = nmod;
@@ -416,24 +451,41 @@ int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_byt
     pl.magic[i] = T.magic[i];
   }
   const int64_t rplane = (int64_t)m * L.ldr;
-  return bn == 128 ? launch_tc_slice_gemm<128, kResidue>(V.pa, V.pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
-                                                          nullptr, nullptr, stream, V.R, L.ldr, rplane)
-                   : launch_tc_slice_gemm<256, kResidue>(V.pa, V.pb, nmod, nmod, L.ldp, m, n, k, pl, nullptr, 0,
-                                                          nullptr, nullptr, stream, V.R, L.ldr, rplane);
+  const uint16_t* pa = V.pa + (int64_t)r0 * L.ldp;
+  uint8_t* R = V.R + (int64_t)r0 * L.ldr;
+  TcGemmOpts opt;
+  opt.a_plane_rows = m;
+  opt.cfg_m = m;
+  opt.cfg_n = n;
+  opt.cfg_k = k;
+  return bn == 128 ? launch_tc_slice_gemm<128, kResidue>(pa, V.pb, nmod, nmod, L.ldp, rows, n, k, pl, nullptr, 0,
+                                                          nullptr, nullptr, stream, R, L.ldr, rplane, opt)
+                   : launch_tc_slice_gemm<256, kResidue>(pa, V.pb, nmod, nmod, L.ldp, rows, n, k, pl, nullptr, 0,
+                                                          nullptr, nullptr, stream, R, L.ldr, rplane, opt);
 }
 
-// C += CRT(R) * 2^(ea + eb - 2b).
-int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,
-                       cudaStream_t stream) {
+int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
+  return ozaki2_multiply_rows(m, 0, m, k, n, nmod, ws, ws_bytes, stream, bn);
+}
+
+// Rows [r0, r0 + rows) of C (dC its row 0) += CRT(R) * 2^(ea + eb - 2b).
+int ozaki2_reconstruct_rows(int m, int r0, int rows, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws,
+                            size_t ws_bytes, cudaStream_t stream) {
   Ozaki2Layout L;
   Ozaki2Views V;
   const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
   if (rc != PHPC_OK) return rc;
+  if (r0 < 0 || rows <= 0 || r0 + rows > m) return PHPC_ERR_ARG;
   const ModTable T = make_table(nmod, k);
-  crt_kernel<<<dim3(m, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(V.R, L.ldr, (int64_t)m * L.ldr, m, n, V.ea,
-                                                                        V.eb, T, dC, ldc);
+  crt_kernel<<<dim3(rows, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(
+      V.R + (int64_t)r0 * L.ldr, L.ldr, (int64_t)m * L.ldr, rows, n, V.ea + r0, V.eb, T, dC + (int64_t)r0 * ldc, ldc);
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
+}
+
+int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,
+                       cudaStream_t stream) {
+  return ozaki2_reconstruct_rows(m, 0, m, k, n, dC, ldc, nmod, ws, ws_bytes, stream);
 }
 
 int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,

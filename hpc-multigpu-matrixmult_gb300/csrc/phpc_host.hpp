@@ -57,6 +57,16 @@ int ozaki2_bits(int nmod, int k);
 int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int nmod,
                     void* ws, size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b);
 int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, cudaStream_t stream, int bn);
+// Row-panel pieces of the modular scheme (device pointers to row 0 of the full
+// m-row operands; the workspace is that of the full m x k x n problem).
+int ozaki2_prepare_a_rows(int m, int r0, int rows, int k, int n, const double* dA, int64_t lda, int nmod, void* ws,
+                          size_t ws_bytes, cudaStream_t stream);
+int ozaki2_prepare_b(int m, int k, int n, const double* dB, int64_t ldb, int nmod, void* ws, size_t ws_bytes,
+                     cudaStream_t stream);
+int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const void* ws, size_t ws_bytes,
+                         cudaStream_t stream, int bn);
+int ozaki2_reconstruct_rows(int m, int r0, int rows, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws,
+                            size_t ws_bytes, cudaStream_t stream);
 int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,
                        cudaStream_t stream);
 int ozaki_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,

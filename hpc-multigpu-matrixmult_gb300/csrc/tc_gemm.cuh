@@ -587,4 +587,17 @@ inline bool tc_regs_ok(const void* kernel) {
   return fa.numRegs == kTcLaunchRegs && fa.maxThreadsPerBlock >= kTcThreads;
 }
 
+// Options of the host launcher below.
+struct TcGemmOpts {
+  int64_t a_plane_rows = 0;            // rows between consecutive A planes (0: m, the planes are m rows high)
+  int cfg_m = 0, cfg_n = 0, cfg_k = 0;  // shape whose tuning entry sets cluster and raster (0: this GEMM's)
+};
+
+// Host launcher of tc_slice_gemm_kernel (ozaki.cu) over bf16 planes
+// A [nplanesA][.][ldp] (m rows used) and B [nplanesB][n][ldp], K-major.
+template <int BN, int MODE>
+int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
+                         int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
+                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane, const TcGemmOpts& opt = {});
+
 }  // namespace phpc

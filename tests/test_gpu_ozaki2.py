@@ -127,3 +127,35 @@ def test_host_entry_uses_modular_scheme(phpc, monkeypatch):
     phpc.gemm_host("ozaki", a, b, c)
     np.testing.assert_array_equal(c, want)
 
+
+
+@pytest.mark.parametrize("m,k,n", [(2500, 300, 200), (4096, 64, 256)])
+def test_host_pipeline_panels_equal_device_call(phpc, torch_cuda, monkeypatch, m, k, n):
+    """phpc_gemm_cublas runs the modular scheme over row panels of A and C
+    (ragged last panel here); the result equals the one-call device path."""
+    monkeypatch.setenv("PHPC_MODULI", "15")
+    rng = np.random.default_rng(m + k + n)
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+    b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-20, 21, (k, n)))
+    c0 = rng.uniform(-1, 1, (m, n))
+    want = run_dev(phpc, torch_cuda, a, b, c0, 15)
+    c = c0.copy()
+    phpc.gemm_host("ozaki", a, b, c)
+    np.testing.assert_array_equal(c, want)
+
+
+def test_host_pipeline_nonfinite_in_last_panel(phpc, monkeypatch):
+    monkeypatch.setenv("PHPC_MODULI", "15")
+    rng = np.random.default_rng(12)
+    m, k, n = 2304, 96, 128
+    a = rng.uniform(-1, 1, (m, k))
+    b = rng.uniform(-1, 1, (k, n))
+    a[m - 3, 7] = np.nan
+    b[5, 17] = -np.inf
+    c = rng.uniform(-1, 1, (m, n))
+    want = c + a @ b
+    phpc.gemm_host("ozaki", a, b, c)
+    np.testing.assert_array_equal(np.isnan(c), np.isnan(want))
+    np.testing.assert_array_equal(np.isinf(c), np.isinf(want))
+    fin = np.isfinite(want)
+    np.testing.assert_allclose(c[fin], want[fin], rtol=1e-12, atol=1e-12)
