@@ -1,0 +1,200 @@
+// Chinese-remainder reconstruction of the modular Ozaki scheme, shared by
+// the standalone CRT kernel (ozaki2.cu) and the residue GEMM's fused
+// epilogue (tc_gemm.cuh).
+#pragma once
+
+#include <cstdint>
+
+namespace phpc {
+
+constexpr int kCrtMaxModuli = 16;  // M < 2^126: weights in four 32-bit limbs, sums in five
+
+struct CrtTable {
+  int n;                          // number of moduli
+  int bits;                       // b: the operands' fixed-point grid (result scale 2^(ea + eb - 2b))
+  uint32_t W[kCrtMaxModuli][4];   // CRT weights (M / m_i) ((M / m_i)^-1 mod m_i), little-endian 32-bit limbs
+  uint32_t M[4];                  // product of the moduli
+  uint32_t Mhalf[4];              // floor(M / 2)
+  int qlimb;                      // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
+  float Minv;                     // 1 / (M >> 32 qlimb) rounded to float
+  int fast;                       // 1: every result y has |y| / M <= 1/2 - 1/32 (crt_round's one-step path)
+};
+
+// c + v * 2^x for a double v and an int x, one rounding (the scaling is exact
+// unless the result leaves the normal range).
+__device__ __forceinline__ double crt_add_scaled(double c, double v, int x) {
+  const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(v));
+  const int E = static_cast<int>((bits >> 52) & 0x7FF) + x;
+  if (E >= 1 && E <= 2046)
+    return c + __longlong_as_double(static_cast<long long>((bits & ~(0x7FFull << 52)) | (static_cast<uint64_t>(E) << 52)));
+  return c + ldexp(v, x);
+}
+
+// The symmetric representative of acc mod M (acc = sum r_i W_i < 2^12 M, as
+// five 32-bit limbs) rounded once to double: returns v and sets shift so that
+// the result is v * 2^shift (v an integer-valued double, 0 for a zero result).
+__device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T, int& shift) {
+  // acc / M estimated in single precision from the 64 bits at limb qlimb
+  // (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20): absolute error < 0.01.
+  // (Limbs chosen with constant indices: an array indexed by a runtime value
+  // would live in local memory.)
+  uint32_t tlo = l[0], thi = l[1];
+  if (T.qlimb >= 1) {
+    tlo = l[1];
+    thi = l[2];
+  }
+  if (T.qlimb >= 2) {
+    tlo = l[2];
+    thi = l[3];
+  }
+  if (T.qlimb >= 3) {
+    tlo = l[3];
+    thi = l[4];
+  }
+  const float est = static_cast<float>((static_cast<uint64_t>(thi) << 32) | tlo) * T.Minv;
+  uint32_t x[4];  // magnitude of the result
+  bool neg;
+  if (T.fast) {
+    // The result y satisfies |y| / M < 1/2 - 1/32 (the table checks it), so
+    // q = round(acc / M) is exact and y = acc - q M, computed modulo 2^128,
+    // is the symmetric representative itself.
+    const uint32_t q = __float2uint_rn(est);
+    uint64_t carry = 0;
+    uint32_t borrow = 0;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const uint64_t pm = static_cast<uint64_t>(T.M[w]) * q + carry;
+      carry = pm >> 32;
+      const uint64_t sub = static_cast<uint64_t>(l[w]) - static_cast<uint32_t>(pm) - borrow;
+      x[w] = static_cast<uint32_t>(sub);
+      borrow = static_cast<uint32_t>(sub >> 63);
+    }
+    neg = (x[3] >> 31) != 0;
+    if (neg) {  // two's complement negation
+      uint32_t c = 1;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint64_t t = static_cast<uint64_t>(~x[w]) + c;
+        x[w] = static_cast<uint32_t>(t);
+        c = static_cast<uint32_t>(t >> 32);
+      }
+    }
+  } else {
+    // q = floor(acc / M) from the estimate, corrected by at most one in
+    // either direction, then the symmetric representative.
+    const uint32_t q = static_cast<uint32_t>(est);
+    uint32_t rr[5];
+    uint64_t carry = 0;
+    uint32_t borrow = 0;
+#pragma unroll
+    for (int w = 0; w < 5; ++w) {  // r = acc - q M (160-bit two's complement)
+      const uint64_t pm = (w < 4 ? static_cast<uint64_t>(T.M[w]) * q : 0) + carry;
+      carry = pm >> 32;
+      const uint64_t sub = static_cast<uint64_t>(l[w]) - static_cast<uint32_t>(pm) - borrow;
+      rr[w] = static_cast<uint32_t>(sub);
+      borrow = static_cast<uint32_t>(sub >> 63);
+    }
+    if (rr[4] & 0x80000000u) {  // negative: q was one too large, add M back
+      uint64_t c2 = 0;
+#pragma unroll
+      for (int w = 0; w < 5; ++w) {
+        const uint64_t t = static_cast<uint64_t>(rr[w]) + (w < 4 ? T.M[w] : 0) + c2;
+        rr[w] = static_cast<uint32_t>(t);
+        c2 = t >> 32;
+      }
+    } else {  // r >= M: q was one too small, subtract M
+      bool ge = rr[4] != 0;
+      if (!ge) {
+        ge = true;
+#pragma unroll
+        for (int w = 3; w >= 0; --w)
+          if (rr[w] != T.M[w]) {
+            ge = rr[w] > T.M[w];
+            break;
+          }
+      }
+      if (ge) {
+        uint32_t b2 = 0;
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+          const uint64_t t = static_cast<uint64_t>(rr[w]) - T.M[w] - b2;
+          rr[w] = static_cast<uint32_t>(t);
+          b2 = static_cast<uint32_t>(t >> 63);
+        }
+      }
+    }
+    // symmetric representative: r > M/2 -> r - M, magnitude M - r
+    bool gt_half = false;
+#pragma unroll
+    for (int w = 3; w >= 0; --w)
+      if (rr[w] != T.Mhalf[w]) {
+        gt_half = rr[w] > T.Mhalf[w];
+        break;
+      }
+#pragma unroll
+    for (int w = 0; w < 4; ++w) x[w] = rr[w];
+    neg = gt_half;
+    if (gt_half) {
+      uint32_t b2 = 0;
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint64_t t = static_cast<uint64_t>(T.M[w]) - x[w] - b2;
+        x[w] = static_cast<uint32_t>(t);
+        b2 = static_cast<uint32_t>(t >> 63);
+      }
+    }
+  }
+  const uint64_t hi = (static_cast<uint64_t>(x[3]) << 32) | x[2];
+  const uint64_t lo = (static_cast<uint64_t>(x[1]) << 32) | x[0];
+  double v;
+  if (hi == 0) {
+    v = __ull2double_rn(lo);
+    shift = 0;
+  } else {
+    // round the 128-bit magnitude to 53 bits once: its top 64 bits plus a
+    // sticky bit for everything below them, converted with round-to-nearest
+    const int lz = __clzll(static_cast<long long>(hi));
+    const uint64_t topbits = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    const uint64_t rest = lz ? (lo << lz) : lo;
+    v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
+    shift = 64 - lz;
+  }
+  return neg ? -v : v;
+}
+
+// The CRT of byte c (0..3) of each word rw[i] (the residue mod m_i of one
+// element): acc = sum r_i W_i, rounded as crt_round.
+__device__ __forceinline__ double crt_value(const uint32_t (&rw)[kCrtMaxModuli], int c, const CrtTable& T,
+                                            int& shift) {
+  // 32-bit limbs accumulated in 64 bits (no overflow: 16 x 2^8 x 2^32 < 2^45)
+  uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+  for (int i = 0; i < kCrtMaxModuli; ++i) {
+    if (i < T.n) {
+      const uint32_t r = (rw[i] >> (8 * c)) & 0xFFu;
+      a0 += static_cast<uint64_t>(r) * T.W[i][0];
+      a1 += static_cast<uint64_t>(r) * T.W[i][1];
+      a2 += static_cast<uint64_t>(r) * T.W[i][2];
+      a3 += static_cast<uint64_t>(r) * T.W[i][3];
+    }
+  }
+  uint32_t l[5];
+  uint64_t t = a0;
+  l[0] = static_cast<uint32_t>(t);
+  t = (t >> 32) + a1;
+  l[1] = static_cast<uint32_t>(t);
+  t = (t >> 32) + a2;
+  l[2] = static_cast<uint32_t>(t);
+  t = (t >> 32) + a3;
+  l[3] = static_cast<uint32_t>(t);
+  l[4] = static_cast<uint32_t>(t >> 32);
+  return crt_round(l, T, shift);
+}
+
+// *c += v * 2^(shift + e): the CRT result of one element applied to C
+// (c + 0.0 for a zero result, as an exact product would give).
+__device__ __forceinline__ void crt_apply(double* c, double v, int shift_plus_e) {
+  *c = v == 0.0 ? *c + 0.0 : crt_add_scaled(*c, v, shift_plus_e);
+}
+
+}  // namespace phpc

@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdlib>
 
+#include "crt.cuh"
 #include "ozaki_digits.cuh"
 #include "phpc_host.hpp"
 #include "tc_gemm.cuh"
@@ -33,7 +34,7 @@ namespace phpc {
 
 namespace {
 
-constexpr int kMaxModuli = 16;  // M < 2^126: weights in four 32-bit limbs, sums in five
+constexpr int kMaxModuli = kCrtMaxModuli;
 constexpr int kMinModuli = 8;
 // Pairwise coprime, largest first: 256 = 2^8, 255 = 3 5 17, 253 = 11 23, 247 = 13 19, the rest prime.
 constexpr uint32_t kModuli[kMaxModuli] = {256, 255, 253, 251, 247, 241, 239, 233,
@@ -47,11 +48,7 @@ struct ModTable {
   float cf[kMaxModuli][3];     // symmetric residues of 2^16, 2^32, 2^48 mod m (|c| <= 127)
   float invm[kMaxModuli];      // 1 / m rounded to float
   float mf[kMaxModuli];        // m as a float
-  uint32_t W[kMaxModuli][4];   // CRT weights, little-endian 32-bit limbs
-  uint32_t M[4];               // product of the moduli
-  uint32_t Mhalf[4];           // floor(M / 2)
-  int qlimb;                   // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
-  float Minv;                  // 1 / (M >> 32 qlimb) rounded to float
+  CrtTable crt;                // the reconstruction's constants
 };
 
 using u128 = unsigned __int128;
@@ -84,16 +81,23 @@ ModTable make_table(int nmod, int k) {
     for (uint32_t v = 1; v < m; ++v)
       if ((static_cast<uint64_t>(mi_mod) * v) % m == 1) { inv = v; break; }
     const u128 W = Mi * inv;  // < M
-    for (int l = 0; l < 4; ++l) T.W[i][l] = static_cast<uint32_t>(W >> (32 * l));
+    for (int l = 0; l < 4; ++l) T.crt.W[i][l] = static_cast<uint32_t>(W >> (32 * l));
   }
   for (int l = 0; l < 4; ++l) {
-    T.M[l] = static_cast<uint32_t>(M >> (32 * l));
-    T.Mhalf[l] = static_cast<uint32_t>((M >> 1) >> (32 * l));
+    T.crt.M[l] = static_cast<uint32_t>(M >> (32 * l));
+    T.crt.Mhalf[l] = static_cast<uint32_t>((M >> 1) >> (32 * l));
   }
   int bitlen = 0;
   while (bitlen < 128 && (M >> bitlen) != 0) ++bitlen;
-  T.qlimb = std::max(0, (bitlen - 20) / 32);
-  T.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.qlimb))));
+  T.crt.qlimb = std::max(0, (bitlen - 20) / 32);
+  T.crt.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.crt.qlimb))));
+  T.crt.n = T.n;
+  T.crt.bits = T.bits;
+  // |result| <= K 2^(2b) (|A'|, |B'| <= 2^b); the one-step reconstruction
+  // needs its ratio to M at most 1/2 - 1/32 (the quotient estimate errs by
+  // less than 0.01)
+  const double ratio = std::exp2(std::log2(static_cast<double>(k)) + 2.0 * T.bits - log_m);
+  T.crt.fast = ratio <= 0.5 - 1.0 / 32 - 1e-9 ? 1 : 0;
   return T;
 }
 
@@ -198,95 +202,6 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
   }
 }
 
-// c + v * 2^x for a double v and an int x, one rounding (the scaling is exact
-// unless the result leaves the normal range).
-__device__ __forceinline__ double add_scaled(double c, double v, int x) {
-  const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(v));
-  const int E = static_cast<int>((bits >> 52) & 0x7FF) + x;
-  if (E >= 1 && E <= 2046)
-    return c + __longlong_as_double(static_cast<long long>((bits & ~(0x7FFull << 52)) | (static_cast<uint64_t>(E) << 52)));
-  return c + ldexp(v, x);
-}
-
-// The symmetric representative of acc mod M (acc = sum r_i W_i < 2^12 M, as
-// five 32-bit limbs) rounded once to double: returns v and sets shift so that
-// the result is v * 2^shift (v an integer-valued double, 0 for a zero result).
-__device__ __forceinline__ double crt_round(uint32_t (&l)[5], const ModTable& T, int& shift) {
-  // q = floor(acc / M) < 2^12, estimated in single precision from the 64 bits
-  // at limb qlimb (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20: error well
-  // below one), then corrected by at most one in either direction
-  const float top = static_cast<float>((static_cast<uint64_t>(l[T.qlimb + 1]) << 32) | l[T.qlimb]);
-  const uint32_t q = static_cast<uint32_t>(top * T.Minv);
-  uint32_t rr[5];
-  uint64_t carry = 0;
-  uint32_t borrow = 0;
-#pragma unroll
-  for (int w = 0; w < 5; ++w) {  // r = acc - q M (160-bit two's complement)
-    const uint64_t pm = (w < 4 ? static_cast<uint64_t>(T.M[w]) * q : 0) + carry;
-    carry = pm >> 32;
-    const uint64_t sub = static_cast<uint64_t>(l[w]) - static_cast<uint32_t>(pm) - borrow;
-    rr[w] = static_cast<uint32_t>(sub);
-    borrow = static_cast<uint32_t>(sub >> 63);
-  }
-  if (rr[4] & 0x80000000u) {  // negative: q was one too large, add M back
-    uint64_t c2 = 0;
-#pragma unroll
-    for (int w = 0; w < 5; ++w) {
-      const uint64_t t = static_cast<uint64_t>(rr[w]) + (w < 4 ? T.M[w] : 0) + c2;
-      rr[w] = static_cast<uint32_t>(t);
-      c2 = t >> 32;
-    }
-  } else {  // r >= M: q was one too small, subtract M
-    bool ge = rr[4] != 0;
-    if (!ge) {
-      ge = true;
-#pragma unroll
-      for (int w = 3; w >= 0; --w)
-        if (rr[w] != T.M[w]) { ge = rr[w] > T.M[w]; break; }
-    }
-    if (ge) {
-      uint32_t b2 = 0;
-#pragma unroll
-      for (int w = 0; w < 4; ++w) {
-        const uint64_t t = static_cast<uint64_t>(rr[w]) - T.M[w] - b2;
-        rr[w] = static_cast<uint32_t>(t);
-        b2 = static_cast<uint32_t>(t >> 63);
-      }
-    }
-  }
-  // symmetric representative: r > M/2 -> r - M, magnitude M - r
-  bool gt_half = false;
-#pragma unroll
-  for (int w = 3; w >= 0; --w)
-    if (rr[w] != T.Mhalf[w]) { gt_half = rr[w] > T.Mhalf[w]; break; }
-  uint32_t x[4] = {rr[0], rr[1], rr[2], rr[3]};
-  if (gt_half) {
-    uint32_t b2 = 0;
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-      const uint64_t t = static_cast<uint64_t>(T.M[w]) - x[w] - b2;
-      x[w] = static_cast<uint32_t>(t);
-      b2 = static_cast<uint32_t>(t >> 63);
-    }
-  }
-  const uint64_t hi = (static_cast<uint64_t>(x[3]) << 32) | x[2];
-  const uint64_t lo = (static_cast<uint64_t>(x[1]) << 32) | x[0];
-  double v;
-  if (hi == 0) {
-    v = __ull2double_rn(lo);
-    shift = 0;
-  } else {
-    // round the 128-bit magnitude to 53 bits once: its top 64 bits plus a
-    // sticky bit for everything below them, converted with round-to-nearest
-    const int lz = __clzll(static_cast<long long>(hi));
-    const uint64_t topbits = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
-    const uint64_t rest = lz ? (lo << lz) : lo;
-    v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
-    shift = 64 - lz;
-  }
-  return gt_half ? -v : v;
-}
-
 constexpr int kCrtCols = 4;  // consecutive columns per thread (one 32-bit load per plane)
 
 // C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
@@ -298,43 +213,18 @@ __global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R,
   const int64_t c0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * kCrtCols;
   if (row >= M || c0 >= N) return;
   // c0 is a multiple of 4 below N <= ldr (a multiple of 16): the word is in the plane
-  uint32_t rw[kMaxModuli];
+  uint32_t rw[kCrtMaxModuli];
   const uint8_t* rp = R + row * ldr + c0;
 #pragma unroll
-  for (int i = 0; i < kMaxModuli; ++i) rw[i] = i < T.n ? *reinterpret_cast<const uint32_t*>(rp + i * rplane) : 0u;
+  for (int i = 0; i < kCrtMaxModuli; ++i) rw[i] = i < T.n ? *reinterpret_cast<const uint32_t*>(rp + i * rplane) : 0u;
   const int e_row = max(ea[row], -20000) - 2 * T.bits;
   double* cp = C + row * ldc + c0;
 #pragma unroll
   for (int c = 0; c < kCrtCols; ++c) {
     if (c0 + c >= N) break;
-    // acc = sum r_i W_i in 32-bit limbs accumulated in 64 bits (16 x 2^8 x 2^32 < 2^45)
-    uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-#pragma unroll
-    for (int i = 0; i < kMaxModuli; ++i) {
-      if (i < T.n) {
-        const uint32_t r = (rw[i] >> (8 * c)) & 0xFFu;
-        a0 += static_cast<uint64_t>(r) * T.W[i][0];
-        a1 += static_cast<uint64_t>(r) * T.W[i][1];
-        a2 += static_cast<uint64_t>(r) * T.W[i][2];
-        a3 += static_cast<uint64_t>(r) * T.W[i][3];
-      }
-    }
-    uint32_t l[5];
-    uint64_t t = a0;
-    l[0] = static_cast<uint32_t>(t);
-    t = (t >> 32) + a1;
-    l[1] = static_cast<uint32_t>(t);
-    t = (t >> 32) + a2;
-    l[2] = static_cast<uint32_t>(t);
-    t = (t >> 32) + a3;
-    l[3] = static_cast<uint32_t>(t);
-    l[4] = static_cast<uint32_t>(t >> 32);
     int shift;
-    const double v = crt_round(l, T, shift);
-    if (v == 0.0)
-      cp[c] = cp[c] + 0.0;
-    else
-      cp[c] = add_scaled(cp[c], v, shift + e_row + max(eb[c0 + c], -20000));
+    const double v = crt_value(rw, c, T.crt, shift);
+    crt_apply(cp + c, v, shift + e_row + max(eb[c0 + c], -20000));
   }
 }
 
