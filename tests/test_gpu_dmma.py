@@ -141,3 +141,35 @@ def test_nonfinite_propagate(phpc):
     expect = a @ b
     np.testing.assert_array_equal(np.isnan(c), np.isnan(expect))
     np.testing.assert_array_equal(c[np.isfinite(expect)], expect[np.isfinite(expect)])
+
+
+@pytest.mark.parametrize("m,k,n,tw,gw,gh", [(1024, 1024, 1024, 32, 4, 4), (384, 512, 256, 16, 3, 2),
+                                            (256, 1000, 512, 32, 8, 8)])
+def test_bit_identical_to_reference_gpu_kernel(phpc, torch_cuda, m, k, n, tw, gw, gh):
+    """The DMMA kernel reproduces the reference's own CUDA kernel
+    (src/phpc_gemm.cu gemm_kernel, compiled unchanged for sm_103a into
+    oracle/_ref by build_oracle.py) bit for bit, C accumulation included: both
+    sum each output over k in increasing order with fused multiply-adds and add
+    the sum into C once."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parent.parent / "oracle"))
+    import ref_gpu_kernel
+
+    if not ref_gpu_kernel.CUBIN.exists():
+        pytest.skip("reference kernel image not built here (needs the reference sources)")
+    torch = torch_cuda
+    rng = np.random.default_rng(m + k + n)
+    a = rng.uniform(-1, 1, (m, k))
+    b = rng.uniform(-1, 1, (k, n))
+    c0 = rng.uniform(-1, 1, (m, n))
+    A, B = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    C_ref, C_ours = torch.from_numpy(c0).cuda(), torch.from_numpy(c0).cuda()
+    st = torch.cuda.current_stream()
+    ref_gpu_kernel.RefGemmKernel().launch(A.data_ptr(), B.data_ptr(), C_ref.data_ptr(), m, n, k, tw, gw, gh,
+                                          st.cuda_stream)
+    phpc.dgemm_dmma_dev(m, k, n, A, k, B, n, C_ours, n, gw, gh, 256, st)
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    np.testing.assert_array_equal(C_ours.cpu().numpy(), C_ref.cpu().numpy())
