@@ -18,6 +18,7 @@ struct CrtTable {
   int qlimb;                      // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
   float Minv;                     // 1 / (M >> 32 qlimb) rounded to float
   int fast;                       // 1: every result y has |y| / M <= 1/2 - 1/32 (crt_round's one-step path)
+                                  //    for this table's K (grouped problems carry their own flag)
 };
 
 // c + v * 2^x for a double v and an int x, one rounding (the scaling is exact
@@ -33,7 +34,7 @@ __device__ __forceinline__ double crt_add_scaled(double c, double v, int x) {
 // The symmetric representative of acc mod M (acc = sum r_i W_i < 2^12 M, as
 // five 32-bit limbs) rounded once to double: returns v and sets shift so that
 // the result is v * 2^shift (v an integer-valued double, 0 for a zero result).
-__device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T, int& shift) {
+__device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T, int fast, int& shift) {
   // acc / M estimated in single precision from the 64 bits at limb qlimb
   // (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20): absolute error < 0.01.
   // (Limbs chosen with constant indices: an array indexed by a runtime value
@@ -54,7 +55,7 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T,
   const float est = static_cast<float>((static_cast<uint64_t>(thi) << 32) | tlo) * T.Minv;
   uint32_t x[4];  // magnitude of the result
   bool neg;
-  if (T.fast) {
+  if (fast) {
     // The result y satisfies |y| / M < 1/2 - 1/32 (the table checks it), so
     // q = round(acc / M) is exact and y = acc - q M, computed modulo 2^128,
     // is the symmetric representative itself.
@@ -163,9 +164,10 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T,
 }
 
 // The CRT of byte c (0..3) of each word rw[i] (the residue mod m_i of one
-// element): acc = sum r_i W_i, rounded as crt_round.
+// element): acc = sum r_i W_i, rounded as crt_round (fast: the one-step path,
+// allowed when the product's grid leaves the margin CrtTable::fast states).
 __device__ __forceinline__ double crt_value(const uint32_t (&rw)[kCrtMaxModuli], int c, const CrtTable& T,
-                                            int& shift) {
+                                            int fast, int& shift) {
   // 32-bit limbs accumulated in 64 bits (no overflow: 16 x 2^8 x 2^32 < 2^45)
   uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
@@ -188,7 +190,7 @@ __device__ __forceinline__ double crt_value(const uint32_t (&rw)[kCrtMaxModuli],
   t = (t >> 32) + a3;
   l[3] = static_cast<uint32_t>(t);
   l[4] = static_cast<uint32_t>(t >> 32);
-  return crt_round(l, T, shift);
+  return crt_round(l, T, fast, shift);
 }
 
 // *c += v * 2^(shift + e): the CRT result of one element applied to C

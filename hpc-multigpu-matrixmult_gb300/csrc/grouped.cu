@@ -15,6 +15,11 @@
 //    (tc_gemm.cuh, grouped mode: a tile finds its problem by binary search);
 //  - phpc_grouped_graph_launch captures those five launches once into a CUDA
 //    graph and replays it.
+// A modular-scheme plan (phpc_grouped_modular_plan_create) has six launches:
+// the two scans, residue splits of all rows and of all column blocks, the
+// persistent residue GEMM over all tiles (each tile's residues go to its
+// problem's planes), and the CRT of all rows; every problem uses the plan's
+// moduli and the grid width of its own K.
 #include <cuda.h>
 
 #include <algorithm>
@@ -24,6 +29,7 @@
 
 #include "ozaki_digits.cuh"
 #include "phpc_host.hpp"
+#include "residue.cuh"
 #include "tc_gemm.cuh"
 
 namespace phpc {
@@ -41,6 +47,12 @@ struct GSplitProb {
   int* eb;
   uint16_t* pa;
   uint16_t* pb;
+  // modular scheme only
+  uint8_t* R;       // residue planes [moduli][m][ldr]
+  int64_t ldr;
+  int bits, fast;   // the grid width for this K and the CRT path it allows
+  double* C;
+  int64_t ldc;
 };
 
 // Last problem p with start(p) <= x, over a field of the records.
@@ -96,21 +108,62 @@ __global__ void __launch_bounds__(256) g_split_cols_kernel(const GSplitProb* __r
   split_col_block(p.B, p.ldb, p.k, p.n, p.eb, s, p.pb, p.ldp, (int64_t)p.n * p.ldp, k0, j0, st);
 }
 
+// Modular scheme: residue planes of one row piece of each row.
+__global__ void g_residue_rows_kernel(const GSplitProb* __restrict__ P, int count, int total_rows,
+                                      const __grid_constant__ ModTable T) {
+  const int r = blockIdx.x;
+  if (r >= total_rows) return;
+  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
+  const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
+  if (k0 >= p.ldp) return;
+  const int64_t row = r - p.row_start;
+  residue_row_piece(p.A + row * p.lda, p.k, p.ea[row], p.bits, T, p.pa + row * p.ldp, (int64_t)p.m * p.ldp, k0);
+}
+
+__global__ void __launch_bounds__(256) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
+                                                             int total_blocks, const __grid_constant__ ModTable T) {
+  __shared__ uint32_t st[8][64][17];
+  const int b = blockIdx.x;
+  if (b >= total_blocks) return;  // uniform over the CTA
+  const GSplitProb& p = P[locate(P, count, b, [](const GSplitProb& q) { return q.sblock_start; })];
+  const int lb = b - p.sblock_start;
+  const int64_t j0 = (int64_t)(lb % p.nblk_j) * 64, k0 = (int64_t)(lb / p.nblk_j) * 32;
+  residue_col_block(p.B, p.ldb, p.k, p.n, p.eb, p.bits, T, p.pb, p.ldp, (int64_t)p.n * p.ldp, k0, j0, st);
+}
+
+// Modular scheme: C += the CRT of the residues, four columns per thread.
+__global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict__ P, int count, int total_rows,
+                                                    const __grid_constant__ ModTable T) {
+  const int r = blockIdx.x;
+  if (r >= total_rows) return;
+  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
+  const int64_t c0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * kCrtCols;
+  if (c0 >= p.n) return;
+  const int64_t row = r - p.row_start;
+  crt_cols(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
+           static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - 2 * p.bits,
+           p.eb + c0, p.C + row * p.ldc + c0);
+}
+
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct ProbLayout {
-  int64_t ldp;
-  size_t ea, eb, pa, pb, end;  // offsets relative to the problem's base
+  int64_t ldp, ldr;
+  size_t ea, eb, pa, pb, r, end;  // offsets relative to the problem's base
 };
 
-ProbLayout prob_layout(const phpc_gemm_problem& q, int s) {
+// planes = slices (digit scheme) or moduli (modular scheme, which adds the
+// residue planes R).
+ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
   ProbLayout L;
   L.ldp = ((int64_t)q.k + 7) / 8 * 8;
+  L.ldr = ((int64_t)q.n + 15) / 16 * 16;
   L.ea = 0;
   L.eb = align_up(sizeof(int) * (size_t)q.m, 256);
   L.pa = align_up(L.eb + sizeof(int) * (size_t)q.n, 256);
-  L.pb = align_up(L.pa + (size_t)s * q.m * L.ldp * 2, 256);
-  L.end = align_up(L.pb + (size_t)s * q.n * L.ldp * 2, 256);
+  L.pb = align_up(L.pa + (size_t)planes * q.m * L.ldp * 2, 256);
+  L.r = align_up(L.pb + (size_t)planes * q.n * L.ldp * 2, 256);
+  L.end = modular ? align_up(L.r + (size_t)planes * q.m * L.ldr, 256) : L.r;
   return L;
 }
 
@@ -145,16 +198,29 @@ PairList grouped_pairs(int s) {
   return pl;
 }
 
+// Modular scheme: pair i multiplies residue plane i of A and B modulo m_i.
+PairList residue_pairs(const ModTable& T) {
+  PairList pl{};
+  pl.n = T.n;
+  for (int i = 0; i < T.n; ++i) {
+    pl.a[i] = pl.b[i] = pl.g[i] = static_cast<uint8_t>(i);
+    pl.mod[i] = static_cast<uint16_t>(T.m[i]);
+    pl.magic[i] = T.magic[i];
+  }
+  return pl;
+}
+
 }  // namespace
 }  // namespace phpc
 
 struct phpc_grouped_plan {
   int device;
-  int count, s, bn;
-  int total_rows, total_cols, total_sblocks, total_tiles, max_kgroups;
+  int count, s, moduli, bn;  // moduli > 0: modular scheme (s unused)
+  int total_rows, total_cols, total_sblocks, total_tiles, max_kgroups, max_cgroups;
   phpc::GSplitProb* d_split;
   phpc::TcGroupTable table;
   phpc::PairList pairs;
+  phpc::ModTable mods;  // modular scheme: moduli constants (grid widths are per problem)
   cudaGraph_t graph;
   cudaGraphExec_t exec;
 };
@@ -162,7 +228,7 @@ struct phpc_grouped_plan {
 namespace phpc {
 namespace {
 
-template <int BN>
+template <int BN, int MODE>
 int launch_grouped_gemm(const phpc_grouped_plan* pl, cudaStream_t stream) {
   using Cfg = TcCfg<BN>;
   const DeviceInfo* dev = current_device();
@@ -172,15 +238,15 @@ int launch_grouped_gemm(const phpc_grouped_plan* pl, cudaStream_t stream) {
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   const int grid = std::min(pl->total_tiles, dev->sm_count);
-  tc_slice_gemm_kernel<BN, kOzaki, true><<<grid, kTcThreads, Cfg::kSmem, stream>>>(dummy, dummy, pl->pairs, a,
-                                                                                   pl->table);
+  tc_slice_gemm_kernel<BN, MODE, true><<<grid, kTcThreads, Cfg::kSmem, stream>>>(dummy, dummy, pl->pairs, a,
+                                                                                 pl->table);
   return cudaGetLastError() == cudaSuccess ? PHPC_OK : PHPC_ERR_CUDA;
 }
 
-template <int BN>
+template <int BN, int MODE>
 int prepare_grouped_gemm() {
   using Cfg = TcCfg<BN>;
-  auto kern = tc_slice_gemm_kernel<BN, kOzaki, true>;
+  auto kern = tc_slice_gemm_kernel<BN, MODE, true>;
   if (!tc_regs_ok(reinterpret_cast<const void*>(kern))) return PHPC_ERR_UNSUPPORTED;
   PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
   return PHPC_OK;
@@ -188,65 +254,77 @@ int prepare_grouped_gemm() {
 
 int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   int* status = device_status_ptr();
+  const bool modular = pl->moduli > 0;
   if (pl->total_rows > 0) {
     g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
                                                                         status);
     g_scan_cols_kernel<<<ceil_div(pl->total_cols, 128), 128, 0, stream>>>(pl->d_split, pl->count, pl->total_cols,
                                                                           status);
-    g_split_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
-                                                                                   pl->total_rows, pl->s);
-    g_split_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks, pl->s);
+    if (modular) {
+      g_residue_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                                       pl->total_rows, pl->mods);
+      g_residue_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks,
+                                                                   pl->mods);
+    } else {
+      g_split_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                                     pl->total_rows, pl->s);
+      g_split_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks, pl->s);
+    }
     if (cudaGetLastError() != cudaSuccess) return PHPC_ERR_CUDA;
   }
   if (pl->total_tiles == 0) return PHPC_OK;
-  return pl->bn == 128 ? launch_grouped_gemm<128>(pl, stream) : launch_grouped_gemm<256>(pl, stream);
+  int rc;
+  if (modular)
+    rc = pl->bn == 128 ? launch_grouped_gemm<128, kResidue>(pl, stream) : launch_grouped_gemm<256, kResidue>(pl, stream);
+  else
+    rc = pl->bn == 128 ? launch_grouped_gemm<128, kOzaki>(pl, stream) : launch_grouped_gemm<256, kOzaki>(pl, stream);
+  if (rc == PHPC_OK && modular) {
+    g_crt_kernel<<<dim3(pl->total_rows, pl->max_cgroups), 128, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
+                                                                            pl->mods);
+    if (cudaGetLastError() != cudaSuccess) rc = PHPC_ERR_CUDA;
+  }
+  return rc;
 }
 
-}  // namespace
-}  // namespace phpc
-
-extern "C" size_t phpc_grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int slices) {
-  using namespace phpc;
-  if (!problems || count <= 0 || slices < 2 || slices > 8) return 0;
+size_t grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int planes, bool modular) {
   size_t total = table_layout(count).end;
   for (int i = 0; i < count; ++i) {
     if (!valid_problem(problems[i])) return 0;
-    total += prob_layout(problems[i], slices).end;
+    total += prob_layout(problems[i], planes, modular).end;
   }
   return total;
 }
 
-extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* problems, int count,
-                                        int slices, void* workspace, size_t workspace_bytes, void* stream) {
-  using namespace phpc;
+// Common plan construction; planes = slices (digit scheme) or moduli.
+int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* problems, int count, int planes,
+                        bool modular, void* workspace, size_t workspace_bytes, cudaStream_t st) {
   int rc = PHPC_OK;
-  if (out) *out = nullptr;
-  if (!out || !problems || count <= 0 || count > (1 << 20) || slices < 2 || slices > 8) {
-    set_last_error(PHPC_ERR_ARG);
-    return PHPC_ERR_ARG;
-  }
+  *out = nullptr;
   for (int i = 0; i < count; ++i)
-    if (!valid_problem(problems[i])) {
-      set_last_error(PHPC_ERR_ARG);
-      return PHPC_ERR_ARG;
-    }
+    if (!valid_problem(problems[i])) return PHPC_ERR_ARG;
   const DeviceInfo* dev = current_device();
-  if (!dev) rc = PHPC_ERR_CUDA;
-  else if (dev->cc_major != 10 || dev->cc_minor != 3) rc = PHPC_ERR_UNSUPPORTED;
-  const size_t need = phpc_grouped_workspace_bytes(problems, count, slices);
-  if (rc == PHPC_OK && (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255)))
-    rc = PHPC_ERR_WORKSPACE;
-  if (rc != PHPC_OK) {
-    set_last_error(rc);
-    return rc;
-  }
+  if (!dev) return PHPC_ERR_CUDA;
+  if (dev->cc_major != 10 || dev->cc_minor != 3) return PHPC_ERR_UNSUPPORTED;
+  const size_t need = grouped_workspace_bytes(problems, count, planes, modular);
+  if (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return PHPC_ERR_WORKSPACE;
+  for (int i = 0; i < count; ++i)
+    if (modular && (problems[i].m > 65535 * 128 || problems[i].k > 65535 * 32)) return PHPC_ERR_ARG;
 
   phpc_grouped_plan* pl = new phpc_grouped_plan();
   pl->device = dev->ordinal;
   pl->count = count;
-  pl->s = slices;
+  pl->s = modular ? 0 : planes;
+  pl->moduli = modular ? planes : 0;
   pl->bn = default_grouped_bn(problems, count);
-  pl->pairs = grouped_pairs(slices);
+  if (modular) {
+    int kmax = 1;
+    for (int i = 0; i < count; ++i) kmax = std::max(kmax, problems[i].k);
+    pl->mods = make_table(planes, kmax);
+    pl->pairs = residue_pairs(pl->mods);
+  } else {
+    pl->pairs = grouped_pairs(planes);
+  }
 
   const TableLayout T = table_layout(count);
   uint8_t* base = static_cast<uint8_t*>(workspace);
@@ -254,12 +332,13 @@ extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm
   std::vector<TcGroupProblem> ht(count);
   std::vector<CUtensorMap> hm(2 * (size_t)count);
   size_t off = T.end;
-  int rows = 0, cols = 0, sblocks = 0, tiles = 0, maxkg = 1;
+  int rows = 0, cols = 0, sblocks = 0, tiles = 0, maxkg = 1, maxcg = 1;
   for (int i = 0; i < count && rc == PHPC_OK; ++i) {
     const phpc_gemm_problem& q = problems[i];
-    const ProbLayout L = prob_layout(q, slices);
+    const ProbLayout L = prob_layout(q, planes, modular);
     uint8_t* pb = base + off;
     GSplitProb& g = hs[i];
+    g = GSplitProb{};
     g.m = q.m;
     g.k = q.k;
     g.n = q.n;
@@ -276,12 +355,22 @@ extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm
     g.eb = reinterpret_cast<int*>(pb + L.eb);
     g.pa = reinterpret_cast<uint16_t*>(pb + L.pa);
     g.pb = reinterpret_cast<uint16_t*>(pb + L.pb);
+    if (modular) {
+      g.R = pb + L.r;
+      g.ldr = L.ldr;
+      g.bits = mod_grid_bits(planes, q.k);
+      g.fast = mod_crt_fast(planes, q.k, g.bits);
+      g.C = static_cast<double*>(q.C);
+      g.ldc = q.ldc;
+    }
     rows += q.m;
     cols += q.n;
     sblocks += g.nblk_j * ceil_div(q.k, 32);
     maxkg = std::max(maxkg, ceil_div(L.ldp / 8, 128));
+    maxcg = std::max(maxcg, ceil_div(q.n, 128 * kCrtCols));
 
     TcGroupProblem& t = ht[i];
+    t = TcGroupProblem{};
     t.M = q.m;
     t.N = q.n;
     t.K = q.k;
@@ -292,12 +381,17 @@ extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm
     t.ldc = q.ldc;
     t.ea = g.ea;
     t.eb = g.eb;
+    if (modular) {
+      t.R = g.R;
+      t.ldr = L.ldr;
+      t.rplane = (int64_t)q.m * L.ldr;
+    }
     tiles += t.tm * t.tn;
 
-    const uint64_t dA[3] = {(uint64_t)q.k, (uint64_t)q.m, (uint64_t)slices};
+    const uint64_t dA[3] = {(uint64_t)q.k, (uint64_t)q.m, (uint64_t)planes};
     const uint64_t sA[2] = {(uint64_t)L.ldp * 2, (uint64_t)L.ldp * 2 * q.m};
     const uint32_t bA[3] = {kTcBK, kTcBM, 1};
-    const uint64_t dB[3] = {(uint64_t)q.k, (uint64_t)q.n, (uint64_t)slices};
+    const uint64_t dB[3] = {(uint64_t)q.k, (uint64_t)q.n, (uint64_t)planes};
     const uint64_t sB[2] = {(uint64_t)L.ldp * 2, (uint64_t)L.ldp * 2 * q.n};
     const uint32_t bB[3] = {kTcBK, (uint32_t)pl->bn, 1};
     if (!encode_tiled(&hm[2 * i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, g.pa, dA, sA, bA, CU_TENSOR_MAP_SWIZZLE_128B) ||
@@ -311,15 +405,20 @@ extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm
   pl->total_sblocks = sblocks;
   pl->total_tiles = tiles;
   pl->max_kgroups = maxkg;
+  pl->max_cgroups = maxcg;
   pl->d_split = reinterpret_cast<GSplitProb*>(base + T.split);
   pl->table.count = count;
   pl->table.ntiles = tiles;
   pl->table.group_rows = 8;
   pl->table.probs = reinterpret_cast<const TcGroupProblem*>(base + T.tprob);
   pl->table.maps = reinterpret_cast<const CUtensorMap*>(base + T.maps);
-  if (rc == PHPC_OK) rc = pl->bn == 128 ? prepare_grouped_gemm<128>() : prepare_grouped_gemm<256>();
+  if (rc == PHPC_OK) {
+    if (modular)
+      rc = pl->bn == 128 ? prepare_grouped_gemm<128, kResidue>() : prepare_grouped_gemm<256, kResidue>();
+    else
+      rc = pl->bn == 128 ? prepare_grouped_gemm<128, kOzaki>() : prepare_grouped_gemm<256, kOzaki>();
+  }
   if (rc == PHPC_OK && !device_status_ptr()) rc = PHPC_ERR_CUDA;  // resolved now, not during a graph capture
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (rc == PHPC_OK &&
       (cudaMemcpyAsync(base + T.split, hs.data(), sizeof(GSplitProb) * count, cudaMemcpyHostToDevice, st) !=
            cudaSuccess ||
@@ -331,12 +430,53 @@ extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm
     rc = PHPC_ERR_CUDA;
   if (rc != PHPC_OK) {
     delete pl;
-    set_last_error(rc);
     return rc;
   }
   *out = pl;
-  set_last_error(PHPC_OK);
   return PHPC_OK;
+}
+
+}  // namespace
+}  // namespace phpc
+
+extern "C" size_t phpc_grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int slices) {
+  if (!problems || count <= 0 || slices < 2 || slices > 8) return 0;
+  return phpc::grouped_workspace_bytes(problems, count, slices, false);
+}
+
+extern "C" size_t phpc_grouped_modular_workspace_bytes(const phpc_gemm_problem* problems, int count, int moduli) {
+  if (!problems || count <= 0 || moduli < phpc::kMinModuli || moduli > phpc::kMaxModuli) return 0;
+  return phpc::grouped_workspace_bytes(problems, count, moduli, true);
+}
+
+extern "C" int phpc_grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* problems, int count,
+                                        int slices, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc;
+  if (!out || !problems || count <= 0 || count > (1 << 20) || slices < 2 || slices > 8) {
+    if (out) *out = nullptr;
+    rc = PHPC_ERR_ARG;
+  } else {
+    rc = phpc::grouped_plan_create(out, problems, count, slices, false, workspace, workspace_bytes,
+                                   static_cast<cudaStream_t>(stream));
+  }
+  phpc::set_last_error(rc);
+  return rc;
+}
+
+extern "C" int phpc_grouped_modular_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* problems,
+                                                int count, int moduli, void* workspace, size_t workspace_bytes,
+                                                void* stream) {
+  int rc;
+  if (!out || !problems || count <= 0 || count > (1 << 20) || moduli < phpc::kMinModuli ||
+      moduli > phpc::kMaxModuli) {
+    if (out) *out = nullptr;
+    rc = PHPC_ERR_ARG;
+  } else {
+    rc = phpc::grouped_plan_create(out, problems, count, moduli, true, workspace, workspace_bytes,
+                                   static_cast<cudaStream_t>(stream));
+  }
+  phpc::set_last_error(rc);
+  return rc;
 }
 
 extern "C" int phpc_grouped_run(const phpc_grouped_plan* plan, void* stream) {

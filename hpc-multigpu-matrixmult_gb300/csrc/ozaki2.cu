@@ -25,115 +25,14 @@
 #include <cmath>
 #include <cstdlib>
 
-#include "crt.cuh"
 #include "ozaki_digits.cuh"
 #include "phpc_host.hpp"
+#include "residue.cuh"
 #include "tc_gemm.cuh"
 
 namespace phpc {
 
 namespace {
-
-constexpr int kMaxModuli = kCrtMaxModuli;
-constexpr int kMinModuli = 8;
-// Pairwise coprime, largest first: 256 = 2^8, 255 = 3 5 17, 253 = 11 23, 247 = 13 19, the rest prime.
-constexpr uint32_t kModuli[kMaxModuli] = {256, 255, 253, 251, 247, 241, 239, 233,
-                                          229, 227, 223, 211, 199, 197, 193, 191};
-
-struct ModTable {
-  int n;     // number of moduli
-  int bits;  // b: operands are integers of magnitude <= 2^b
-  uint32_t m[kMaxModuli];
-  uint32_t magic[kMaxModuli];  // floor(2^32 / m)
-  float cf[kMaxModuli][3];     // symmetric residues of 2^16, 2^32, 2^48 mod m (|c| <= 127)
-  float invm[kMaxModuli];      // 1 / m rounded to float
-  float mf[kMaxModuli];        // m as a float
-  CrtTable crt;                // the reconstruction's constants
-};
-
-using u128 = unsigned __int128;
-
-ModTable make_table(int nmod, int k) {
-  ModTable T{};
-  T.n = nmod;
-  u128 M = 1;
-  double log_m = 0;
-  for (int i = 0; i < nmod; ++i) {
-    M *= kModuli[i];
-    log_m += std::log2(static_cast<double>(kModuli[i]));
-  }
-  int log_k = 1;
-  while ((1ll << log_k) < k) ++log_k;
-  T.bits = std::min(62, static_cast<int>(std::floor((log_m - 1.0 - log_k) / 2.0 - 1e-9)));
-  for (int i = 0; i < nmod; ++i) {
-    const uint32_t m = kModuli[i];
-    T.m[i] = m;
-    T.magic[i] = static_cast<uint32_t>((1ull << 32) / m);
-    for (int j = 0; j < 3; ++j) {
-      const int64_t c = static_cast<int64_t>((1ull << (16 * (j + 1))) % m);
-      T.cf[i][j] = static_cast<float>(2 * c > static_cast<int64_t>(m) ? c - m : c);
-    }
-    T.invm[i] = 1.0f / static_cast<float>(m);
-    T.mf[i] = static_cast<float>(m);
-    const u128 Mi = M / m;
-    const uint32_t mi_mod = static_cast<uint32_t>(Mi % m);
-    uint32_t inv = 0;
-    for (uint32_t v = 1; v < m; ++v)
-      if ((static_cast<uint64_t>(mi_mod) * v) % m == 1) { inv = v; break; }
-    const u128 W = Mi * inv;  // < M
-    for (int l = 0; l < 4; ++l) T.crt.W[i][l] = static_cast<uint32_t>(W >> (32 * l));
-  }
-  for (int l = 0; l < 4; ++l) {
-    T.crt.M[l] = static_cast<uint32_t>(M >> (32 * l));
-    T.crt.Mhalf[l] = static_cast<uint32_t>((M >> 1) >> (32 * l));
-  }
-  int bitlen = 0;
-  while (bitlen < 128 && (M >> bitlen) != 0) ++bitlen;
-  T.crt.qlimb = std::max(0, (bitlen - 20) / 32);
-  T.crt.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.crt.qlimb))));
-  T.crt.n = T.n;
-  T.crt.bits = T.bits;
-  // |result| <= K 2^(2b) (|A'|, |B'| <= 2^b); the one-step reconstruction
-  // needs its ratio to M at most 1/2 - 1/32 (the quotient estimate errs by
-  // less than 0.01)
-  const double ratio = std::exp2(std::log2(static_cast<double>(k)) + 2.0 * T.bits - log_m);
-  T.crt.fast = ratio <= 0.5 - 1.0 / 32 - 1e-9 ? 1 : 0;
-  return T;
-}
-
-// The operand integer V = sign * X (X <= 2^62) as four balanced 16-bit limbs
-// held in floats: V = sum L_j 2^(16 j), |L_j| <= 2^15 (|L_3| <= 2^14 + 1).
-__device__ __forceinline__ void balanced_limbs(uint64_t X, bool neg, float (&L)[4]) {
-  uint64_t x = X;
-#pragma unroll
-  for (int j = 0; j < 3; ++j) {
-    const int d = static_cast<int>(x & 0xFFFFu);
-    const int c = d >= 0x8000;
-    const int l = d - (c << 16);
-    L[j] = float_of_small_int(neg ? -l : l);
-    x = (x >> 16) + static_cast<uint64_t>(c);
-  }
-  const int l3 = static_cast<int>(x);
-  L[3] = float_of_small_int(neg ? -l3 : l3);
-}
-
-// Residue of V modulo m_i with |r| <= 128, in single precision, exactly:
-// t = L_0 + sum_j L_j (2^(16 j) mod m) is an integer with |t| < 2^24 (exact in
-// float at every step); q = round(t * fl(1/m)) through the 1.5 * 2^23 rounding
-// constant is round(t / m) except within 0.004 of a tie, so r = t - q m (one
-// exact FMA) satisfies |r| <= 0.504 m, i.e. |r| <= 128 for m <= 255 (and r
-// is the symmetric residue exactly for m = 256, where 1/m is exact).
-__device__ __forceinline__ float residue_of(const float (&L)[4], const ModTable& T, int i) {
-  const float t = fmaf(L[3], T.cf[i][2], fmaf(L[2], T.cf[i][1], fmaf(L[1], T.cf[i][0], L[0])));
-  const float q = fmaf(t, T.invm[i], 12582912.0f) - 12582912.0f;
-  return fmaf(-q, T.mf[i], t);
-}
-
-// Two residues as a packed BF16 pair (lo in the low half): integer-valued
-// floats of magnitude <= 128 have zero low 16 bits.
-__device__ __forceinline__ uint32_t bf16x2_of_float_ints(float lo, float hi) {
-  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
-}
 
 // A residue planes [n][M][ldp]: blockIdx.x = row, each thread 8 consecutive k.
 __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K,
@@ -142,67 +41,19 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
   const int64_t row = blockIdx.x;
   const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
   if (row >= M || k0 >= ldp) return;
-  const int e = ea[row];
-  const double* a = A + row * lda;
-  float L[8][4];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    bool neg;
-    const uint64_t X = fixed_point(k0 + j < K ? a[k0 + j] : 0.0, e, T.bits, neg);
-    balanced_limbs(X, neg, L[j]);
-  }
-  uint16_t* out = planes + row * ldp + k0;
-  for (int i = 0; i < T.n; ++i) {
-    uint32_t w[4];
-#pragma unroll
-    for (int j = 0; j < 8; j += 2) w[j >> 1] = bf16x2_of_float_ints(residue_of(L[j], T, i), residue_of(L[j + 1], T, i));
-    *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-  }
+  residue_row_piece(A + row * lda, K, ea[row], T.bits, T, planes + row * ldp, plane_stride, k0);
 }
 
-// B residue planes, transposed ([n][N][ldp]): one 32 (k) x 64 (j) block per
-// CTA; the residues are staged through shared memory 8 planes at a time.
+// B residue planes, transposed ([n][N][ldp]): one 32 (k) x 64 (j) block per CTA.
 __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
                                                            const int* __restrict__ eb,
                                                            const __grid_constant__ ModTable T,
                                                            uint16_t* __restrict__ planes, int64_t ldp,
                                                            int64_t plane_stride) {
   __shared__ uint32_t st[8][64][17];
-  const int j = threadIdx.x & 63;
-  const int kp0 = threadIdx.x >> 6;  // 0..3
-  const int64_t k0 = (int64_t)blockIdx.y * 32;
-  const int64_t j0 = (int64_t)blockIdx.x * 64;
-  const int64_t col = j0 + j;
-  const int e = col < N ? eb[col] : kExpZero;
-  float L[8][4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {  // k pairs kp0, kp0 + 4, ...: elements 2u, 2u + 1
-    const int64_t k = k0 + 2 * (kp0 + 4 * u);
-    bool n0, n1;
-    const uint64_t X0 = fixed_point((col < N && k < K) ? B[k * ldb + col] : 0.0, e, T.bits, n0);
-    const uint64_t X1 = fixed_point((col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0, e, T.bits, n1);
-    balanced_limbs(X0, n0, L[2 * u]);
-    balanced_limbs(X1, n1, L[2 * u + 1]);
-  }
-  const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;
-  const int64_t gj = j0 + wj, gk = k0 + 8 * q;
-  for (int i0 = 0; i0 < T.n; i0 += 8) {
-    const int cnt = min(8, T.n - i0);
-    for (int p = 0; p < cnt; ++p) {
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        st[p][j][kp0 + 4 * u] = bf16x2_of_float_ints(residue_of(L[2 * u], T, i0 + p), residue_of(L[2 * u + 1], T, i0 + p));
-    }
-    __syncthreads();
-    if (gj < N && gk < ldp)
-      for (int p = 0; p < cnt; ++p)
-        *reinterpret_cast<uint4*>(planes + (int64_t)(i0 + p) * plane_stride + gj * ldp + gk) =
-            make_uint4(st[p][wj][4 * q], st[p][wj][4 * q + 1], st[p][wj][4 * q + 2], st[p][wj][4 * q + 3]);
-    __syncthreads();
-  }
+  residue_col_block(B, ldb, K, N, eb, T.bits, T, planes, ldp, plane_stride, (int64_t)blockIdx.y * 32,
+                    (int64_t)blockIdx.x * 64, st);
 }
-
-constexpr int kCrtCols = 4;  // consecutive columns per thread (one 32-bit load per plane)
 
 // C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
 __global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
@@ -212,20 +63,8 @@ __global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R,
   const int64_t row = blockIdx.x;
   const int64_t c0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * kCrtCols;
   if (row >= M || c0 >= N) return;
-  // c0 is a multiple of 4 below N <= ldr (a multiple of 16): the word is in the plane
-  uint32_t rw[kCrtMaxModuli];
-  const uint8_t* rp = R + row * ldr + c0;
-#pragma unroll
-  for (int i = 0; i < kCrtMaxModuli; ++i) rw[i] = i < T.n ? *reinterpret_cast<const uint32_t*>(rp + i * rplane) : 0u;
-  const int e_row = max(ea[row], -20000) - 2 * T.bits;
-  double* cp = C + row * ldc + c0;
-#pragma unroll
-  for (int c = 0; c < kCrtCols; ++c) {
-    if (c0 + c >= N) break;
-    int shift;
-    const double v = crt_value(rw, c, T.crt, shift);
-    crt_apply(cp + c, v, shift + e_row + max(eb[c0 + c], -20000));
-  }
+  crt_cols(R + row * ldr + c0, rplane, T.crt, T.crt.fast, static_cast<int>(min(static_cast<int64_t>(kCrtCols), N - c0)),
+           max(ea[row], -20000) - 2 * T.bits, eb + c0, C + row * ldc + c0);
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }

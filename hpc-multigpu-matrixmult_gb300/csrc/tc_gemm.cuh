@@ -103,6 +103,9 @@ struct TcGroupProblem {
   int64_t ldc;
   const int* ea;
   const int* eb;
+  uint8_t* R;                 // kResidue: this problem's residue planes, their row and plane strides
+  int64_t ldr;
+  int64_t rplane;
 };
 
 struct TcGroupTable {
@@ -122,6 +125,9 @@ struct TcJob {
   int64_t ldc;
   const int* ea;
   const int* eb;
+  uint8_t* R;
+  int64_t ldr;
+  int64_t rplane;
 };
 
 // Shared-memory plan: a 192 KB ring of K-stages (64 bf16 deep), the epilogue
@@ -176,6 +182,9 @@ __device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap
     j.ldc = a.ldc;
     j.ea = a.ea;
     j.eb = a.eb;
+    j.R = a.R;
+    j.ldr = a.ldr;
+    j.rplane = a.rplane;
   } else {
     int lo = 0, hi = g.count - 1;
     while (lo < hi) {  // last problem with tile_start <= t
@@ -193,6 +202,9 @@ __device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap
     j.ldc = p.ldc;
     j.ea = p.ea;
     j.eb = p.eb;
+    j.R = p.R;
+    j.ldr = p.ldr;
+    j.rplane = p.rplane;
   }
 }
 
@@ -480,7 +492,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             // contiguous in the residue plane, reduced and stored 16 columns
             // (one 16-byte vector) at a time.
             const int64_t grow = row0 + lane;
-            uint8_t* rp = args.R + static_cast<int64_t>(pairs.g[gstart]) * args.rplane + grow * args.ldr + col0;
+            uint8_t* rp = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane + grow * job.ldr + col0;
 #pragma unroll
             for (int u = 0; u < HALF; u += 16) {
               uint32_t w[4];

@@ -104,6 +104,11 @@ _lib.phpc_grouped_workspace_bytes.restype = ct.c_size_t
 _lib.phpc_grouped_plan_create.argtypes = [ct.POINTER(ct.c_void_p), ct.POINTER(GemmProblem), ct.c_int, ct.c_int,
                                           ct.c_void_p, ct.c_size_t, ct.c_void_p]
 _lib.phpc_grouped_plan_create.restype = ct.c_int
+_lib.phpc_grouped_modular_workspace_bytes.argtypes = [ct.POINTER(GemmProblem), ct.c_int, ct.c_int]
+_lib.phpc_grouped_modular_workspace_bytes.restype = ct.c_size_t
+_lib.phpc_grouped_modular_plan_create.argtypes = [ct.POINTER(ct.c_void_p), ct.POINTER(GemmProblem), ct.c_int,
+                                                  ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p]
+_lib.phpc_grouped_modular_plan_create.restype = ct.c_int
 _lib.phpc_grouped_run.argtypes = [ct.c_void_p, ct.c_void_p]
 _lib.phpc_grouped_run.restype = ct.c_int
 _lib.phpc_grouped_graph_launch.argtypes = [ct.c_void_p, ct.c_void_p]
@@ -275,22 +280,34 @@ class GroupedPlan:
     """A planned grouped FP64-accurate GEMM over device-resident problems.
 
     problems: list of (m, k, n, A, lda, B, ldb, C, ldc) with device pointers or
-    torch tensors. The caller keeps the matrices and the workspace alive."""
+    torch tensors. The caller keeps the matrices and the workspace alive.
+    moduli=q (8..16) plans the modular scheme; otherwise the digit scheme with
+    `slices` slices."""
 
-    def __init__(self, problems, slices, workspace, workspace_bytes, stream=None):
-        arr = (GemmProblem * len(problems))()
-        for i, (m, k, n, A, lda, B, ldb, C, ldc) in enumerate(problems):
-            arr[i] = GemmProblem(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc)
+    def __init__(self, problems, slices, workspace, workspace_bytes, stream=None, moduli=0):
+        arr = self._problems(problems)
         self._arr = arr
         self._plan = ct.c_void_p()
-        _check(_lib.phpc_grouped_plan_create(ct.byref(self._plan), arr, len(problems), slices, _dptr(workspace),
-                                             workspace_bytes, _stream(stream)), "phpc_grouped_plan_create")
+        if moduli:
+            _check(_lib.phpc_grouped_modular_plan_create(ct.byref(self._plan), arr, len(problems), moduli,
+                                                         _dptr(workspace), workspace_bytes, _stream(stream)),
+                   "phpc_grouped_modular_plan_create")
+        else:
+            _check(_lib.phpc_grouped_plan_create(ct.byref(self._plan), arr, len(problems), slices, _dptr(workspace),
+                                                 workspace_bytes, _stream(stream)), "phpc_grouped_plan_create")
 
     @staticmethod
-    def workspace_bytes(problems, slices) -> int:
+    def _problems(problems):
         arr = (GemmProblem * len(problems))()
         for i, (m, k, n, A, lda, B, ldb, C, ldc) in enumerate(problems):
             arr[i] = GemmProblem(m, k, n, _dptr(A), lda, _dptr(B), ldb, _dptr(C), ldc)
+        return arr
+
+    @staticmethod
+    def workspace_bytes(problems, slices, moduli=0) -> int:
+        arr = GroupedPlan._problems(problems)
+        if moduli:
+            return int(_lib.phpc_grouped_modular_workspace_bytes(arr, len(problems), moduli))
         return int(_lib.phpc_grouped_workspace_bytes(arr, len(problems), slices))
 
     def run(self, stream=None) -> None:

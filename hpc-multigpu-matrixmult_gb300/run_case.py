@@ -35,6 +35,8 @@ def main() -> int:
     p.add_argument("--k", type=int, default=0)
     p.add_argument("--slices", type=int, default=7)
     p.add_argument("--moduli", type=int, default=16, help="ozaki2: number of residue GEMMs")
+    p.add_argument("--grouped-moduli", type=int, default=15,
+                   help="grouped: modular scheme with this many moduli (0 = digit scheme with --slices)")
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--emin", type=int, default=-20)
     p.add_argument("--emax", type=int, default=20)
@@ -117,8 +119,10 @@ def main() -> int:
 def run_grouped(a, torch, phpc) -> int:
     """The batching workload: `count` problems with m, k, n log-uniform in
     [64, 2048] (multiples of 16, fixed shape seed), uniform [-1, 1) entries.
-    Times one grouped graph launch (FP64-accurate Ozaki, one plan), one
-    single-problem Ozaki call per problem and one plain DMMA launch per
+    Times one grouped graph launch (FP64-accurate Ozaki, one plan: modular
+    scheme with --grouped-moduli moduli, or the digit scheme with --slices
+    when it is 0), one single-problem Ozaki call per problem and one plain
+    FP64 launch per
     problem, in aggregate FP64-equivalent TFLOP/s, and states the errors of
     the grouped result on sampled rows of the first 8 problems."""
     import numpy as np
@@ -134,10 +138,11 @@ def run_grouped(a, torch, phpc) -> int:
         phpc.fill_uniform_dev(B, k * n, 1001 + 2 * i, 0, st)
         mats.append((A, B, torch.zeros((m, n), dtype=torch.float64, device="cuda")))
     s = a.slices
+    q = a.grouped_moduli
     probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B, C) in zip(shapes, mats)]
-    ws = phpc.GroupedPlan.workspace_bytes(probs, s)
+    ws = phpc.GroupedPlan.workspace_bytes(probs, s, moduli=q)
     W = torch.empty(ws, dtype=torch.uint8, device="cuda")
-    plan = phpc.GroupedPlan(probs, s, W, ws, st)
+    plan = phpc.GroupedPlan(probs, s, W, ws, st, moduli=q)
 
     def timed(fn, reps):
         fn()
@@ -180,7 +185,8 @@ def run_grouped(a, torch, phpc) -> int:
     t_dmma = timed(per_problem_dmma, 1)
     status = phpc.device_status()
     plan.close()
-    print(json.dumps({"method": "grouped", "count": a.count, "slices": s, "flops": flops,
+    print(json.dumps({"method": "grouped", "count": a.count, "scheme": f"modular {q}" if q else f"digits {s}",
+                      "flops": flops,
                       "grouped_graph_ms": round(t_graph, 3), "grouped_tflops": round(flops / t_graph / 1e9, 3),
                       "per_problem_ozaki_ms": round(t_single, 3),
                       "per_problem_ozaki_tflops": round(flops / t_single / 1e9, 3),

@@ -171,8 +171,14 @@ size_t phpc_grouped_workspace_bytes(const phpc_gemm_problem *problems, int count
  * counterpart: the reference runs one GEMM per call (src/phpc_gemm.cu:59). */
 int phpc_grouped_plan_create(phpc_grouped_plan **plan, const phpc_gemm_problem *problems, int count, int slices,
                              void *workspace, size_t workspace_bytes, void *stream);
-/* Enqueues the five launches of the grouped call on `stream` (exponent scans,
- * digit splits, one persistent slice GEMM over all problems' tiles). */
+/* The same on the modular (CRT) scheme with `moduli` (8..16) residue GEMMs per
+ * problem; each problem's grid width follows from its own K. */
+size_t phpc_grouped_modular_workspace_bytes(const phpc_gemm_problem *problems, int count, int moduli);
+int phpc_grouped_modular_plan_create(phpc_grouped_plan **plan, const phpc_gemm_problem *problems, int count,
+                                     int moduli, void *workspace, size_t workspace_bytes, void *stream);
+/* Enqueues the launches of a grouped call on `stream`: exponent scans, digit
+ * or residue splits, one persistent tensor-core GEMM over all problems' tiles
+ * and, for a modular plan, the CRT of all rows. */
 int phpc_grouped_run(const phpc_grouped_plan *plan, void *stream);
 /* Same work, captured once into a CUDA graph on first use, then replayed. */
 int phpc_grouped_graph_launch(phpc_grouped_plan *plan, void *stream);

@@ -91,3 +91,75 @@ def test_plan_validation(phpc, torch_cuda):
     with pytest.raises(phpc.PhpcError) as e:
         phpc.GroupedPlan([(0, 64, 64, A, 64, A, 64, A, 64)], 7, W, 64)
     assert e.value.code == 1
+
+
+def single_modular(phpc, torch, A, B, C, q):
+    m, k = A.shape
+    n = B.shape[1]
+    ws = phpc.ozaki2_workspace_bytes(m, k, n, q)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, q, W, ws)
+
+
+@pytest.mark.parametrize("bn", ["128", "256"])
+def test_grouped_modular_equals_single(phpc, oracle, torch_cuda, monkeypatch, bn):
+    """Modular plan: every problem bit-identical to the single-problem modular
+    call (each with the grid width of its own K), and to the exact-integer
+    model on the small ones."""
+    import ozaki2_model
+
+    torch = torch_cuda
+    monkeypatch.setenv("PHPC_GROUPED_BN", bn)
+    shapes = [(64, 64, 64), (16, 32, 48), (130, 70, 300), (7, 13, 5), (256, 1024, 128), (96, 2048, 80),
+              (300, 17, 1), (1, 500, 260), (40, 2048, 72)] + phpc.grouped_shapes(12, seed=9, lo=16, hi=512)
+    q = 15
+    batch = make_batch(torch, shapes, 5)
+    probs = [(A.shape[0], A.shape[1], B.shape[1], A, A.shape[1], B, B.shape[1], C, B.shape[1])
+             for (_, _, _, A, B, C) in batch]
+    ws = phpc.GroupedPlan.workspace_bytes(probs, 0, moduli=q)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    plan = phpc.GroupedPlan(probs, 0, W, ws, moduli=q)
+    plan.run()
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    for i, (a, b, c0, A, B, C) in enumerate(batch):
+        got = C.cpu().numpy()
+        C1 = torch.from_numpy(c0).cuda()
+        single_modular(phpc, torch, A, B, C1, q)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(got, C1.cpu().numpy(), err_msg=f"problem {i} {shapes[i]}")
+        if a.size * b.shape[1] <= 200000:
+            np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, q), err_msg=f"model, problem {i}")
+        if i < 6:
+            err = oracle.rel_errors(got, oracle.gemm_dd(a, b, c0))
+            assert err["frob"] <= 1e-14, (i, err)
+    plan.close()
+
+
+def test_grouped_modular_graph_replay_and_validation(phpc, torch_cuda):
+    torch = torch_cuda
+    shapes = phpc.grouped_shapes(24, seed=2, lo=32, hi=384)
+    q = 14
+    batch = make_batch(torch, shapes, 6)
+    probs = [(A.shape[0], A.shape[1], B.shape[1], A, A.shape[1], B, B.shape[1], C, B.shape[1])
+             for (_, _, _, A, B, C) in batch]
+    ws = phpc.GroupedPlan.workspace_bytes(probs, 0, moduli=q)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    plan = phpc.GroupedPlan(probs, 0, W, ws, moduli=q)
+    plan.graph_launch()
+    plan.graph_launch()  # C += A B twice
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    for i, (a, b, c0, A, B, C) in enumerate(batch):
+        C2 = torch.from_numpy(c0).cuda()
+        single_modular(phpc, torch, A, B, C2, q)
+        single_modular(phpc, torch, A, B, C2, q)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(C.cpu().numpy(), C2.cpu().numpy(), err_msg=f"problem {i}")
+    plan.close()
+    with pytest.raises(phpc.PhpcError) as e:
+        phpc.GroupedPlan(probs, 0, W, 64, moduli=q)
+    assert e.value.code == 6
+    with pytest.raises(phpc.PhpcError) as e:
+        phpc.GroupedPlan(probs, 0, W, ws, moduli=17)
+    assert e.value.code == 1
