@@ -9,13 +9,14 @@
 //    rows, columns, split blocks and output tiles, plus two TMA descriptors
 //    per problem (A digit planes, B digit planes), written into the head of
 //    the caller's workspace;
-//  - five launches cover the batch: exponent scans of all rows, of all
-//    columns, digit splits of all rows, of all column blocks, and the
+//  - five kernels cover the batch (six launches: the column scan's reset):
+//    exponent scans of all rows, of all columns, digit splits of all rows,
+//    of all column blocks, and the
 //    persistent tcgen05 slice GEMM over the union of all output tiles
 //    (tc_gemm.cuh, grouped mode: a tile finds its problem by binary search);
 //  - phpc_grouped_graph_launch captures those five launches once into a CUDA
 //    graph and replays it.
-// A modular-scheme plan (phpc_grouped_modular_plan_create) has six launches:
+// A modular-scheme plan (phpc_grouped_modular_plan_create) has six kernels:
 // the two scans, residue splits of all rows and of all column blocks, the
 // persistent residue GEMM over all tiles (each tile's residues go to its
 // problem's planes), and the CRT of all rows; every problem uses the plan's
@@ -39,6 +40,7 @@ namespace {
 struct GSplitProb {
   int m, k, n;
   int row_start, col_start, sblock_start;  // prefix sums over the problems
+  int cunit_start, crt_unit_start;         // prefix sums: column-scan units, CRT units
   int nblk_j;                              // 64-column blocks of B
   int64_t lda, ldb, ldp;
   const double* A;
@@ -74,16 +76,28 @@ __global__ void g_scan_rows_kernel(const GSplitProb* __restrict__ P, int count, 
   scan_row_warp(p.A + row * p.lda, p.k, p.ea + row, status);
 }
 
-// One thread per column over the whole K of its problem (no atomics).
-__global__ void g_scan_cols_kernel(const GSplitProb* __restrict__ P, int count, int total_cols, int* status) {
+constexpr int kScanKChunk = 256;  // rows of B one column-scan unit covers
+
+__global__ void g_reset_cols_kernel(const GSplitProb* __restrict__ P, int count, int total_cols) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= total_cols) return;
   const GSplitProb& p = P[locate(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
-  const int64_t col = c - p.col_start;
+  p.eb[c - p.col_start] = kExpZero;
+}
+
+// One thread per (column, 256-row chunk of K) unit, consecutive threads on
+// consecutive columns; chunk maxima meet in eb by atomicMax (eb reset first).
+__global__ void g_scan_cols_kernel(const GSplitProb* __restrict__ P, int count, int total_units, int* status) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= total_units) return;
+  const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.cunit_start; })];
+  const int w = u - p.cunit_start;
+  const int64_t col = w % p.n;
+  const int k0 = (w / p.n) * kScanKChunk, k1 = min(p.k, k0 + kScanKChunk);
   int e = kExpZero;
   bool nf = false;
-  for (int k = 0; k < p.k; ++k) e = max(e, exponent_of(p.B[(int64_t)k * p.ldb + col], nf));
-  p.eb[col] = e;
+  for (int k = k0; k < k1; ++k) e = max(e, exponent_of(p.B[(int64_t)k * p.ldb + col], nf));
+  if (e > kExpZero) atomicMax(&p.eb[col], e);
   if (nf) record_error(status, PHPC_ERR_NONFINITE);
 }
 
@@ -131,15 +145,21 @@ __global__ void __launch_bounds__(256) g_residue_cols_kernel(const GSplitProb* _
   residue_col_block(p.B, p.ldb, p.k, p.n, p.eb, p.bits, T, p.pb, p.ldp, (int64_t)p.n * p.ldp, k0, j0, st);
 }
 
-// Modular scheme: C += the CRT of the residues, four columns per thread.
-__global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict__ P, int count, int total_rows,
+constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one warp)
+
+// Modular scheme: C += the CRT of the residues. One warp per unit of one row
+// and 128 columns, units numbered across the problems (no idle blocks for
+// narrow problems), four columns per thread.
+__global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict__ P, int count, int total_units,
                                                     const __grid_constant__ ModTable T) {
-  const int r = blockIdx.x;
-  if (r >= total_rows) return;
-  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
-  const int64_t c0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * kCrtCols;
+  const int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (u >= total_units) return;
+  const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.crt_unit_start; })];
+  const int w = u - p.crt_unit_start;
+  const int chunks = (p.n + kCrtUnitCols - 1) / kCrtUnitCols;
+  const int64_t row = w / chunks;
+  const int64_t c0 = (int64_t)(w % chunks) * kCrtUnitCols + (threadIdx.x & 31) * kCrtCols;
   if (c0 >= p.n) return;
-  const int64_t row = r - p.row_start;
   crt_cols(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
            static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - 2 * p.bits,
            p.eb + c0, p.C + row * p.ldc + c0);
@@ -216,7 +236,7 @@ PairList residue_pairs(const ModTable& T) {
 struct phpc_grouped_plan {
   int device;
   int count, s, moduli, bn;  // moduli > 0: modular scheme (s unused)
-  int total_rows, total_cols, total_sblocks, total_tiles, max_kgroups, max_cgroups;
+  int total_rows, total_cols, total_sblocks, total_tiles, max_kgroups, total_cunits, total_crt_units;
   phpc::GSplitProb* d_split;
   phpc::TcGroupTable table;
   phpc::PairList pairs;
@@ -258,8 +278,10 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   if (pl->total_rows > 0) {
     g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
                                                                         status);
-    g_scan_cols_kernel<<<ceil_div(pl->total_cols, 128), 128, 0, stream>>>(pl->d_split, pl->count, pl->total_cols,
-                                                                          status);
+    g_reset_cols_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                            pl->total_cols);
+    g_scan_cols_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                            pl->total_cunits, status);
     if (modular) {
       g_residue_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
                                                                                        pl->total_rows, pl->mods);
@@ -279,8 +301,8 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   else
     rc = pl->bn == 128 ? launch_grouped_gemm<128, kOzaki>(pl, stream) : launch_grouped_gemm<256, kOzaki>(pl, stream);
   if (rc == PHPC_OK && modular) {
-    g_crt_kernel<<<dim3(pl->total_rows, pl->max_cgroups), 128, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
-                                                                            pl->mods);
+    g_crt_kernel<<<ceil_div(pl->total_crt_units, 4), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                       pl->total_crt_units, pl->mods);
     if (cudaGetLastError() != cudaSuccess) rc = PHPC_ERR_CUDA;
   }
   return rc;
@@ -332,7 +354,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   std::vector<TcGroupProblem> ht(count);
   std::vector<CUtensorMap> hm(2 * (size_t)count);
   size_t off = T.end;
-  int rows = 0, cols = 0, sblocks = 0, tiles = 0, maxkg = 1, maxcg = 1;
+  int rows = 0, cols = 0, sblocks = 0, tiles = 0, maxkg = 1;
+  int64_t cunits = 0, crt_units = 0;
   for (int i = 0; i < count && rc == PHPC_OK; ++i) {
     const phpc_gemm_problem& q = problems[i];
     const ProbLayout L = prob_layout(q, planes, modular);
@@ -345,6 +368,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     g.row_start = rows;
     g.col_start = cols;
     g.sblock_start = sblocks;
+    g.cunit_start = static_cast<int>(cunits);
+    g.crt_unit_start = static_cast<int>(crt_units);
     g.nblk_j = ceil_div(q.n, 64);
     g.lda = q.lda;
     g.ldb = q.ldb;
@@ -367,7 +392,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     cols += q.n;
     sblocks += g.nblk_j * ceil_div(q.k, 32);
     maxkg = std::max(maxkg, ceil_div(L.ldp / 8, 128));
-    maxcg = std::max(maxcg, ceil_div(q.n, 128 * kCrtCols));
+    cunits += (int64_t)q.n * ceil_div(q.k, kScanKChunk);
+    if (modular) crt_units += (int64_t)q.m * ceil_div(q.n, kCrtUnitCols);
 
     TcGroupProblem& t = ht[i];
     t = TcGroupProblem{};
@@ -400,12 +426,14 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
       rc = PHPC_ERR_CUDA;
     off += L.end;
   }
+  if (cunits > INT32_MAX / 2 || crt_units > INT32_MAX / 2) rc = PHPC_ERR_ARG;
   pl->total_rows = rows;
   pl->total_cols = cols;
   pl->total_sblocks = sblocks;
   pl->total_tiles = tiles;
   pl->max_kgroups = maxkg;
-  pl->max_cgroups = maxcg;
+  pl->total_cunits = static_cast<int>(cunits);
+  pl->total_crt_units = static_cast<int>(crt_units);
   pl->d_split = reinterpret_cast<GSplitProb*>(base + T.split);
   pl->table.count = count;
   pl->table.ntiles = tiles;
