@@ -11,7 +11,8 @@ the result against the double-double reference (phpc_dgemm_dd_rows_dev) on
 sampled rows, for two input classes: uniform [-1, 1) and wide exponents
 (u * 2^e, e uniform in [-20, 20]). A configuration qualifies when both errors
 are below target / margin; the fastest qualifying configuration wins. For the
-grouped call it picks BN on the batching workload (512 problems).
+grouped call it picks BN on the batching workload (512 problems, modular
+plan with --grouped-moduli moduli).
 
 Writes tune_table.txt next to this file (copied into lib/ by the build, where
 the library reads it):
@@ -44,6 +45,7 @@ def main() -> int:
     p.add_argument("--margin", type=float, default=4.0)
     p.add_argument("--rows", type=int, default=32)
     p.add_argument("--grouped-count", type=int, default=512)
+    p.add_argument("--grouped-moduli", type=int, default=15)
     p.add_argument("--clusters", default="1,2")
     p.add_argument("--out", default=str(HERE / "tune_table.txt"))
     a = p.parse_args()
@@ -147,14 +149,14 @@ def main() -> int:
             phpc.fill_uniform_dev(A, m * k, 1000 + 2 * i, 0, st)
             phpc.fill_uniform_dev(B, k * n, 1001 + 2 * i, 0, st)
             mats.append((A, B, torch.zeros((m, n), dtype=torch.float64, device="cuda")))
-        s = 7  # the grouped call uses the digit scheme
+        s, q = 7, a.grouped_moduli  # tuned for the modular grouped plan (q moduli)
         probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B, C) in zip(shapes, mats)]
         best_ms = None
         for bn in (128, 256):
             os.environ["PHPC_GROUPED_BN"] = str(bn)
-            ws = phpc.GroupedPlan.workspace_bytes(probs, s)
+            ws = phpc.GroupedPlan.workspace_bytes(probs, s, moduli=q)
             W = torch.empty(ws, dtype=torch.uint8, device="cuda")
-            plan = phpc.GroupedPlan(probs, s, W, ws, st)
+            plan = phpc.GroupedPlan(probs, s, W, ws, st, moduli=q)
             plan.graph_launch(st)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -166,7 +168,7 @@ def main() -> int:
             ms = e0.elapsed_time(e1) / a.reps
             plan.close()
             del W
-            rec = {"grouped_count": a.grouped_count, "slices": s, "bn": bn, "ms": round(ms, 3)}
+            rec = {"grouped_count": a.grouped_count, "moduli": q, "bn": bn, "ms": round(ms, 3)}
             grouped_rep.append(rec)
             print(json.dumps(rec), flush=True)
             if best_ms is None or ms < best_ms:
