@@ -5,7 +5,9 @@ Outputs (all git-ignored, rebuilt on the GPU host by ``__graft_entry__.build()``
 * ``lib/libphpc_gemm.so``   CUDA kernels + C ABI (include/phpc_gemm.h), sm_103a only.
 * ``lib/libphpc_summa.so``  the SUMMA layer + utils compiled against the single-rank
                              MPI shim (include/phpc_summa.h, include/phpc_utils.h).
-* ``bin/main.out``          the reference-compatible command line driver.
+* ``bin/main.out``          the reference-compatible command line driver;
+* ``bin/iterative.out``     the reference's sequential timing program;
+* ``bin/family.out``        a test family (tests/*.csv format) as one grouped call.
 * ``../oracle/liboracle.so`` the CPU oracle (see oracle/).
 
 Every translation unit is compiled by its own nvcc/gcc process, in parallel.
@@ -79,11 +81,12 @@ def build_host() -> None:
     if not _newer(so, summa_srcs + [LIB / "libphpc_gemm.so"] + list(INC.rglob("*.h"))):
         _run(["gcc", *cflags, "-shared", "-o", str(so), *map(str, summa_srcs), f"-L{LIB}", "-lphpc_gemm",
               "-Wl,-rpath,$ORIGIN"])
-    main = BIN / "main.out"
-    if not _newer(main, [HOST / "main.c", so]):
-        _run(["gcc", *cflags, "-o", str(main), str(HOST / "main.c"), f"-L{LIB}", "-lphpc_summa", "-lphpc_gemm",
-              f"-L{CUDA_HOME / 'lib64'}", "-lcudart", "-lm", "-Wl,-rpath,$ORIGIN/../lib",
-              f"-Wl,-rpath,{CUDA_HOME / 'lib64'}"])
+    for prog in ("main", "iterative", "family"):
+        exe = BIN / f"{prog}.out"
+        if not _newer(exe, [HOST / f"{prog}.c", so]):
+            _run(["gcc", *cflags, "-o", str(exe), str(HOST / f"{prog}.c"), f"-L{LIB}", "-lphpc_summa",
+                  "-lphpc_gemm", f"-L{CUDA_HOME / 'lib64'}", "-lcudart", "-lm", "-Wl,-rpath,$ORIGIN/../lib",
+                  f"-Wl,-rpath,{CUDA_HOME / 'lib64'}"])
 
 
 def build_oracle() -> None:

@@ -64,3 +64,15 @@ double phpc_kat_index_entry(int n, int i, int j) {
   const i128 v = I * N * N * s1 + I * J * N * N + N * s2 + J * s1;
   return (double)v; /* one rounding to nearest */
 }
+
+/* Reference src/iterative.c:8-13, the same loop order (i, then j, then k
+ * innermost, which keeps the inner loop on contiguous rows of B and C). */
+void phpc_gemm_iterative(const double *A, const double *B, double *C, int n) {
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double a = A[(size_t)i * n + j];
+      const double *b = B + (size_t)j * n;
+      double *c = C + (size_t)i * n;
+      for (int k = 0; k < n; ++k) c[k] += a * b[k];
+    }
+}

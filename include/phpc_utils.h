@@ -33,6 +33,11 @@ void phpc_fill_wide(double *x, size_t n, uint64_t seed, uint64_t offset, int emi
 /* x[i] = i (the reference's inputs, src/main.c:85-86). */
 void phpc_fill_index(double *x, size_t n);
 
+/* Reference src/iterative.c:8-13: C += A * B for n x n row-major matrices on
+ * the host, one thread, in the reference's loop order (the CPU timing of
+ * bin/iterative.out). */
+void phpc_gemm_iterative(const double *A, const double *B, double *C, int n);
+
 /* Exact (A * B)[i][j] for A = B = index matrix of order n, rounded once to double:
  * i*n^2*S1 + i*j*n^2 + n*S2 + j*S1, S1 = n(n-1)/2, S2 = (n-1)n(2n-1)/6. */
 double phpc_kat_index_entry(int n, int i, int j);

@@ -71,3 +71,25 @@ def test_main_out_csv(tmp_path, built, dist):
     if dist == "index":
         for r_ in recs:  # exact integer products: both methods reproduce the closed form
             assert float(r_[5]) == 0.0 and float(r_[6]) == 0.0
+
+
+@pytest.mark.parametrize("moduli", ["15", "0"])
+def test_family_out_batched(tmp_path, built, moduli):
+    """A test family (the reference's tests/*.csv layout) as one grouped call:
+    every configuration exact on the index inputs, fields carried through."""
+    fam = tmp_path / "famX.csv"
+    fam.write_text("matrix_size,n_proc,n_gpu,tile_width,grid_width,grid_height\n"
+                   "32,1,1,32,1,1\n64,4,1,32,1,1\n96,1,1,16,2,2\n\n128,16,1,32,1,1\n200,4,1,8,4,4\n")
+    exe = PKG / "bin" / "family.out"
+    r = subprocess.run([str(exe), str(fam), moduli], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "csv" / "famX_batched.csv").read_text().strip().splitlines()
+    assert lines[0].split(",")[-3:] == ["single_gpu_seconds", "batch_gpu_seconds", "max_rel_err"]
+    rows = [line.split(",") for line in lines[1:]]
+    assert [r_[:6] for r_ in rows] == [["32", "1", "1", "32", "1", "1"], ["64", "4", "1", "32", "1", "1"],
+                                       ["96", "1", "1", "16", "2", "2"], ["128", "16", "1", "32", "1", "1"],
+                                       ["200", "4", "1", "8", "4", "4"]]
+    for r_ in rows:
+        assert float(r_[6]) > 0 and float(r_[7]) > 0
+        assert float(r_[8]) == 0.0  # integer products below 2^53: exact
+    assert len({r_[7] for r_ in rows}) == 1  # one batch time for the family

@@ -89,6 +89,37 @@ def test_index_known_answer(summa_lib):
             assert summa_lib.phpc_kat_index_entry(n, i, j) == float(exact)
 
 
+def test_gemm_iterative_loop(summa_lib, oracle):
+    """The host loop of bin/iterative.out (src/iterative.c:8-13): exact on the
+    index inputs, within rounding of the oracle's port of the same loop on
+    uniform inputs, and accumulating into C."""
+    f = summa_lib.phpc_gemm_iterative
+    f.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int]
+    f.restype = None
+    n = 48
+    a = np.arange(n * n, dtype=np.float64).reshape(n, n)
+    c = np.zeros((n, n))
+    f(a.ctypes.data, a.ctypes.data, c.ctypes.data, n)
+    np.testing.assert_array_equal(c, (a.astype(object) @ a.astype(object)).astype(np.float64))
+    rng = np.random.default_rng(3)
+    a, b = rng.uniform(-1, 1, (n, n)), rng.uniform(-1, 1, (n, n))
+    c0 = rng.uniform(-1, 1, (n, n))
+    c, ref = c0.copy(), c0.copy()
+    f(a.ctypes.data, b.ctypes.data, c.ctypes.data, n)
+    oracle.gemm_iterative(a, b, ref)
+    np.testing.assert_allclose(c, ref, rtol=0, atol=1e-13)
+
+
+def test_iterative_out_prints_size_and_seconds(built):
+    exe = ROOT / "hpc-multigpu-matrixmult_gb300" / "bin" / "iterative.out"
+    r = subprocess.run([str(exe), "128"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    size, seconds = r.stdout.strip().split(",")
+    assert size == "128" and float(seconds) >= 0.0
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Usage" in r.stderr
+
+
 def test_main_out_usage_and_divisibility(built):
     exe = str(PKG / "bin" / "main.out")
     r = subprocess.run([exe, "64", "32"], capture_output=True, text=True)
@@ -171,3 +202,31 @@ def test_crt_model_error_vs_dd_oracle(oracle, dist, nmod, bound):
         b *= np.exp2(rng.integers(-20, 21, (n, n)))
     err = oracle.rel_errors(ozaki2_model.gemm(a, b, None, nmod), oracle.gemm_dd(a, b))
     assert err["frob"] <= bound, err
+
+
+def test_report_pipeline(tmp_path):
+    """report.py reads main.out's CSV files and iterative.csv and writes the
+    summary table and SVG charts."""
+    import report  # hpc-multigpu-matrixmult_gb300/report.py
+
+    d = tmp_path / "csv"
+    d.mkdir()
+    (d / "iterative.csv").write_text("512,2.0\n1024,16.0\n")
+    for n, t in ((512, 0.002), (1024, 0.01)):
+        stem = f"fam_N{n}_T1_G1_TW32_GW2_GH2"
+        (d / f"{stem}.csv").write_text(f"{n},1,1,4,1024,4096,0.5,{t},{t / 10}\n")
+        (d / f"{stem}_ext.csv").write_text(
+            "method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err\n"
+            f"dmma,{n},0.5,{t},{2 * n ** 3 / t / 1e12},0.000e+00,0.000e+00\n"
+            f"ozaki_split,{n},0.4,{t / 10},{2 * n ** 3 / t * 10 / 1e12},1.0e-16,2.0e-16\n")
+    recs = report.collect(d, 1.25)
+    assert len(recs) == 4
+    r = next(x for x in recs if x["method"] == "ozaki_split" and x["matrix_size"] == 1024)
+    assert r["speedup_vs_sequential"] == pytest.approx(16.0 / 0.4)
+    assert r["x_fp64_peak"] == pytest.approx(r["tflops"] / 1.25)
+    out = tmp_path / "plots"
+    out.mkdir()
+    report.write_summary(recs, out / "summary.csv")
+    charts = report.write_charts(recs, out)
+    assert (out / "summary.csv").read_text().startswith("test,matrix_size")
+    assert len(charts) == 3 and all(p.read_text().startswith("<svg") for p in charts)
