@@ -316,6 +316,9 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       cudaStreamWaitEvent(sC, ev_bcopy, 0);
       for (int p = 0; p < np && rc == PHPC_OK; ++p) {
         const int r0 = p * pr, rows = std::min(pr, m - r0);
+        // B's copy gates the first GEMM: only A's first panel shares the
+        // host link with it, the later panels follow it
+        if (p == 1) cudaStreamWaitEvent(sA, ev_bcopy, 0);
         if (cudaMemcpy2DAsync(r.dA + (int64_t)r0 * dlda, dlda * 8, a + (int64_t)r0 * lda, (size_t)lda * 8,
                               (size_t)k * 8, rows, cudaMemcpyHostToDevice, sA) != cudaSuccess ||
             cudaMemcpy2DAsync(r.dC + (int64_t)r0 * dldc, dldc * 8, c + (int64_t)r0 * ldc, (size_t)ldc * 8,

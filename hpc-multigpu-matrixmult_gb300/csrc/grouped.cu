@@ -134,7 +134,7 @@ __global__ void g_residue_rows_kernel(const GSplitProb* __restrict__ P, int coun
   residue_row_piece(p.A + row * p.lda, p.k, p.ea[row], p.bits, T, p.pa + row * p.ldp, (int64_t)p.m * p.ldp, k0);
 }
 
-__global__ void __launch_bounds__(256) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
+__global__ void __launch_bounds__(256, 5) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
                                                              int total_blocks, const __grid_constant__ ModTable T) {
   __shared__ uint32_t st[8][64][17];
   const int b = blockIdx.x;

@@ -45,7 +45,7 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
 }
 
 // B residue planes, transposed ([n][N][ldp]): one 32 (k) x 64 (j) block per CTA.
-__global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
+__global__ void __launch_bounds__(256, 5) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
                                                            const int* __restrict__ eb,
                                                            const __grid_constant__ ModTable T,
                                                            uint16_t* __restrict__ planes, int64_t ldp,
