@@ -363,14 +363,30 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
         }
       }
     }
+    cudaEvent_t ev_out{};
+    new_event(ev_out);
+    if (rc == PHPC_OK) cudaEventRecord(ev_out, sO);
     for (cudaStream_t st : {sB, sA, sC, sG, sO})
       if (cudaStreamSynchronize(st) != cudaSuccess && rc == PHPC_OK) rc = PHPC_ERR_CUDA;
+    if (rc == PHPC_OK && getenv("PHPC_VERBOSE")) {
+      // timeline of the call (ms after the allocations): B copied / split,
+      // per panel A split, C copied, GEMM + CRT done, and the last copy-out
+      fprintf(stderr, "phpc: modular pipeline %d panels of %d rows: B copied %.2f split %.2f |", np, pr,
+              elapsed_ms(ev_alloc, ev_bcopy), elapsed_ms(ev_alloc, ev_b1));
+      for (int p = 0; p < np; ++p)
+        fprintf(stderr, " p%d A %.2f C %.2f G %.2f", p, elapsed_ms(ev_alloc, ev_a1[p]), elapsed_ms(ev_alloc, ev_c[p]),
+                elapsed_ms(ev_alloc, ev_g[p]));
+      fprintf(stderr, " | out %.2f\n", elapsed_ms(ev_alloc, ev_out));
+    }
     if (rc == PHPC_OK && cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       rc = PHPC_ERR_CUDA;
     float kernel_ms = 0.f;
     if (rc == PHPC_OK) {
-      kernel_ms = elapsed_ms(ev_b0, ev_b1) + elapsed_ms(ev_g0, ev_g1);
-      for (int p = 0; p < np; ++p) kernel_ms += elapsed_ms(ev_a0[p], ev_a1[p]);
+      // device compute time: A's first panel split (it runs during B's copy),
+      // then B's split through the last panel's CRT, a span in which the
+      // kernels follow one another without gaps (later A splits run between
+      // the panel GEMMs); spans that only wait for the SMs are not added
+      kernel_ms = elapsed_ms(ev_a0[0], ev_a1[0]) + elapsed_ms(ev_b0, ev_g1);
     }
     if (rc == PHPC_OK && nonfinite) {
       // inf/NaN cannot be carried by integers: redo the call in IEEE FP64
