@@ -7,7 +7,7 @@
 
 namespace phpc {
 
-constexpr int kCrtMaxModuli = 16;  // M < 2^126: weights in four 32-bit limbs, sums in five
+constexpr int kCrtMaxModuli = 15;  // M < 2^127: weights in four 32-bit limbs, sums in five
 
 struct CrtTable {
   int n;                          // number of moduli
@@ -31,12 +31,13 @@ __device__ __forceinline__ double crt_add_scaled(double c, double v, int x) {
   return c + ldexp(v, x);
 }
 
-// The symmetric representative of acc mod M (acc = sum r_i W_i < 2^12 M, as
+// The symmetric representative of acc mod M (acc = sum r_i W_i < 2^13 M, as
 // five 32-bit limbs) rounded once to double: returns v and sets shift so that
 // the result is v * 2^shift (v an integer-valued double, 0 for a zero result).
 __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T, int fast, int& shift) {
   // acc / M estimated in single precision from the 64 bits at limb qlimb
-  // (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20): absolute error < 0.01.
+  // (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20): absolute error below
+  // 2^13 (2^-20 + 3 2^-24) < 0.01.
   // (Limbs chosen with constant indices: an array indexed by a runtime value
   // would live in local memory.)
   uint32_t tlo = l[0], thi = l[1];
@@ -163,17 +164,17 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T,
   return neg ? -v : v;
 }
 
-// The CRT of byte c (0..3) of each word rw[i] (the residue mod m_i of one
-// element): acc = sum r_i W_i, rounded as crt_round (fast: the one-step path,
-// allowed when the product's grid leaves the margin CrtTable::fast states).
-__device__ __forceinline__ double crt_value(const uint32_t (&rw)[kCrtMaxModuli], int c, const CrtTable& T,
-                                            int fast, int& shift) {
-  // 32-bit limbs accumulated in 64 bits (no overflow: 16 x 2^8 x 2^32 < 2^45)
+// The CRT of one element from its residues r[i] mod m_i: acc = sum r_i W_i,
+// rounded as crt_round (fast: the one-step path, allowed when the product's
+// grid leaves the margin CrtTable::fast states).
+__device__ __forceinline__ double crt_value(const uint32_t (&rr)[kCrtMaxModuli], const CrtTable& T, int fast,
+                                            int& shift) {
+  // 32-bit limbs accumulated in 64 bits (no overflow: 15 x 2^9 x 2^32 < 2^45)
   uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i) {
     if (i < T.n) {
-      const uint32_t r = (rw[i] >> (8 * c)) & 0xFFu;
+      const uint32_t r = rr[i];
       a0 += static_cast<uint64_t>(r) * T.W[i][0];
       a1 += static_cast<uint64_t>(r) * T.W[i][1];
       a2 += static_cast<uint64_t>(r) * T.W[i][2];

@@ -50,7 +50,7 @@ struct GSplitProb {
   uint16_t* pa;
   uint16_t* pb;
   // modular scheme only
-  uint8_t* R;       // residue planes [moduli][m][ldr]
+  uint16_t* R;      // residue planes [moduli][m][ldr], 16 bits per residue
   int64_t ldr;
   int bits, fast;   // the grid width for this K and the CRT path it allows
   double* C;
@@ -134,7 +134,7 @@ __global__ void g_residue_rows_kernel(const GSplitProb* __restrict__ P, int coun
   residue_row_piece(p.A + row * p.lda, p.k, p.ea[row], p.bits, T, p.pa + row * p.ldp, (int64_t)p.m * p.ldp, k0);
 }
 
-__global__ void __launch_bounds__(256, 5) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
+__global__ void __launch_bounds__(256) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
                                                              int total_blocks, const __grid_constant__ ModTable T) {
   __shared__ uint32_t st[8][64][17];
   const int b = blockIdx.x;
@@ -183,7 +183,7 @@ ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
   L.pa = align_up(L.eb + sizeof(int) * (size_t)q.n, 256);
   L.pb = align_up(L.pa + (size_t)planes * q.m * L.ldp * 2, 256);
   L.r = align_up(L.pb + (size_t)planes * q.n * L.ldp * 2, 256);
-  L.end = modular ? align_up(L.r + (size_t)planes * q.m * L.ldr, 256) : L.r;
+  L.end = modular ? align_up(L.r + (size_t)planes * q.m * L.ldr * 2, 256) : L.r;
   return L;
 }
 
@@ -381,7 +381,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     g.pa = reinterpret_cast<uint16_t*>(pb + L.pa);
     g.pb = reinterpret_cast<uint16_t*>(pb + L.pb);
     if (modular) {
-      g.R = pb + L.r;
+      g.R = reinterpret_cast<uint16_t*>(pb + L.r);
       g.ldr = L.ldr;
       g.bits = mod_grid_bits(planes, q.k);
       g.fast = mod_crt_fast(planes, q.k, g.bits);

@@ -97,7 +97,7 @@ PairList ozaki_pairs(int s) {
 template <int BN, int MODE>
 int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
                          int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane, const TcGemmOpts& opt) {
+                         cudaStream_t stream, uint16_t* R, int64_t ldr, int64_t rplane, const TcGemmOpts& opt) {
   using Cfg = TcCfg<BN>;
   const DeviceInfo* dev = current_device();
   if (!dev) return PHPC_ERR_CUDA;
@@ -169,7 +169,7 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
 #define PHPC_INSTANTIATE_TC(BN, MODE)                                                                         \
   template int launch_tc_slice_gemm<BN, MODE>(const void*, const void*, int, int, int64_t, int, int, int,         \
                                               const PairList&, void*, int64_t, const int*, const int*, cudaStream_t, \
-                                              uint8_t*, int64_t, int64_t, const TcGemmOpts&);
+                                              uint16_t*, int64_t, int64_t, const TcGemmOpts&);
 PHPC_INSTANTIATE_TC(256, kF32)
 PHPC_INSTANTIATE_TC(128, kF32)
 PHPC_INSTANTIATE_TC(256, kResidue)

@@ -4,14 +4,15 @@
 // C += A * B (the reference's semantics, src/phpc_gemm.cu:55) computed as:
 //  1. Exponent scans, as in ozaki.cu: ea[i] = max_k e(A[i][k]),
 //     eb[j] = max_k e(B[k][j]).
-//  2. Residue split (integer only): each element becomes the integer
+//  2. Residue split: each element becomes the integer
 //     A'[i][k] = sign * round(|A[i][k]| * 2^(b - ea[i])), |A'| <= 2^b (B'
 //     likewise with eb[j]), and then its symmetric residues modulo n pairwise
-//     coprime moduli m_1..m_n <= 256: integers in [-128, 127], exact in BF16.
-//     Planes A_i = [n][M][ldp], B_i = [n][N][ldp] (transposed, K-major).
+//     coprime moduli m_1..m_n <= 363: integers with |r| <= 181, exact in BF16
+//     (residue.cuh). Planes A_i = [n][M][ldp], B_i = [n][N][ldp] (transposed,
+//     K-major).
 //  3. n residue GEMMs on the tcgen05 engine (tc_gemm.cuh, kResidue): the exact
-//     int32 sum of A_i * B_i^T (f32 chunks of 1024 products, as in the digit
-//     scheme) reduced mod m_i, one byte per element, into plane i of R.
+//     int32 sum of A_i * B_i^T (exact f32 chunks of 512 products) reduced
+//     mod m_i, one 16-bit residue per element, into plane i of R.
 //  4. CRT (this file): C_int = sum_i r_i * W_i mod M, W_i = (M/m_i) *
 //     ((M/m_i)^-1 mod m_i), M = prod m_i, in 160-bit integer arithmetic;
 //     b is the largest width with 2 * K * 2^(2b) < M, so the symmetric
@@ -19,8 +20,9 @@
 //     C += round_to_double(C_int) * 2^(ea[i] + eb[j] - 2b).
 //
 // Compared with the digit scheme (s slices, s(s+1)/2 slice products) the
-// tensor-core work is n GEMMs with no triangular truncation: n = 16 gives
-// b = 55 at K = 16384, the grid of 7 digits, for 16 GEMMs instead of 28.
+// tensor-core work is n GEMMs with no triangular truncation: n = 15 gives
+// b = 55 at K = 16384, the grid of 7 digits, for 15 GEMMs instead of 28;
+// n = 14 gives b = 51.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -45,7 +47,7 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
 }
 
 // B residue planes, transposed ([n][N][ldp]): one 32 (k) x 64 (j) block per CTA.
-__global__ void __launch_bounds__(256, 5) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
+__global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
                                                            const int* __restrict__ eb,
                                                            const __grid_constant__ ModTable T,
                                                            uint16_t* __restrict__ planes, int64_t ldp,
@@ -56,7 +58,7 @@ __global__ void __launch_bounds__(256, 5) residue_cols_kernel(const double* __re
 }
 
 // C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
-__global__ void __launch_bounds__(128) crt_kernel(const uint8_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
+__global__ void __launch_bounds__(128) crt_kernel(const uint16_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
                                                   int N, const int* __restrict__ ea, const int* __restrict__ eb,
                                                   const __grid_constant__ ModTable T, double* __restrict__ C,
                                                   int64_t ldc) {
@@ -83,7 +85,7 @@ Ozaki2Layout ozaki2_layout(int m, int k, int n, int nmod) {
   L.off_pa = align256(L.off_eb + sizeof(int) * (size_t)n);
   L.off_pb = align256(L.off_pa + (size_t)nmod * m * L.ldp * 2);
   L.off_r = align256(L.off_pb + (size_t)nmod * n * L.ldp * 2);
-  L.total = align256(L.off_r + (size_t)nmod * m * L.ldr);
+  L.total = align256(L.off_r + (size_t)nmod * m * L.ldr * 2);
   return L;
 }
 
@@ -92,7 +94,7 @@ struct Ozaki2Views {
   int* eb;
   uint16_t* pa;
   uint16_t* pb;
-  uint8_t* R;
+  uint16_t* R;
 };
 
 int ozaki2_views(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, Ozaki2Layout& L, Ozaki2Views& V) {
@@ -106,7 +108,7 @@ int ozaki2_views(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes,
   V.eb = reinterpret_cast<int*>(base + L.off_eb);
   V.pa = reinterpret_cast<uint16_t*>(base + L.off_pa);
   V.pb = reinterpret_cast<uint16_t*>(base + L.off_pb);
-  V.R = base + L.off_r;
+  V.R = reinterpret_cast<uint16_t*>(base + L.off_r);
   return PHPC_OK;
 }
 
@@ -181,7 +183,7 @@ int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const 
   }
   const int64_t rplane = (int64_t)m * L.ldr;
   const uint16_t* pa = V.pa + (int64_t)r0 * L.ldp;
-  uint8_t* R = V.R + (int64_t)r0 * L.ldr;
+  uint16_t* R = V.R + (int64_t)r0 * L.ldr;
   TcGemmOpts opt;
   opt.a_plane_rows = m;
   opt.cfg_m = m;

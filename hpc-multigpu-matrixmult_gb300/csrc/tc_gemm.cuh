@@ -12,9 +12,10 @@
 //          chunks, before int32 could overflow) it folds the integer sums into
 //          the FP64 output: C[i][j] += S * 2^(ea[i] + eb[j] + 2 - 8g).
 //  kResidue Modular Ozaki GEMM: pair i multiplies the residue planes of
-//          modulus m_i; its exact int32 sum (f32 chunks of 1024 products, as
-//          in kOzaki) is reduced mod m_i and stored as one byte per element
-//          in residue plane i of R; the CRT pass (ozaki2.cu) combines them.
+//          modulus m_i; its exact int32 sum (f32 chunks of 512 products of
+//          |r| <= 181) is reduced mod m_i and stored as one 16-bit residue per
+//          element in residue plane i of R; the CRT pass (ozaki2.cu) combines
+//          them.
 //  kF32    3xBF16 split GEMM: all pairs accumulate into one f32 result. The
 //          tensor cores' f32 accumulation does not round to nearest, so its
 //          error grows with the number of MMAs summed; the accumulator is
@@ -42,7 +43,8 @@ enum TcMode { kOzaki = 0, kF32 = 1, kResidue = 2 };
 constexpr int kTcBM = 128;
 constexpr int kTcBK = 64;              // bf16 elements of K per stage (one 128-byte swizzle row)
 constexpr int kTcMaxPairs = 64;
-constexpr int kTcChunkSteps = 16;      // 16 x 64 = 1024 products per exact f32 chunk
+constexpr int kTcChunkSteps = 16;      // kOzaki: 16 x 64 = 1024 products (|d| <= 128) per exact f32 chunk
+constexpr int kTcResidueChunkSteps = 8;  // kResidue: 8 x 64 = 512 products (|r| <= 181) per exact f32 chunk
 constexpr int kTcF32ChunkSteps = 8;    // kF32: flush to round-to-nearest registers every 512 products
 constexpr int kTcFoldChunks = 127;     // 127 chunks of |v| <= 2^24 keep |int32 sum| < 2^31
 constexpr int kTcEpiWarps = 8;
@@ -86,9 +88,9 @@ struct TcArgs {
   const int* ea;              // kOzaki: per-row exponent of A
   const int* eb;              // kOzaki: per-column exponent of B
   int* status;
-  uint8_t* R;                 // kResidue: residue planes [pairs][M][ldr]
-  int64_t ldr;                // kResidue: row stride of a residue plane (multiple of 16)
-  int64_t rplane;             // kResidue: plane stride
+  uint16_t* R;                // kResidue: residue planes [pairs][M][ldr] (one 16-bit residue per element)
+  int64_t ldr;                // kResidue: row stride of a residue plane in elements (multiple of 16)
+  int64_t rplane;             // kResidue: plane stride in elements
 };
 
 // Grouped mode: many independent problems in one persistent launch. The
@@ -103,7 +105,7 @@ struct TcGroupProblem {
   int64_t ldc;
   const int* ea;
   const int* eb;
-  uint8_t* R;                 // kResidue: this problem's residue planes, their row and plane strides
+  uint16_t* R;                // kResidue: this problem's residue planes, their row and plane strides
   int64_t ldr;
   int64_t rplane;
 };
@@ -125,7 +127,7 @@ struct TcJob {
   int64_t ldc;
   const int* ea;
   const int* eb;
-  uint8_t* R;
+  uint16_t* R;
   int64_t ldr;
   int64_t rplane;
 };
@@ -360,7 +362,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           else
             gend = pairs.n;
           const int total = (gend - gstart) * job.nk;
-          const int chunk = MODE != kF32 ? kTcChunkSteps : kTcF32ChunkSteps;
+          const int chunk = MODE == kOzaki ? kTcChunkSteps : MODE == kResidue ? kTcResidueChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
             const int len = min(chunk, total - done);
             if (!wait_parity(&tempty[buf], tphase[buf] ^ 1, status, 12)) { ok = false; break; }
@@ -439,7 +441,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         else
           gend = pairs.n;
         const int total = (gend - gstart) * job.nk;
-        const int chunk = MODE != kF32 ? kTcChunkSteps : kTcF32ChunkSteps;
+        const int chunk = MODE == kOzaki ? kTcChunkSteps : MODE == kResidue ? kTcResidueChunkSteps : kTcF32ChunkSteps;
         const int nchunks = (total + chunk - 1) / chunk;
         for (int c = 0; c < nchunks && ok; ++c) {
           // all lanes must agree before the warp-collective tcgen05.ld below
@@ -488,27 +490,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               for (int u = 0; u < HALF; ++u) acc[u] = static_cast<int32_t>(mod_signed(acc[u], m, magic));
               continue;
             }
-            // One byte per element: the thread's row segment of HALF columns is
-            // contiguous in the residue plane, reduced and stored 16 columns
-            // (one 16-byte vector) at a time.
+            // One 16-bit residue per element: the thread's row segment of HALF
+            // columns is contiguous in the residue plane, reduced and stored 8
+            // columns (one 16-byte vector) at a time.
             const int64_t grow = row0 + lane;
-            uint8_t* rp = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane + grow * job.ldr + col0;
+            uint16_t* rp = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane + grow * job.ldr + col0;
 #pragma unroll
-            for (int u = 0; u < HALF; u += 16) {
+            for (int u = 0; u < HALF; u += 8) {
               uint32_t w[4];
 #pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                w[q] = 0;
-#pragma unroll
-                for (int v = 0; v < 4; ++v) w[q] |= mod_signed(acc[u + 4 * q + v], m, magic) << (8 * v);
-              }
+              for (int q = 0; q < 4; ++q)
+                w[q] = mod_signed(acc[u + 2 * q], m, magic) | (mod_signed(acc[u + 2 * q + 1], m, magic) << 16);
               if (grow < job.M) {
-                if (col0 + u + 16 <= job.N) {
+                if (col0 + u + 8 <= job.N) {
                   *reinterpret_cast<uint4*>(rp + u) = make_uint4(w[0], w[1], w[2], w[3]);
                 } else {
 #pragma unroll
-                  for (int q = 0; q < 16; ++q)
-                    if (col0 + u + q < job.N) rp[u + q] = static_cast<uint8_t>(w[q >> 2] >> (8 * (q & 3)));
+                  for (int q = 0; q < 8; ++q)
+                    if (col0 + u + q < job.N) rp[u + q] = static_cast<uint16_t>(w[q >> 1] >> (16 * (q & 1)));
                 }
               }
             }
@@ -610,6 +609,6 @@ struct TcGemmOpts {
 template <int BN, int MODE>
 int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA, int nplanesB, int64_t ldp, int m,
                          int n, int k, const PairList& pairs, void* C, int64_t ldc, const int* ea, const int* eb,
-                         cudaStream_t stream, uint8_t* R, int64_t ldr, int64_t rplane, const TcGemmOpts& opt = {});
+                         cudaStream_t stream, uint16_t* R, int64_t ldr, int64_t rplane, const TcGemmOpts& opt = {});
 
 }  // namespace phpc

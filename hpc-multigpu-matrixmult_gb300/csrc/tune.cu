@@ -3,7 +3,7 @@
 // Order of precedence for each choice: an environment variable, then the
 // tuning table written by the autotuner (PHPC_TUNE_TABLE, or tune_table.txt
 // next to the library), then a built-in default. Schemes: the modular one
-// (PHPC_MODULI = 8..16 residue GEMMs; built-in default: the fewest moduli
+// (PHPC_MODULI = 8..15 residue GEMMs; built-in default: the fewest moduli
 // whose operand grid has at least 51 bits, Frobenius error about 2e-15 on
 // inputs whose exponents spread over 2^+-20 inside a row) or, with
 // PHPC_MODULI=0 or a table entry of 0 moduli, the digit scheme (PHPC_SLICES =
@@ -22,7 +22,7 @@
 namespace phpc {
 namespace {
 
-constexpr int kMinModuliCount = 8, kMaxModuliCount = 16;  // range of the modular scheme
+constexpr int kMinModuliCount = 8, kMaxModuliCount = 15;  // range of the modular scheme
 
 struct TuneEntry {
   long long max_mnk;  // entry applies to problems with m*n*k <= max_mnk (first match wins)

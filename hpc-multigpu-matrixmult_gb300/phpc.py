@@ -281,7 +281,7 @@ class GroupedPlan:
 
     problems: list of (m, k, n, A, lda, B, ldb, C, ldc) with device pointers or
     torch tensors. The caller keeps the matrices and the workspace alive.
-    moduli=q (8..16) plans the modular scheme; otherwise the digit scheme with
+    moduli=q (8..15) plans the modular scheme; otherwise the digit scheme with
     `slices` slices."""
 
     def __init__(self, problems, slices, workspace, workspace_bytes, stream=None, moduli=0):

@@ -84,10 +84,12 @@ int phpc_dgemm_ozaki_dev(int m, int k, int n, const double *dA, int64_t lda, con
                          double *dC, int64_t ldc, int slices, void *workspace, size_t workspace_bytes, void *stream);
 
 /* FP64-accurate GEMM by the modular (Chinese-remainder) Ozaki scheme:
- * C += A * B from `moduli` (8..16) residue GEMMs. Each operand element becomes
+ * C += A * B from `moduli` (8..15) residue GEMMs. Each operand element becomes
  * an integer on the fixed-point grid of its row (A) / column (B), b bits wide
  * with b the largest width for which 2 K 2^(2b) < M = product of the moduli
- * (moduli = 16: b = 55 at K = 16384); its residues (|r| <= 128) are exact in
+ * (moduli = 14: b = 51, moduli = 15: b = 55 at K = 16384); its residues
+ * modulo the pairwise-coprime moduli 363, 362, 361, 359, 355, 353, 349, 347,
+ * 343, 337, 331, 317, 313, 311, 307 (the first `moduli`; |r| <= 181) are exact in
  * BF16, the residue products run on tcgen05, and the exact integer product is
  * recovered by the CRT and rounded once to double. */
 size_t phpc_ozaki2_workspace_bytes(int m, int k, int n, int moduli);
@@ -171,7 +173,7 @@ size_t phpc_grouped_workspace_bytes(const phpc_gemm_problem *problems, int count
  * counterpart: the reference runs one GEMM per call (src/phpc_gemm.cu:59). */
 int phpc_grouped_plan_create(phpc_grouped_plan **plan, const phpc_gemm_problem *problems, int count, int slices,
                              void *workspace, size_t workspace_bytes, void *stream);
-/* The same on the modular (CRT) scheme with `moduli` (8..16) residue GEMMs per
+/* The same on the modular (CRT) scheme with `moduli` (8..15) residue GEMMs per
  * problem; each problem's grid width follows from its own K. */
 size_t phpc_grouped_modular_workspace_bytes(const phpc_gemm_problem *problems, int count, int moduli);
 int phpc_grouped_modular_plan_create(phpc_grouped_plan **plan, const phpc_gemm_problem *problems, int count,
@@ -189,7 +191,7 @@ void phpc_grouped_plan_destroy(phpc_grouped_plan *plan);
 int phpc_default_slices(int m, int k, int n);
 
 /* Scheme phpc_gemm_cublas uses for an m x k x n problem: the number of moduli
- * of the modular scheme (8..16), or 0 for the digit scheme with
+ * of the modular scheme (8..15), or 0 for the digit scheme with
  * phpc_default_slices slices (PHPC_MODULI, else the autotuner's table, else
  * the fewest moduli giving a grid of at least 51 bits). */
 int phpc_default_moduli(int m, int k, int n);

@@ -21,7 +21,7 @@ import numpy as np
 import ozaki_model
 
 # Pairwise-coprime moduli, largest first (the library's table).
-MODULI = [256, 255, 253, 251, 247, 241, 239, 233, 229, 227, 223, 211, 199, 197, 193, 191, 181, 179, 173, 167]
+MODULI = [363, 362, 361, 359, 355, 353, 349, 347, 343, 337, 331, 317, 313, 311, 307]
 
 
 def bits_for(nmod: int, k: int) -> int:

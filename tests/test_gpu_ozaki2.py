@@ -15,8 +15,6 @@ from golden_inputs import golden_cases, golden_inputs
 pytestmark = pytest.mark.gpu
 
 
-# (40, 2048, 72) at 14 moduli has K 2^(2b) / M = 0.493: the reconstruction
-# takes its exact multi-step path there and the one-step path elsewhere.
 
 
 def run_dev(phpc, torch, a, b, c0, nmod):
@@ -33,7 +31,7 @@ def run_dev(phpc, torch, a, b, c0, nmod):
     return C.cpu().numpy()
 
 
-@pytest.mark.parametrize("nmod", [8, 12, 14, 16])
+@pytest.mark.parametrize("nmod", [8, 12, 14, 15])
 @pytest.mark.parametrize("m,k,n", [(128, 64, 256), (70, 300, 130), (7, 13, 5), (200, 1100, 96), (40, 2048, 72)])
 def test_bitexact_vs_model(phpc, torch_cuda, nmod, m, k, n):
     rng = np.random.default_rng(nmod * 1009 + m + k + n)
@@ -51,8 +49,8 @@ def test_bitexact_tile_variants(phpc, torch_cuda, monkeypatch, cluster, bn):
     rng = np.random.default_rng(77)
     a = rng.uniform(-1, 1, (300, 400))
     b = rng.uniform(-1, 1, (400, 520))
-    got = run_dev(phpc, torch_cuda, a, b, np.zeros((300, 520)), 16)
-    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 16))
+    got = run_dev(phpc, torch_cuda, a, b, np.zeros((300, 520)), 15)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 15))
 
 
 @pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] == "index"], ids=lambda c: c["name"])
@@ -60,7 +58,7 @@ def test_index_inputs_exact(case, phpc, torch_cuda, oracle):
     a, b, c = golden_inputs(case)
     ref = c.copy()
     oracle.gemm_iterative(a, b, ref)
-    np.testing.assert_array_equal(run_dev(phpc, torch_cuda, a, b, c, 16), ref)
+    np.testing.assert_array_equal(run_dev(phpc, torch_cuda, a, b, c, 15), ref)
 
 
 @pytest.mark.parametrize("dist", ["uniform", "wide"])
@@ -72,7 +70,7 @@ def test_n1024_frobenius_1e14(phpc, torch_cuda, oracle, dist):
     if dist == "wide":
         a *= np.exp2(rng.integers(-20, 21, (n, n)))
         b *= np.exp2(rng.integers(-20, 21, (n, n)))
-    c = run_dev(phpc, torch_cuda, a, b, np.zeros((n, n)), 16)
+    c = run_dev(phpc, torch_cuda, a, b, np.zeros((n, n)), 15)
     rows = np.arange(0, n, 16)
     err = oracle.rel_errors(c[rows], oracle.gemm_dd(a, b, rows=rows))
     assert err["frob"] <= 1e-15 and err["max"] <= 1e-15, err
@@ -85,17 +83,17 @@ def test_zero_rows_columns_and_argument_errors(phpc, torch_cuda):
     a[3] = 0.0
     b[:, 7] = 0.0
     c0 = rng.uniform(-1, 1, (64, 80))
-    got = run_dev(phpc, torch_cuda, a, b, c0, 16)
-    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 16))
+    got = run_dev(phpc, torch_cuda, a, b, c0, 15)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 15))
     np.testing.assert_array_equal(got[3], c0[3])
     torch = torch_cuda
     A = torch.zeros(64, 64, dtype=torch.float64, device="cuda")
     W = torch.empty(16, dtype=torch.uint8, device="cuda")
     with pytest.raises(phpc.PhpcError) as e:
-        phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 16, W, 16)
+        phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 15, W, 16)
     assert e.value.code == 6
     with pytest.raises(phpc.PhpcError) as e:
-        phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 17, W, 16)
+        phpc.dgemm_ozaki2_dev(64, 64, 64, A, 64, A, 64, A, 64, 16, W, 16)
     assert e.value.code == 1
 
 
@@ -163,3 +161,19 @@ def test_host_pipeline_nonfinite_in_last_panel(phpc, monkeypatch):
     np.testing.assert_array_equal(np.isinf(c), np.isinf(want))
     fin = np.isfinite(want)
     np.testing.assert_allclose(c[fin], want[fin], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("nmod", [12, 14])
+def test_crt_multi_step_path_same_bits(phpc, torch_cuda, monkeypatch, nmod):
+    """The CRT's exact multi-step path (forced) gives the same bits as the
+    one-step path the library's moduli always allow, and as the model."""
+    rng = np.random.default_rng(nmod)
+    m, k, n = 90, 700, 140
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+    b = rng.uniform(-1, 1, (k, n))
+    c0 = rng.uniform(-1, 1, (m, n))
+    fast = run_dev(phpc, torch_cuda, a, b, c0, nmod)
+    monkeypatch.setenv("PHPC_CRT_EXACT", "1")
+    exact = run_dev(phpc, torch_cuda, a, b, c0, nmod)
+    np.testing.assert_array_equal(exact, fast)
+    np.testing.assert_array_equal(exact, ozaki2_model.gemm(a, b, c0, nmod))

@@ -177,19 +177,20 @@ def test_moduli_pairwise_coprime_and_bits():
 
     import ozaki2_model
 
-    mods = ozaki2_model.MODULI[:16]
+    mods = ozaki2_model.MODULI[:15]
     for i in range(len(mods)):
         for j in range(i + 1, len(mods)):
             assert math.gcd(mods[i], mods[j]) == 1
-    assert ozaki2_model.bits_for(16, 16384) == 55
-    for nmod in range(8, 17):
+    assert ozaki2_model.bits_for(15, 16384) == 55 and ozaki2_model.bits_for(14, 16384) == 51
+    assert max(mods) <= 363 and math.prod(mods) < 2 ** 128
+    for nmod in range(8, 16):
         for k in (16, 1000, 16384):
             b = ozaki2_model.bits_for(nmod, k)
             assert 2 * k * 2 ** (2 * b) < math.prod(mods[:nmod])
 
 
-@pytest.mark.parametrize("dist,nmod,bound", [("uniform", 16, 1e-16), ("wide", 16, 1e-16), ("wide", 14, 5e-15),
-                                             ("uniform", 12, 2e-13)])
+@pytest.mark.parametrize("dist,nmod,bound", [("uniform", 15, 1e-16), ("wide", 15, 1e-16), ("wide", 13, 5e-15),
+                                             ("uniform", 11, 2e-13)])
 def test_crt_model_error_vs_dd_oracle(oracle, dist, nmod, bound):
     import ozaki2_model
 

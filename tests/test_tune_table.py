@@ -49,12 +49,12 @@ def test_scheme_selection(built, tmp_path):
 
     t = tmp_path / "table.txt"
     t.write_text(f"{1024**3} 7 128 8 1 0\n" + f"{4096**3} 7 256 8 2 14\n" + f"{2**62} 7 256 8 1\n")
-    rule = [min(q for q in range(8, 17) if ozaki2_model.bits_for(q, n) >= 51) for n in (256, 1024, 4096, 16384)]
-    assert rule == [15, 15, 15, 15]
+    rule = [min(q for q in range(8, 16) if ozaki2_model.bits_for(q, n) >= 51) for n in (256, 1024, 4096, 16384)]
+    assert rule == [14, 14, 14, 14]
     assert _probe(built, {"PHPC_TUNE_TABLE": str(t)}, "phpc_default_moduli") == [0, 0, 14, rule[3]]
     missing = str(tmp_path / "missing.txt")
     assert _probe(built, {"PHPC_TUNE_TABLE": missing}, "phpc_default_moduli") == rule
-    assert _probe(built, {"PHPC_TUNE_TABLE": missing, "PHPC_MODULI": "16"}, "phpc_default_moduli") == [16] * 4
+    assert _probe(built, {"PHPC_TUNE_TABLE": missing, "PHPC_MODULI": "15"}, "phpc_default_moduli") == [15] * 4
     assert _probe(built, {"PHPC_TUNE_TABLE": str(t), "PHPC_MODULI": "0"}, "phpc_default_moduli") == [0] * 4
 
 
@@ -66,4 +66,4 @@ def test_committed_table_is_well_formed():
         mnk, s, bn, gr = f[:4]
         assert 2 <= s <= 8 and bn in (128, 256) and 1 <= gr <= 64
         assert len(f) == 4 or f[4] in (1, 2)
-        assert len(f) <= 5 or f[5] == 0 or 8 <= f[5] <= 16
+        assert len(f) <= 5 or f[5] == 0 or 8 <= f[5] <= 15
