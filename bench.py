@@ -62,7 +62,7 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 # (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by
 # (N, "slices" | "moduli", count).
 NCU_TRAFFIC_BYTES = {(16384, "slices", 7): 426.25e9 + 15.28e9,
-                     (16384, "moduli", 15): 178.37e9 + 4.06e9}
+                     (16384, "moduli", 14): 153.23e9 + 7.52e9}
 UNIT = "TFLOP/s"
 
 
