@@ -55,19 +55,41 @@ def split(x: np.ndarray, e: np.ndarray, s: int) -> np.ndarray:
     return d.astype(np.float64)
 
 
+FOLD_STEPS = 127 * 16  # K-steps of 64 between two folds of a diagonal (int32 range of 127 exact f32 chunks)
+
+
 def gemm(a: np.ndarray, b: np.ndarray, c0: np.ndarray | None, s: int) -> np.ndarray:
+    """The digit scheme's result, folds included: per diagonal g the pairs
+    (p, g - p), p ascending, are streamed as K-steps of 64; the exact integer
+    sum is added into C (one FP64 rounding) every FOLD_STEPS steps of that
+    stream and at its end."""
     ea = exponents(a, axis=1)
     eb = exponents(b, axis=0)
     da = split(a, ea[:, None], s)
     db = split(b, eb[None, :], s)
     c = np.zeros((a.shape[0], b.shape[1])) if c0 is None else c0.astype(np.float64).copy()
     base = ea[:, None] + eb[None, :]
+    k = a.shape[1]
+    nk = -(-k // 64)
     for g in range(2, s + 2):
+        scale = np.clip(base + 2 - 8 * g, -30000, 30000).astype(np.int64)
         sg = np.zeros_like(c)
+        done = 0  # steps accumulated since the last fold
         for p in range(1, g):
             q = g - p
             if p > s or q > s:
                 continue
-            sg += da[p - 1] @ db[q - 1]
-        c = c + np.ldexp(sg, np.clip(base + 2 - 8 * g, -30000, 30000).astype(np.int64))
+            st = 0
+            while st < nk:
+                take = min(nk - st, FOLD_STEPS - done)
+                lo, hi = st * 64, min(k, (st + take) * 64)
+                sg += da[p - 1][:, lo:hi] @ db[q - 1][lo:hi, :]
+                st += take
+                done += take
+                if done == FOLD_STEPS:
+                    c = c + np.ldexp(sg, scale)
+                    sg = np.zeros_like(c)
+                    done = 0
+        if done:
+            c = c + np.ldexp(sg, scale)
     return c

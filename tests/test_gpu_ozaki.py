@@ -173,3 +173,16 @@ def test_bitexact_vs_model_cta_pair(phpc, torch_cuda, monkeypatch, s, m, k, n, b
     c0 = rng.uniform(-1, 1, (m, n))
     got = run_dev(phpc, torch_cuda, a, b, c0, s)
     np.testing.assert_array_equal(got, ozaki_model.gemm(a, b, c0, s))
+
+
+def test_long_k_intermediate_fold(phpc, torch_cuda):
+    """K = 140000 > 127 chunks of 1024 products: the digit scheme folds the
+    int32 sums into C in the middle of a diagonal (before they could
+    overflow); bit-identical to the digit model."""
+    rng = np.random.default_rng(140000)
+    m, k, n = 8, 140000, 16
+    a = rng.uniform(-1, 1, (m, k))
+    b = rng.uniform(-1, 1, (k, n))
+    c0 = rng.uniform(-1, 1, (m, n))
+    got = run_dev(phpc, torch_cuda, a, b, c0, 7)
+    np.testing.assert_array_equal(got, ozaki_model.gemm(a, b, c0, 7))

@@ -177,3 +177,38 @@ def test_crt_multi_step_path_same_bits(phpc, torch_cuda, monkeypatch, nmod):
     exact = run_dev(phpc, torch_cuda, a, b, c0, nmod)
     np.testing.assert_array_equal(exact, fast)
     np.testing.assert_array_equal(exact, ozaki2_model.gemm(a, b, c0, nmod))
+
+
+def test_long_k_intermediate_reduction(phpc, torch_cuda):
+    """K = 70000 > 127 chunks of 512 products: the int32 sums are reduced mod
+    m_i in the middle of a modulus (before they could overflow) and the
+    result stays bit-identical to the exact model."""
+    rng = np.random.default_rng(70000)
+    m, k, n = 12, 70000, 20
+    a = rng.uniform(-1, 1, (m, k))
+    b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-8, 9, (k, n)))
+    c0 = rng.uniform(-1, 1, (m, n))
+    got = run_dev(phpc, torch_cuda, a, b, c0, 14)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 14))
+
+
+def test_strided_leading_dimensions(phpc, torch_cuda):
+    """Operands and result as sub-blocks of wider matrices (lda > k, ldb > n,
+    ldc > n): the untouched columns of C stay as they were."""
+    torch = torch_cuda
+    rng = np.random.default_rng(33)
+    m, k, n = 150, 260, 90
+    A_full = rng.uniform(-1, 1, (m, k + 13))
+    B_full = rng.uniform(-1, 1, (k, n + 7))
+    C_full = rng.uniform(-1, 1, (m, n + 5))
+    a, b, c0 = A_full[:, :k], B_full[:, :n], C_full[:, :n]
+    want = ozaki2_model.gemm(np.ascontiguousarray(a), np.ascontiguousarray(b), np.ascontiguousarray(c0), 14)
+    A, B, C = (torch.from_numpy(x).cuda() for x in (A_full, B_full, C_full))
+    ws = phpc.ozaki2_workspace_bytes(m, k, n, 14)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    phpc.dgemm_ozaki2_dev(m, k, n, A, k + 13, B, n + 7, C, n + 5, 14, W, ws)
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    got = C.cpu().numpy()
+    np.testing.assert_array_equal(got[:, :n], want)
+    np.testing.assert_array_equal(got[:, n:], C_full[:, n:])
