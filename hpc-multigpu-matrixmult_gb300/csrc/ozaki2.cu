@@ -162,7 +162,7 @@ int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const do
 }
 
 // The residue GEMMs of rows [r0, r0 + rows): plane i of R = (A_i * B_i^T) mod
-// m_i, one byte per element. Tile width, cluster and raster are those of the
+// m_i, one 16-bit residue per element. Tile width, cluster and raster are those of the
 // full m x k x n problem.
 int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const void* ws, size_t ws_bytes,
                          cudaStream_t stream, int bn) {

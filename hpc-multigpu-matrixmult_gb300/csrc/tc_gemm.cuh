@@ -64,7 +64,7 @@ struct PairList {
   uint32_t magic[kTcMaxPairs];  // kResidue: floor(2^32 / modulus)
 };
 
-// x mod m for 0 <= x < 2^32, m <= 256, magic = floor(2^32 / m) (Barrett: the
+// x mod m for 0 <= x < 2^32, 2 <= m < 2^16, magic = floor(2^32 / m) (Barrett: the
 // quotient estimate is low by at most one).
 __device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t m, uint32_t magic) {
   const uint32_t q = __umulhi(x, magic);

@@ -8,7 +8,9 @@
  * 9-column row (src/utils.c:26-27):
  *   N,size,gpu_count,num_blocks,threads_per_block,total_threads,
  *   cuda_time,cuda_gpu_time,cublas_time
- * "cuda" is the plain FP64 DMMA SUMMA, "cublas" the FP64-accurate Ozaki SUMMA.
+ * "cuda" is the plain FP64 SUMMA (phpc_gemm_cuda), "cublas" the FP64-accurate
+ * Ozaki SUMMA (phpc_gemm_cublas); the _ext.csv method names are "dmma" and
+ * "ozaki_split" for them.
  *
  * Differences from the reference, all opt-in or corrective:
  *  - C is zeroed before each method (the reference accumulated the second

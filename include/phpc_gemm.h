@@ -46,7 +46,10 @@ const char *phpc_error_string(int code);
 
 /*
  * Replaces phpc_gemm_cuda (reference src/phpc_gemm.cu:59-156).
- * C[m x n] += A[m x k] * B[k x n] in plain FP64 on the tensor cores (DMMA).
+ * C[m x n] += A[m x k] * B[k x n] in plain FP64: the scalar DFMA pipe by
+ * default, the FP64 tensor cores (DMMA) with PHPC_FP64_PIPE=dmma; both give the
+ * bits of the reference's own kernel (every output summed over k in order
+ * with one rounding per fused multiply-add, then added into C).
  * grid_width x grid_height is the logical SUMMA block decomposition of C that
  * the persistent CTAs walk; block_width (the reference's thread-block edge,
  * 1..32) is validated and otherwise only reported. gpu_count is accepted for
@@ -59,16 +62,20 @@ void phpc_gemm_cuda(const double *a, int lda, const double *b, int ldb, double *
 /*
  * Replaces phpc_gemm_cublas (reference src/phpc_gemm.cu:158-174), which called
  * cuBLASXt Dgemm with alpha = beta = 1. Here the same C += A * B is computed
- * by the FP64-accurate split-precision (Ozaki) GEMM on BF16 tensor cores; the
- * slice count comes from the tuning table or PHPC_SLICES. Unlike the
- * reference, *gpu_time receives the real device time (scan + split + GEMM).
+ * by the FP64-accurate split-precision (Ozaki) GEMM on BF16 tensor cores: the
+ * modular scheme with phpc_default_moduli(m, k, n) moduli, pipelined over row
+ * panels of A and C, or the digit scheme where that is 0 (tuning table,
+ * PHPC_MODULI, PHPC_SLICES). Unlike the reference, *gpu_time receives the
+ * real device time of the kernels (scans, splits, tensor-core GEMM,
+ * reconstruction).
  */
 void phpc_gemm_cublas(const double *a, int lda, const double *b, int ldb, double *c, int ldc, int m, int k, int n,
                       int gpu_count, int grid_width, int grid_height, int block_width, float *gpu_time);
 
 /* ---------------------------------------------- device-pointer entry points */
 
-/* Plain FP64 DMMA GEMM: C += A * B. Requires 16-byte aligned pointers and even
+/* Plain FP64 GEMM (phpc_gemm_cuda's kernel; DFMA pipe, or DMMA with
+ * PHPC_FP64_PIPE=dmma): C += A * B. Requires 16-byte aligned pointers and even
  * leading dimensions (TMA). kpanel (multiple of 16, 0 = 256) is the SUMMA
  * k-panel width; grid_width/grid_height (>= 1) the logical block grid. */
 int phpc_dgemm_dmma_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb, double *dC,
@@ -98,7 +105,7 @@ int phpc_dgemm_ozaki2_dev(int m, int k, int n, const double *dA, int64_t lda, co
 
 /* The three phases of phpc_dgemm_ozaki2_dev (same workspace):
  * prepare = exponent scans + residue split of A and B;
- * multiply = the residue GEMMs (one byte per element and modulus, in the
+ * multiply = the residue GEMMs (one 16-bit residue per element and modulus, in the
  * workspace); reconstruct = CRT, rounding and C += result * 2^(ea + eb - 2b). */
 int phpc_ozaki2_prepare_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
                             int moduli, void *workspace, size_t workspace_bytes, void *stream);

@@ -6,8 +6,8 @@
  * panels; at step k the owner column broadcasts its A panel along the process
  * row, the owner row its B panel along the process column, and every process
  * adds A_panel * B_panel into its C block through the local GEMM; the blocks
- * are then gathered on rank 0. The local GEMM is phpc_gemm_cuda (plain FP64
- * DMMA) or phpc_gemm_cublas (FP64-accurate Ozaki split).
+ * are then gathered on rank 0. The local GEMM is phpc_gemm_cuda (plain FP64)
+ * or phpc_gemm_cublas (FP64-accurate Ozaki GEMM).
  *
  * Include <mpi.h> from a real MPI, or include/mpi_shim/mpi.h for the
  * single-rank build used on one-GPU nodes (`mpirun -np 1`).
