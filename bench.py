@@ -77,7 +77,7 @@ def parse_args():
                    help="modular scheme with this many moduli (8..16); 0 = digit scheme; -1 = library default")
     p.add_argument("--slices", type=int, default=0, help="digit scheme slices; 0 = library default")
     p.add_argument("--dmma-steps", type=int, default=1)
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=7)
     p.add_argument("--seed", type=int, default=20241203)
     p.add_argument("--ref-gpu-kernel", type=int, default=1,
                    help="--impl reference: also time the reference's own CUDA kernel for context (1/0)")
