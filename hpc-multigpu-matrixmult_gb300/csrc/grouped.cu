@@ -40,6 +40,7 @@ namespace {
 struct GSplitProb {
   int m, k, n;
   int row_start, col_start, sblock_start;  // prefix sums over the problems
+  int rblock_start;                        // modular scheme: residue column blocks
   int cunit_start, crt_unit_start;         // prefix sums: column-scan units, CRT units
   int nblk_j;                              // 64-column blocks of B
   int64_t lda, ldb, ldp;
@@ -136,13 +137,15 @@ __global__ void g_residue_rows_kernel(const GSplitProb* __restrict__ P, int coun
 
 __global__ void __launch_bounds__(256) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
                                                              int total_blocks, const __grid_constant__ ModTable T) {
-  __shared__ uint32_t st[8][64][17];
   const int b = blockIdx.x;
   if (b >= total_blocks) return;  // uniform over the CTA
-  const GSplitProb& p = P[locate(P, count, b, [](const GSplitProb& q) { return q.sblock_start; })];
-  const int lb = b - p.sblock_start;
-  const int64_t j0 = (int64_t)(lb % p.nblk_j) * 64, k0 = (int64_t)(lb / p.nblk_j) * 32;
-  residue_col_block(p.B, p.ldb, p.k, p.n, p.eb, p.bits, T, p.pb, p.ldp, (int64_t)p.n * p.ldp, k0, j0, st);
+  const GSplitProb& p = P[locate(P, count, b, [](const GSplitProb& q) { return q.rblock_start; })];
+  const int lb = b - p.rblock_start;
+  const int nblk_j = (p.n + kColBlockJ - 1) / kColBlockJ;
+  const int64_t col = (int64_t)(lb % nblk_j) * kColBlockJ + (threadIdx.x >> 3);
+  const int64_t k0 = (int64_t)(lb / nblk_j) * kColBlockK + (threadIdx.x & 7) * 8;
+  if (col >= p.n || k0 >= p.ldp) return;
+  residue_col_piece(p.B, p.ldb, p.k, col, p.eb[col], p.bits, T, p.pb + col * p.ldp, (int64_t)p.n * p.ldp, k0);
 }
 
 constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one warp)
@@ -236,7 +239,8 @@ PairList residue_pairs(const ModTable& T) {
 struct phpc_grouped_plan {
   int device;
   int count, s, moduli, bn;  // moduli > 0: modular scheme (s unused)
-  int total_rows, total_cols, total_sblocks, total_tiles, max_kgroups, total_cunits, total_crt_units;
+  int total_rows, total_cols, total_sblocks, total_rblocks, total_tiles, max_kgroups, total_cunits,
+      total_crt_units;
   phpc::GSplitProb* d_split;
   phpc::TcGroupTable table;
   phpc::PairList pairs;
@@ -285,7 +289,7 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
     if (modular) {
       g_residue_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
                                                                                        pl->total_rows, pl->mods);
-      g_residue_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks,
+      g_residue_cols_kernel<<<pl->total_rblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rblocks,
                                                                    pl->mods);
     } else {
       g_split_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
@@ -354,7 +358,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   std::vector<TcGroupProblem> ht(count);
   std::vector<CUtensorMap> hm(2 * (size_t)count);
   size_t off = T.end;
-  int rows = 0, cols = 0, sblocks = 0, tiles = 0, maxkg = 1;
+  int rows = 0, cols = 0, sblocks = 0, rblocks = 0, tiles = 0, maxkg = 1;
   int64_t cunits = 0, crt_units = 0;
   for (int i = 0; i < count && rc == PHPC_OK; ++i) {
     const phpc_gemm_problem& q = problems[i];
@@ -368,6 +372,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     g.row_start = rows;
     g.col_start = cols;
     g.sblock_start = sblocks;
+    g.rblock_start = rblocks;
     g.cunit_start = static_cast<int>(cunits);
     g.crt_unit_start = static_cast<int>(crt_units);
     g.nblk_j = ceil_div(q.n, 64);
@@ -391,6 +396,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     rows += q.m;
     cols += q.n;
     sblocks += g.nblk_j * ceil_div(q.k, 32);
+    rblocks += ceil_div(q.n, kColBlockJ) * ceil_div((int)L.ldp, kColBlockK);
     maxkg = std::max(maxkg, ceil_div(L.ldp / 8, 128));
     cunits += (int64_t)q.n * ceil_div(q.k, kScanKChunk);
     if (modular) crt_units += (int64_t)q.m * ceil_div(q.n, kCrtUnitCols);
@@ -430,6 +436,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->total_rows = rows;
   pl->total_cols = cols;
   pl->total_sblocks = sblocks;
+  pl->total_rblocks = rblocks;
   pl->total_tiles = tiles;
   pl->max_kgroups = maxkg;
   pl->total_cunits = static_cast<int>(cunits);

@@ -46,15 +46,17 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
   residue_row_piece(A + row * lda, K, ea[row], T.bits, T, planes + row * ldp, plane_stride, k0);
 }
 
-// B residue planes, transposed ([n][N][ldp]): one 32 (k) x 64 (j) block per CTA.
+// B residue planes, transposed ([n][N][ldp]): one kColBlockK x kColBlockJ
+// block per 256-thread CTA (residue.cuh).
 __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
                                                            const int* __restrict__ eb,
                                                            const __grid_constant__ ModTable T,
                                                            uint16_t* __restrict__ planes, int64_t ldp,
                                                            int64_t plane_stride) {
-  __shared__ uint32_t st[8][64][17];
-  residue_col_block(B, ldb, K, N, eb, T.bits, T, planes, ldp, plane_stride, (int64_t)blockIdx.y * 32,
-                    (int64_t)blockIdx.x * 64, st);
+  const int64_t col = (int64_t)blockIdx.x * kColBlockJ + (threadIdx.x >> 3);
+  const int64_t k0 = (int64_t)blockIdx.y * kColBlockK + (threadIdx.x & 7) * 8;
+  if (col >= N || k0 >= ldp) return;
+  residue_col_piece(B, ldb, K, col, eb[col], T.bits, T, planes + col * ldp, plane_stride, k0);
 }
 
 // C[i][j] += C_int * 2^(ea[i] + eb[j] - 2b), C_int recovered from the residues.
@@ -147,8 +149,8 @@ int ozaki2_prepare_b(int m, int k, int n, const double* dB, int64_t ldb, int nmo
   fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(V.eb, n, kExpZero);
   scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream>>>(dB, ldb, k, n, 256, V.eb,
                                                                                   device_status_ptr());
-  residue_cols_kernel<<<dim3(ceil_div(n, 64), ceil_div(k, 32)), 256, 0, stream>>>(dB, ldb, k, n, V.eb, T, V.pb,
-                                                                                  L.ldp, (int64_t)n * L.ldp);
+  residue_cols_kernel<<<dim3(ceil_div(n, kColBlockJ), ceil_div(L.ldp, kColBlockK)), 256, 0, stream>>>(
+      dB, ldb, k, n, V.eb, T, V.pb, L.ldp, (int64_t)n * L.ldp);
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
 }

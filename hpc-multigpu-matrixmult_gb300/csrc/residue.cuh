@@ -30,9 +30,10 @@ struct ModTable {
   int bits;  // b: operands are integers of magnitude <= 2^b
   uint32_t m[kMaxModuli];
   uint32_t magic[kMaxModuli];  // floor(2^32 / m)
-  float cf[kMaxModuli][4];     // symmetric residues of 2^13, 2^26, 2^39, 2^52 mod m (|c| <= 181)
-  float invm[kMaxModuli];      // 1 / m rounded to float
-  float mf[kMaxModuli];        // m as a float
+  // Per modulus, each value twice (both lanes of a packed f32x2 FMA):
+  float2 cf[kMaxModuli][4];  // symmetric residues of 2^13, 2^26, 2^39, 2^52 mod m (|c| <= 181)
+  float2 invm[kMaxModuli];   // 1 / m rounded to float
+  float2 negm[kMaxModuli];   // -m
   CrtTable crt;                // the reconstruction's constants
 };
 
@@ -74,10 +75,12 @@ inline ModTable make_table(int nmod, int k) {
     T.magic[i] = static_cast<uint32_t>((1ull << 32) / m);
     for (int j = 0; j < 4; ++j) {
       const int64_t c = static_cast<int64_t>((1ull << (13 * (j + 1))) % m);
-      T.cf[i][j] = static_cast<float>(2 * c > static_cast<int64_t>(m) ? c - m : c);
+      const float cs = static_cast<float>(2 * c > static_cast<int64_t>(m) ? c - m : c);
+      T.cf[i][j] = make_float2(cs, cs);
     }
-    T.invm[i] = 1.0f / static_cast<float>(m);
-    T.mf[i] = static_cast<float>(m);
+    const float rm = 1.0f / static_cast<float>(m);
+    T.invm[i] = make_float2(rm, rm);
+    T.negm[i] = make_float2(-static_cast<float>(m), -static_cast<float>(m));
     const u128 Mi = M / m;
     const uint32_t mi_mod = static_cast<uint32_t>(Mi % m);
     uint32_t inv = 0;
@@ -120,23 +123,56 @@ __device__ __forceinline__ void balanced_limbs(uint64_t X, bool neg, float (&L)[
   L[kLimbs - 1] = float_of_small_int(neg ? -top : top);
 }
 
-// Residue of V modulo m_i with |r| <= 181, in single precision, exactly:
-// t = L_0 + sum_j L_j (2^(13 j) mod m, symmetric) is an integer with
-// |t| < 2.5 * 2^20 (exact in float at every step); q = round(t * fl(1/m))
-// through the 1.5 * 2^23 rounding constant is round(t / m) except within
-// 0.001 of a tie, so r = t - q m (one exact FMA) has |r| <= 0.501 m, i.e.
-// |r| <= 181 for m <= 363.
-__device__ __forceinline__ float residue_of(const float (&L)[kLimbs], const ModTable& T, int i) {
-  const float t =
-      fmaf(L[4], T.cf[i][3], fmaf(L[3], T.cf[i][2], fmaf(L[2], T.cf[i][1], fmaf(L[1], T.cf[i][0], L[0]))));
-  const float q = fmaf(t, T.invm[i], 12582912.0f) - 12582912.0f;
-  return fmaf(-q, T.mf[i], t);
-}
-
 // Two residues as a packed BF16 pair (lo in the low half): integer-valued
 // floats of magnitude <= 256 have zero low 16 bits.
 __device__ __forceinline__ uint32_t bf16x2_of_float_ints(float lo, float hi) {
   return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+// Residues of two operand integers (limbs L, one value per lane) modulo m_i
+// with |r| <= 181, in single precision, exactly, two lanes per packed f32x2
+// instruction: t = L_0 + sum_j L_j (2^(13 j) mod m, symmetric) is an integer
+// with |t| < 2.5 * 2^20 (exact in float at every step); q = round(t * fl(1/m))
+// through the 1.5 * 2^23 rounding constant is round(t / m) except within
+// 0.001 of a tie, so r = t - q m (one exact FMA) has |r| <= 0.501 m, i.e.
+// |r| <= 181 for m <= 363.
+__device__ __forceinline__ float2 residue_pair(const float2 (&L)[kLimbs], const ModTable& T, int i) {
+  const float2 kRound = make_float2(12582912.0f, 12582912.0f);
+  const float2 kUnround = make_float2(-12582912.0f, -12582912.0f);
+  float2 t = __ffma2_rn(L[1], T.cf[i][0], L[0]);
+  t = __ffma2_rn(L[2], T.cf[i][1], t);
+  t = __ffma2_rn(L[3], T.cf[i][2], t);
+  t = __ffma2_rn(L[4], T.cf[i][3], t);
+  const float2 q = __fadd2_rn(__ffma2_rn(t, T.invm[i], kRound), kUnround);
+  return __ffma2_rn(q, T.negm[i], t);
+}
+
+// Limbs of the 8 values v[0..7] as 4 lane pairs (v[2p], v[2p + 1]).
+__device__ __forceinline__ void limb_pairs(const double (&v)[8], int e, int bits, float2 (&P)[4][kLimbs]) {
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    float L0[kLimbs], L1[kLimbs];
+    bool n0, n1;
+    balanced_limbs(fixed_point(v[2 * p], e, bits, n0), n0, L0);
+    balanced_limbs(fixed_point(v[2 * p + 1], e, bits, n1), n1, L1);
+#pragma unroll
+    for (int j = 0; j < kLimbs; ++j) P[p][j] = make_float2(L0[j], L1[j]);
+  }
+}
+
+// Residue planes of 8 consecutive values (limb pairs P): plane i gets one
+// 16-byte vector at out + i * plane_stride.
+__device__ __forceinline__ void store_residues8(const float2 (&P)[4][kLimbs], const ModTable& T,
+                                                uint16_t* __restrict__ out, int64_t plane_stride) {
+  for (int i = 0; i < T.n; ++i) {
+    uint32_t w[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const float2 r = residue_pair(P[p], T, i);
+      w[p] = bf16x2_of_float_ints(r.x, r.y);
+    }
+    *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
 }
 
 // Residue planes of row piece [k0, k0 + 8) of one operand row a (K long,
@@ -144,61 +180,33 @@ __device__ __forceinline__ uint32_t bf16x2_of_float_ints(float lo, float hi) {
 __device__ __forceinline__ void residue_row_piece(const double* __restrict__ a, int K, int e, int bits,
                                                   const ModTable& T, uint16_t* __restrict__ out,
                                                   int64_t plane_stride, int64_t k0) {
-  float L[8][kLimbs];
+  double v[8];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    bool neg;
-    const uint64_t X = fixed_point(k0 + j < K ? a[k0 + j] : 0.0, e, bits, neg);
-    balanced_limbs(X, neg, L[j]);
-  }
-  out += k0;
-  for (int i = 0; i < T.n; ++i) {
-    uint32_t w[4];
-#pragma unroll
-    for (int j = 0; j < 8; j += 2) w[j >> 1] = bf16x2_of_float_ints(residue_of(L[j], T, i), residue_of(L[j + 1], T, i));
-    *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
-  }
+  for (int j = 0; j < 8; ++j) v[j] = k0 + j < K ? a[k0 + j] : 0.0;
+  float2 P[4][kLimbs];
+  limb_pairs(v, e, bits, P);
+  store_residues8(P, T, out + k0, plane_stride);
 }
 
-// Residue planes of the 32 (k) x 64 (j) block at (k0, j0) of B (K x N, column
-// exponents eb), written transposed ([N][ldp] per plane) through shared
-// memory 8 planes at a time; all 256 threads of the CTA take part.
-__device__ __forceinline__ void residue_col_block(const double* __restrict__ B, int64_t ldb, int K, int N,
-                                                  const int* __restrict__ eb, int bits, const ModTable& T,
-                                                  uint16_t* __restrict__ planes, int64_t ldp, int64_t plane_stride,
-                                                  int64_t k0, int64_t j0, uint32_t (&st)[8][64][17]) {
-  const int j = threadIdx.x & 63;
-  const int kp0 = threadIdx.x >> 6;  // 0..3
-  const int64_t col = j0 + j;
-  const int e = col < N ? eb[col] : kExpZero;
-  float L[8][kLimbs];
+// Residue planes of column piece [k0, k0 + 8) of column col of B (K x N, row
+// stride ldb, column exponent e), written transposed: plane i holds the
+// column as a row of [N][ldp] (out = row col of plane 0).
+__device__ __forceinline__ void residue_col_piece(const double* __restrict__ B, int64_t ldb, int K, int64_t col, int e,
+                                                  int bits, const ModTable& T, uint16_t* __restrict__ out,
+                                                  int64_t plane_stride, int64_t k0) {
+  double v[8];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) {  // k pairs kp0, kp0 + 4, ...: elements 2u, 2u + 1
-    const int64_t k = k0 + 2 * (kp0 + 4 * u);
-    bool n0, n1;
-    const uint64_t X0 = fixed_point((col < N && k < K) ? B[k * ldb + col] : 0.0, e, bits, n0);
-    const uint64_t X1 = fixed_point((col < N && k + 1 < K) ? B[(k + 1) * ldb + col] : 0.0, e, bits, n1);
-    balanced_limbs(X0, n0, L[2 * u]);
-    balanced_limbs(X1, n1, L[2 * u + 1]);
-  }
-  const int wj = threadIdx.x >> 2, q = threadIdx.x & 3;
-  const int64_t gj = j0 + wj, gk = k0 + 8 * q;
-  for (int i0 = 0; i0 < T.n; i0 += 8) {
-    const int cnt = min(8, T.n - i0);
-    for (int p = 0; p < cnt; ++p) {
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        st[p][j][kp0 + 4 * u] =
-            bf16x2_of_float_ints(residue_of(L[2 * u], T, i0 + p), residue_of(L[2 * u + 1], T, i0 + p));
-    }
-    __syncthreads();
-    if (gj < N && gk < ldp)
-      for (int p = 0; p < cnt; ++p)
-        *reinterpret_cast<uint4*>(planes + (int64_t)(i0 + p) * plane_stride + gj * ldp + gk) =
-            make_uint4(st[p][wj][4 * q], st[p][wj][4 * q + 1], st[p][wj][4 * q + 2], st[p][wj][4 * q + 3]);
-    __syncthreads();
-  }
+  for (int u = 0; u < 8; ++u) v[u] = k0 + u < K ? B[(k0 + u) * ldb + col] : 0.0;
+  float2 P[4][kLimbs];
+  limb_pairs(v, e, bits, P);
+  store_residues8(P, T, out + k0, plane_stride);
 }
+
+// Column blocks of the transposed split: 64 rows of B (k) x 32 columns (j)
+// per 256-thread CTA; thread t owns column j0 + t / 8 and rows
+// k0 + 8 (t % 8) .. + 7, so the 8 threads of one column write one contiguous
+// 128-byte run of each plane row and a warp's loads cover 4 columns of 8 rows.
+constexpr int kColBlockK = 64, kColBlockJ = 32;
 
 constexpr int kCrtCols = 4;  // consecutive columns per thread (one 8-byte load per residue plane)
 
