@@ -1,7 +1,6 @@
-// Chinese-remainder reconstruction of the modular Ozaki scheme (used through
-// crt_cols, residue.cuh, by the CRT kernels of ozaki2.cu and grouped.cu).
-// Everything up to the final addition into C is integer and FP32 work: the
-// FP64 pipe, slow on this GPU, sees one add per element.
+// Chinese-remainder reconstruction of the modular Ozaki scheme, shared by
+// the standalone CRT kernel (ozaki2.cu) and the residue GEMM's fused
+// epilogue (tc_gemm.cuh).
 #pragma once
 
 #include <cstdint>
@@ -18,58 +17,27 @@ struct CrtTable {
   uint32_t Mhalf[4];              // floor(M / 2)
   int qlimb;                      // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
   float Minv;                     // 1 / (M >> 32 qlimb) rounded to float
-  float Minv32;                   // Minv * 2^32
   int fast;                       // 1: every result y has |y| / M <= 1/2 - 1/32 (crt_round's one-step path)
                                   //    for this table's K (grouped problems carry their own flag)
 };
 
-// A reconstructed element rounded once to 53 bits: (-1)^neg mant 2^exp2 with
-// mant = 0 (a zero result) or 2^52 <= mant < 2^53.
-struct CrtRounded {
-  uint64_t mant;
-  int exp2;
-  bool neg;
-};
-
-// Round-to-nearest-even of the 128-bit magnitude hi:lo to 53 bits, in
-// integer arithmetic: the top 64 bits (normalised, with a sticky bit for the
-// bits below them) lose their low 11 bits, a tie going to the even mantissa.
-__device__ __forceinline__ CrtRounded round53(uint64_t hi, uint64_t lo, bool neg) {
-  CrtRounded r{0, 0, neg};
-  uint64_t top;
-  int base;  // hi:lo = top * 2^base, up to the sticky bit
-  if (hi == 0) {
-    if (lo == 0) return r;
-    const int lz = __clzll(static_cast<long long>(lo));
-    top = lo << lz;
-    base = -lz;
-  } else {
-    const int lz = __clzll(static_cast<long long>(hi));
-    top = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
-    const uint64_t rest = lz ? (lo << lz) : lo;
-    top |= rest != 0 ? 1ull : 0ull;
-    base = 64 - lz;
-  }
-  uint64_t mant = top >> 11;
-  const uint32_t rb = static_cast<uint32_t>(top & 0x7FFu);
-  mant += (rb > 0x400u || (rb == 0x400u && (mant & 1u))) ? 1u : 0u;
-  int e = base + 11;
-  if (mant >> 53) {  // rounded up to 2^53
-    mant >>= 1;
-    ++e;
-  }
-  r.mant = mant;
-  r.exp2 = e;
-  return r;
+// c + v * 2^x for a double v and an int x, one rounding (the scaling is exact
+// unless the result leaves the normal range).
+__device__ __forceinline__ double crt_add_scaled(double c, double v, int x) {
+  const uint64_t bits = static_cast<uint64_t>(__double_as_longlong(v));
+  const int E = static_cast<int>((bits >> 52) & 0x7FF) + x;
+  if (E >= 1 && E <= 2046)
+    return c + __longlong_as_double(static_cast<long long>((bits & ~(0x7FFull << 52)) | (static_cast<uint64_t>(E) << 52)));
+  return c + ldexp(v, x);
 }
 
 // The symmetric representative of acc mod M (acc = sum r_i W_i < 2^13 M, as
-// five 32-bit limbs) rounded once to 53 bits.
-__device__ __forceinline__ CrtRounded crt_round(uint32_t (&l)[5], const CrtTable& T, int fast) {
+// five 32-bit limbs) rounded once to double: returns v and sets shift so that
+// the result is v * 2^shift (v an integer-valued double, 0 for a zero result).
+__device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T, int fast, int& shift) {
   // acc / M estimated in single precision from the 64 bits at limb qlimb
-  // (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20), as
-  // fl(hi) Minv 2^32 + fl(lo) Minv: absolute error below
-  // 2^13 (2^-20 + 4 2^-24) < 0.01.
+  // (acc >> 32 qlimb < 2^64, M >> 32 qlimb >= 2^20): absolute error below
+  // 2^13 (2^-20 + 3 2^-24) < 0.01.
   // (Limbs chosen with constant indices: an array indexed by a runtime value
   // would live in local memory.)
   uint32_t tlo = l[0], thi = l[1];
@@ -85,7 +53,7 @@ __device__ __forceinline__ CrtRounded crt_round(uint32_t (&l)[5], const CrtTable
     tlo = l[3];
     thi = l[4];
   }
-  const float est = fmaf(__uint2float_rn(thi), T.Minv32, __uint2float_rn(tlo) * T.Minv);
+  const float est = static_cast<float>((static_cast<uint64_t>(thi) << 32) | tlo) * T.Minv;
   uint32_t x[4];  // magnitude of the result
   bool neg;
   if (fast) {
@@ -178,13 +146,29 @@ __device__ __forceinline__ CrtRounded crt_round(uint32_t (&l)[5], const CrtTable
       }
     }
   }
-  return round53((static_cast<uint64_t>(x[3]) << 32) | x[2], (static_cast<uint64_t>(x[1]) << 32) | x[0], neg);
+  const uint64_t hi = (static_cast<uint64_t>(x[3]) << 32) | x[2];
+  const uint64_t lo = (static_cast<uint64_t>(x[1]) << 32) | x[0];
+  double v;
+  if (hi == 0) {
+    v = __ull2double_rn(lo);
+    shift = 0;
+  } else {
+    // round the 128-bit magnitude to 53 bits once: its top 64 bits plus a
+    // sticky bit for everything below them, converted with round-to-nearest
+    const int lz = __clzll(static_cast<long long>(hi));
+    const uint64_t topbits = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    const uint64_t rest = lz ? (lo << lz) : lo;
+    v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
+    shift = 64 - lz;
+  }
+  return neg ? -v : v;
 }
 
 // The CRT of one element from its residues r[i] mod m_i: acc = sum r_i W_i,
 // rounded as crt_round (fast: the one-step path, allowed when the product's
 // grid leaves the margin CrtTable::fast states).
-__device__ __forceinline__ CrtRounded crt_value(const uint32_t (&rr)[kCrtMaxModuli], const CrtTable& T, int fast) {
+__device__ __forceinline__ double crt_value(const uint32_t (&rr)[kCrtMaxModuli], const CrtTable& T, int fast,
+                                            int& shift) {
   // 32-bit limbs accumulated in 64 bits (no overflow: 15 x 2^9 x 2^32 < 2^45)
   uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
@@ -207,28 +191,13 @@ __device__ __forceinline__ CrtRounded crt_value(const uint32_t (&rr)[kCrtMaxModu
   t = (t >> 32) + a3;
   l[3] = static_cast<uint32_t>(t);
   l[4] = static_cast<uint32_t>(t >> 32);
-  return crt_round(l, T, fast);
+  return crt_round(l, T, fast, shift);
 }
 
-// *c += v * 2^e for the rounded element v (c + 0.0 for a zero result, as an
-// exact product would give). The scaled value is built from its bits when its
-// exponent is in the normal range (exact scaling), else through ldexp.
-__device__ __forceinline__ void crt_apply(double* c, const CrtRounded& v, int e) {
-  if (v.mant == 0) {
-    *c = *c + 0.0;
-    return;
-  }
-  const int E = 1023 + 52 + v.exp2 + e;  // biased exponent of mant 2^(exp2 + e)
-  const uint64_t sign = v.neg ? (1ull << 63) : 0ull;
-  double d;
-  if (E >= 1 && E <= 2046) {
-    d = __longlong_as_double(static_cast<long long>(sign | (static_cast<uint64_t>(E) << 52) | (v.mant - (1ull << 52))));
-  } else {
-    const double m = __longlong_as_double(
-        static_cast<long long>(sign | (static_cast<uint64_t>(1023 + 52) << 52) | (v.mant - (1ull << 52))));
-    d = ldexp(m, v.exp2 + e);
-  }
-  *c = *c + d;
+// *c += v * 2^(shift + e): the CRT result of one element applied to C
+// (c + 0.0 for a zero result, as an exact product would give).
+__device__ __forceinline__ void crt_apply(double* c, double v, int shift_plus_e) {
+  *c = v == 0.0 ? *c + 0.0 : crt_add_scaled(*c, v, shift_plus_e);
 }
 
 }  // namespace phpc

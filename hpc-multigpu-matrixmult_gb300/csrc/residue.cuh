@@ -99,7 +99,6 @@ inline ModTable make_table(int nmod, int k) {
   // 64-bit window of acc at limb qlimb cannot overflow
   T.crt.qlimb = std::max(0, (bitlen - 51 + 31) / 32);
   T.crt.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.crt.qlimb))));
-  T.crt.Minv32 = std::ldexp(T.crt.Minv, 32);
   T.crt.n = T.n;
   T.crt.bits = T.bits;
   T.crt.fast = mod_crt_fast(nmod, k, T.bits);
@@ -227,7 +226,9 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
     uint32_t r[kCrtMaxModuli];
 #pragma unroll
     for (int i = 0; i < kCrtMaxModuli; ++i) r[i] = ((c < 2 ? rw[i].x : rw[i].y) >> (16 * (c & 1))) & 0xFFFFu;
-    crt_apply(cp + c, crt_value(r, T, fast), e_row_2b + max(ebp[c], -20000));
+    int shift;
+    const double v = crt_value(r, T, fast, shift);
+    crt_apply(cp + c, v, shift + e_row_2b + max(ebp[c], -20000));
   }
 }
 
