@@ -244,14 +244,27 @@ int panel_rows(int m, int k, int n, int sms) {
   return static_cast<int>(std::min<int64_t>(pr, m));
 }
 
+// Column panels of B in the pipelined modular path: four when a block of the
+// first row panel x a quarter of the columns still fills every SM with output
+// tiles, else one. (Narrower panels copy slower: the host-to-device copy of
+// B's 2048-column panels at N = 16384, 16 KB pieces of each row, ran at about
+// 100 GB/s, 4096-column panels at 175 GB/s, whole rows at 211 GB/s.)
+int b_panels(int rows, int n, int bn, int cl, int sms) {
+  const int64_t tiles = (int64_t)ceil_div(rows, 128 * cl) * ceil_div(ceil_div(n, 4), bn);
+  return tiles >= sms / cl ? 4 : 1;
+}
+
 // phpc_gemm_cublas on the modular scheme, pipelined over row panels of A and
-// C: B travels and is split on stream sB while A's panels travel and are
-// split on sA and C's panels travel on sC; panel p's residue GEMMs and CRT
-// run on sG as soon as B and A_p (C_p for the CRT) are ready, and C_p returns
-// on sO while later panels compute. Only B's copy and split, the first
-// panel's GEMM and the last panel's copy-out are not overlapped. Inputs with
-// inf/NaN are detected after the scans, before any of C is copied back, and
-// the call is redone in IEEE FP64 (DMMA) from the original C.
+// C and, for the first row panel, column panels of B: B's column panels
+// travel on stream sB and are split on sS as each arrives, A's row panels
+// travel and are split on sA and C's on sC; the first row panel's residue
+// GEMMs run block by block on sG as soon as A_0 and the block's B panel are
+// ready, later panels' GEMMs once all of B is, each panel's CRT once its
+// GEMMs and C_p are done, and C_p returns on sO while later panels compute.
+// Only the first blocks' copies and splits and the last panel's copy-out are
+// not overlapped. Inputs with inf/NaN are detected after the scans, before
+// any of C is copied back, and the call is redone in IEEE FP64 (DMMA) from
+// the original C.
 int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k, int n,
                       int nmod, float* seconds) {
   const DeviceInfo* dev = current_device();
@@ -266,11 +279,14 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
   const int pr = panel_rows(m, k, n, dev->sm_count);
   const int np = ceil_div(m, pr);
   const int bn = default_bn(m, k, n);
+  const int nbp = np > 1 ? b_panels(pr, n, bn, default_cluster(m, k, n), dev->sm_count) : 1;
+  const int bcols = nbp == 1 ? n : ceil_div(ceil_div(n, nbp), bn) * bn;
+  const int nbpanels = ceil_div(n, bcols);
   const size_t ws_bytes = ozaki2_workspace_bytes(m, k, n, nmod);
   int rc = PHPC_OK;
   {
     CallResources r;
-    cudaStream_t sx[2] = {nullptr, nullptr};  // sC (C panels in), sO (C panels out)
+    cudaStream_t sx[3] = {nullptr, nullptr, nullptr};  // sC (C panels in), sO (C panels out), sS (B splits)
     std::vector<cudaEvent_t> evs;
     auto new_event = [&](cudaEvent_t& e) {
       if (rc == PHPC_OK && cudaEventCreate(&e) != cudaSuccess) rc = PHPC_ERR_CUDA;
@@ -281,16 +297,20 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
     for (auto& x : sx)
       if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
-    cudaStream_t sB = r.st[0], sA = r.st[1], sG = r.st[2], sC = sx[0], sO = sx[1];
-    cudaEvent_t ev_alloc{}, ev_bcopy{}, ev_b0{}, ev_b1{}, ev_g0{}, ev_g1{};
+    cudaStream_t sB = r.st[0], sA = r.st[1], sG = r.st[2], sC = sx[0], sO = sx[1], sS = sx[2];
+    cudaEvent_t ev_alloc{}, ev_bcopy{}, ev_b1{}, ev_g0{}, ev_g1{}, ev_crt0{};
     std::vector<cudaEvent_t> ev_a0(np), ev_a1(np), ev_c(np), ev_g(np);
-    for (cudaEvent_t* e : {&ev_alloc, &ev_bcopy, &ev_b0, &ev_b1, &ev_g0, &ev_g1}) new_event(*e);
+    // per B column panel: copied; split started, done; first row panel's block GEMM started, done
+    std::vector<cudaEvent_t> ev_bc(nbpanels), ev_bs0(nbpanels), ev_bs1(nbpanels), ev_gb0(nbpanels), ev_gb1(nbpanels);
+    for (cudaEvent_t* e : {&ev_alloc, &ev_bcopy, &ev_b1, &ev_g0, &ev_g1, &ev_crt0}) new_event(*e);
     for (int p = 0; p < np; ++p) {
       new_event(ev_a0[p]);
       new_event(ev_a1[p]);
       new_event(ev_c[p]);
       new_event(ev_g[p]);
     }
+    for (int j = 0; j < nbpanels; ++j)
+      for (auto* v : {&ev_bc, &ev_bs0, &ev_bs1, &ev_gb0, &ev_gb1}) new_event((*v)[j]);
     if (rc == PHPC_OK &&
         (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, pool, sB) !=
              cudaSuccess ||
@@ -303,42 +323,69 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
     if (rc == PHPC_OK) {
       cudaMemsetAsync(status, 0, sizeof(int), sB);
       cudaEventRecord(ev_alloc, sB);
-      for (cudaStream_t st : {sA, sG, sC, sO}) cudaStreamWaitEvent(st, ev_alloc, 0);
-      // B: copy, then exponent scan and residue split
-      if (cudaMemcpy2DAsync(r.dB, dldb * 8, b, (size_t)ldb * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, sB) !=
-          cudaSuccess)
-        rc = PHPC_ERR_CUDA;
+      for (cudaStream_t st : {sA, sG, sC, sO, sS}) cudaStreamWaitEvent(st, ev_alloc, 0);
+      // A's row panel p: copy, exponent scan and residue split on sA
+      auto issue_a = [&](int p) {
+        const int r0 = p * pr, rows = std::min(pr, m - r0);
+        if (cudaMemcpy2DAsync(r.dA + (int64_t)r0 * dlda, dlda * 8, a + (int64_t)r0 * lda, (size_t)lda * 8,
+                              (size_t)k * 8, rows, cudaMemcpyHostToDevice, sA) != cudaSuccess) {
+          rc = PHPC_ERR_CUDA;
+          return;
+        }
+        cudaEventRecord(ev_a0[p], sA);
+        rc = ozaki2_prepare_a_rows(m, r0, rows, k, n, r.dA, dlda, nmod, r.ws, ws_bytes, sA);
+        cudaEventRecord(ev_a1[p], sA);
+      };
+      // The host-to-device copies run in the order they are issued: A's first
+      // panel, then B's column panels (each split on sS as it arrives), so
+      // that the first block GEMM waits for A_0 and B_0 only; then C's and
+      // A's remaining panels.
+      issue_a(0);
+      for (int j = 0; j < nbpanels && rc == PHPC_OK; ++j) {
+        const int c0 = j * bcols, cols = std::min(bcols, n - c0);
+        if (cudaMemcpy2DAsync(r.dB + c0, dldb * 8, b + c0, (size_t)ldb * 8, (size_t)cols * 8, k,
+                              cudaMemcpyHostToDevice, sB) != cudaSuccess) {
+          rc = PHPC_ERR_CUDA;
+          break;
+        }
+        cudaEventRecord(ev_bc[j], sB);
+        cudaStreamWaitEvent(sS, ev_bc[j], 0);
+        cudaEventRecord(ev_bs0[j], sS);
+        rc = ozaki2_prepare_b_cols(m, k, n, c0, cols, r.dB, dldb, nmod, r.ws, ws_bytes, sS);
+        cudaEventRecord(ev_bs1[j], sS);
+      }
       cudaEventRecord(ev_bcopy, sB);
-      cudaEventRecord(ev_b0, sB);
-      if (rc == PHPC_OK) rc = ozaki2_prepare_b(m, k, n, r.dB, dldb, nmod, r.ws, ws_bytes, sB);
-      cudaEventRecord(ev_b1, sB);
-      // A panels: copy, scan and split; C panels: copy (after B's copy)
+      cudaEventRecord(ev_b1, sS);
       cudaStreamWaitEvent(sC, ev_bcopy, 0);
+      cudaStreamWaitEvent(sA, ev_bcopy, 0);
       for (int p = 0; p < np && rc == PHPC_OK; ++p) {
         const int r0 = p * pr, rows = std::min(pr, m - r0);
-        // B's copy gates the first GEMM: only A's first panel shares the
-        // host link with it, the later panels follow it
-        if (p == 1) cudaStreamWaitEvent(sA, ev_bcopy, 0);
-        if (cudaMemcpy2DAsync(r.dA + (int64_t)r0 * dlda, dlda * 8, a + (int64_t)r0 * lda, (size_t)lda * 8,
-                              (size_t)k * 8, rows, cudaMemcpyHostToDevice, sA) != cudaSuccess ||
-            cudaMemcpy2DAsync(r.dC + (int64_t)r0 * dldc, dldc * 8, c + (int64_t)r0 * ldc, (size_t)ldc * 8,
+        if (cudaMemcpy2DAsync(r.dC + (int64_t)r0 * dldc, dldc * 8, c + (int64_t)r0 * ldc, (size_t)ldc * 8,
                               (size_t)n * 8, rows, cudaMemcpyHostToDevice, sC) != cudaSuccess) {
           rc = PHPC_ERR_CUDA;
           break;
         }
         cudaEventRecord(ev_c[p], sC);
-        cudaEventRecord(ev_a0[p], sA);
-        rc = ozaki2_prepare_a_rows(m, r0, rows, k, n, r.dA, dlda, nmod, r.ws, ws_bytes, sA);
-        cudaEventRecord(ev_a1[p], sA);
+        if (p > 0) issue_a(p);
       }
-      // residue GEMMs and CRT per panel
-      cudaStreamWaitEvent(sG, ev_b1, 0);
+      // residue GEMMs and CRT per panel (the first panel's GEMMs per B column panel)
       for (int p = 0; p < np && rc == PHPC_OK; ++p) {
         const int r0 = p * pr, rows = std::min(pr, m - r0);
         cudaStreamWaitEvent(sG, ev_a1[p], 0);
-        if (p == 0) cudaEventRecord(ev_g0, sG);
-        rc = ozaki2_multiply_rows(m, r0, rows, k, n, nmod, r.ws, ws_bytes, sG, bn);
+        if (p == 0) {
+          cudaEventRecord(ev_g0, sG);
+          for (int j = 0; j < nbpanels && rc == PHPC_OK; ++j) {
+            const int c0 = j * bcols, cols = std::min(bcols, n - c0);
+            cudaStreamWaitEvent(sG, ev_bs1[j], 0);
+            cudaEventRecord(ev_gb0[j], sG);
+            rc = ozaki2_multiply_block(m, r0, rows, c0, cols, k, n, nmod, r.ws, ws_bytes, sG, bn);
+            cudaEventRecord(ev_gb1[j], sG);
+          }
+        } else {
+          rc = ozaki2_multiply_rows(m, r0, rows, k, n, nmod, r.ws, ws_bytes, sG, bn);
+        }
         cudaStreamWaitEvent(sG, ev_c[p], 0);
+        if (p == 0) cudaEventRecord(ev_crt0, sG);
         if (rc == PHPC_OK) rc = ozaki2_reconstruct_rows(m, r0, rows, k, n, r.dC, dldc, nmod, r.ws, ws_bytes, sG);
         cudaEventRecord(ev_g[p], sG);
       }
@@ -366,13 +413,18 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
     cudaEvent_t ev_out{};
     new_event(ev_out);
     if (rc == PHPC_OK) cudaEventRecord(ev_out, sO);
-    for (cudaStream_t st : {sB, sA, sC, sG, sO})
+    for (cudaStream_t st : {sB, sA, sC, sG, sO, sS})
       if (cudaStreamSynchronize(st) != cudaSuccess && rc == PHPC_OK) rc = PHPC_ERR_CUDA;
     if (rc == PHPC_OK && getenv("PHPC_VERBOSE")) {
-      // timeline of the call (ms after the allocations): B copied / split,
-      // per panel A split, C copied, GEMM + CRT done, and the last copy-out
-      fprintf(stderr, "phpc: modular pipeline %d panels of %d rows: B copied %.2f split %.2f |", np, pr,
-              elapsed_ms(ev_alloc, ev_bcopy), elapsed_ms(ev_alloc, ev_b1));
+      // timeline of the call (ms after the allocations): B's panels copied /
+      // split, the first row panel's block GEMMs, per panel A split, C
+      // copied, GEMM + CRT done, and the last copy-out
+      fprintf(stderr, "phpc: modular pipeline %d row panels of %d rows, %d B panels of %d columns:", np, pr, nbpanels,
+              bcols);
+      for (int j = 0; j < nbpanels; ++j)
+        fprintf(stderr, " b%d copied %.2f split %.2f gemm %.2f-%.2f", j, elapsed_ms(ev_alloc, ev_bc[j]),
+                elapsed_ms(ev_alloc, ev_bs1[j]), elapsed_ms(ev_alloc, ev_gb0[j]), elapsed_ms(ev_alloc, ev_gb1[j]));
+      fprintf(stderr, " |");
       for (int p = 0; p < np; ++p)
         fprintf(stderr, " p%d A %.2f C %.2f G %.2f", p, elapsed_ms(ev_alloc, ev_a1[p]), elapsed_ms(ev_alloc, ev_c[p]),
                 elapsed_ms(ev_alloc, ev_g[p]));
@@ -382,11 +434,14 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       rc = PHPC_ERR_CUDA;
     float kernel_ms = 0.f;
     if (rc == PHPC_OK) {
-      // device compute time: A's first panel split (it runs during B's copy),
-      // then B's split through the last panel's CRT, a span in which the
-      // kernels follow one another without gaps (later A splits run between
-      // the panel GEMMs); spans that only wait for the SMs are not added
-      kernel_ms = elapsed_ms(ev_a0[0], ev_a1[0]) + elapsed_ms(ev_b0, ev_g1);
+      // device compute time: A's first panel split and B's panel splits (they
+      // run while B travels), the first row panel's block GEMMs, then its CRT
+      // through the last panel's CRT, a span in which the kernels follow one
+      // another without gaps (later A splits run between the panel GEMMs);
+      // spans that only wait for copies are not added
+      kernel_ms = elapsed_ms(ev_a0[0], ev_a1[0]) + elapsed_ms(ev_crt0, ev_g1);
+      for (int j = 0; j < nbpanels; ++j)
+        kernel_ms += elapsed_ms(ev_bs0[j], ev_bs1[j]) + elapsed_ms(ev_gb0[j], ev_gb1[j]);
     }
     if (rc == PHPC_OK && nonfinite) {
       // inf/NaN cannot be carried by integers: redo the call in IEEE FP64

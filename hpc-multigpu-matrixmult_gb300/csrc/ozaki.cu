@@ -107,7 +107,8 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   const uint64_t sA[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * a_plane_rows};
   const uint32_t bA[3] = {kTcBK, kTcBM, 1};
   const uint64_t dB[3] = {(uint64_t)k, (uint64_t)n, (uint64_t)nplanesB};
-  const uint64_t sB[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * n};
+  const int64_t b_plane_rows = opt.b_plane_rows > 0 ? opt.b_plane_rows : n;
+  const uint64_t sB[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * b_plane_rows};
   const int cm = opt.cfg_m > 0 ? opt.cfg_m : m, cn = opt.cfg_n > 0 ? opt.cfg_n : n,
             ck = opt.cfg_k > 0 ? opt.cfg_k : k;
   const int cluster = default_cluster(cm, ck, cn);

@@ -138,21 +138,31 @@ int ozaki2_prepare_a_rows(int m, int r0, int rows, int k, int n, const double* d
   return PHPC_OK;
 }
 
-// B (k x n): exponent scan and residue split.
-int ozaki2_prepare_b(int m, int k, int n, const double* dB, int64_t ldb, int nmod, void* ws, size_t ws_bytes,
-                     cudaStream_t stream) {
+// Columns [c0, c0 + cols) of B (k x n, dB its column 0): exponent scan and
+// residue split into the planes of the full problem.
+int ozaki2_prepare_b_cols(int m, int k, int n, int c0, int cols, const double* dB, int64_t ldb, int nmod, void* ws,
+                          size_t ws_bytes, cudaStream_t stream) {
   Ozaki2Layout L;
   Ozaki2Views V;
   const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
   if (rc != PHPC_OK) return rc;
+  if (c0 < 0 || cols <= 0 || c0 + cols > n) return PHPC_ERR_ARG;
   const ModTable T = make_table(nmod, k);
-  fill_int_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(V.eb, n, kExpZero);
-  scan_cols_kernel<<<dim3(ceil_div(n, 256), ceil_div(k, 256)), 256, 0, stream>>>(dB, ldb, k, n, 256, V.eb,
-                                                                                  device_status_ptr());
-  residue_cols_kernel<<<dim3(ceil_div(n, kColBlockJ), ceil_div(L.ldp, kColBlockK)), 256, 0, stream>>>(
-      dB, ldb, k, n, V.eb, T, V.pb, L.ldp, (int64_t)n * L.ldp);
+  const double* b = dB + c0;
+  int* eb = V.eb + c0;
+  fill_int_kernel<<<ceil_div(cols, 256), 256, 0, stream>>>(eb, cols, kExpZero);
+  scan_cols_kernel<<<dim3(ceil_div(cols, 256), ceil_div(k, 256)), 256, 0, stream>>>(b, ldb, k, cols, 256, eb,
+                                                                                     device_status_ptr());
+  residue_cols_kernel<<<dim3(ceil_div(cols, kColBlockJ), ceil_div(L.ldp, kColBlockK)), 256, 0, stream>>>(
+      b, ldb, k, cols, eb, T, V.pb + (int64_t)c0 * L.ldp, L.ldp, (int64_t)n * L.ldp);
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
+}
+
+// B (k x n): exponent scan and residue split.
+int ozaki2_prepare_b(int m, int k, int n, const double* dB, int64_t ldb, int nmod, void* ws, size_t ws_bytes,
+                     cudaStream_t stream) {
+  return ozaki2_prepare_b_cols(m, k, n, 0, n, dB, ldb, nmod, ws, ws_bytes, stream);
 }
 
 // Exponent scans and residue splits: A's on stream_a, B's on stream_b.
@@ -163,16 +173,16 @@ int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const do
   return rc;
 }
 
-// The residue GEMMs of rows [r0, r0 + rows): plane i of R = (A_i * B_i^T) mod
-// m_i, one 16-bit residue per element. Tile width, cluster and raster are those of the
-// full m x k x n problem.
-int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const void* ws, size_t ws_bytes,
-                         cudaStream_t stream, int bn) {
+// The residue GEMMs of the block rows [r0, r0 + rows) x columns [c0, c0 +
+// cols): plane i of R = (A_i * B_i^T) mod m_i, one 16-bit residue per element.
+// Tile width, cluster and raster are those of the full m x k x n problem.
+int ozaki2_multiply_block(int m, int r0, int rows, int c0, int cols, int k, int n, int nmod, const void* ws,
+                          size_t ws_bytes, cudaStream_t stream, int bn) {
   Ozaki2Layout L;
   Ozaki2Views V;
   const int rc = ozaki2_views(m, k, n, nmod, ws, ws_bytes, L, V);
   if (rc != PHPC_OK) return rc;
-  if (r0 < 0 || rows <= 0 || r0 + rows > m) return PHPC_ERR_ARG;
+  if (r0 < 0 || rows <= 0 || r0 + rows > m || c0 < 0 || cols <= 0 || c0 + cols > n || c0 % 8) return PHPC_ERR_ARG;
   const ModTable T = make_table(nmod, k);
   PairList pl{};
   pl.n = nmod;
@@ -185,16 +195,24 @@ int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const 
   }
   const int64_t rplane = (int64_t)m * L.ldr;
   const uint16_t* pa = V.pa + (int64_t)r0 * L.ldp;
-  uint16_t* R = V.R + (int64_t)r0 * L.ldr;
+  const uint16_t* pb = V.pb + (int64_t)c0 * L.ldp;
+  uint16_t* R = V.R + (int64_t)r0 * L.ldr + c0;
   TcGemmOpts opt;
   opt.a_plane_rows = m;
+  opt.b_plane_rows = n;
   opt.cfg_m = m;
   opt.cfg_n = n;
   opt.cfg_k = k;
-  return bn == 128 ? launch_tc_slice_gemm<128, kResidue>(pa, V.pb, nmod, nmod, L.ldp, rows, n, k, pl, nullptr, 0,
+  return bn == 128 ? launch_tc_slice_gemm<128, kResidue>(pa, pb, nmod, nmod, L.ldp, rows, cols, k, pl, nullptr, 0,
                                                           nullptr, nullptr, stream, R, L.ldr, rplane, opt)
-                   : launch_tc_slice_gemm<256, kResidue>(pa, V.pb, nmod, nmod, L.ldp, rows, n, k, pl, nullptr, 0,
+                   : launch_tc_slice_gemm<256, kResidue>(pa, pb, nmod, nmod, L.ldp, rows, cols, k, pl, nullptr, 0,
                                                           nullptr, nullptr, stream, R, L.ldr, rplane, opt);
+}
+
+// The residue GEMMs of rows [r0, r0 + rows), all columns.
+int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const void* ws, size_t ws_bytes,
+                         cudaStream_t stream, int bn) {
+  return ozaki2_multiply_block(m, r0, rows, 0, n, k, n, nmod, ws, ws_bytes, stream, bn);
 }
 
 int ozaki2_multiply(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {

@@ -65,6 +65,13 @@ int ozaki2_prepare_b(int m, int k, int n, const double* dB, int64_t ldb, int nmo
                      cudaStream_t stream);
 int ozaki2_multiply_rows(int m, int r0, int rows, int k, int n, int nmod, const void* ws, size_t ws_bytes,
                          cudaStream_t stream, int bn);
+// Column-panel pieces (dB: column 0 of the full k x n operand): B's scan and
+// split of columns [c0, c0 + cols), and the residue GEMMs of the block of rows
+// [r0, r0 + rows) x columns [c0, c0 + cols).
+int ozaki2_prepare_b_cols(int m, int k, int n, int c0, int cols, const double* dB, int64_t ldb, int nmod, void* ws,
+                          size_t ws_bytes, cudaStream_t stream);
+int ozaki2_multiply_block(int m, int r0, int rows, int c0, int cols, int k, int n, int nmod, const void* ws,
+                          size_t ws_bytes, cudaStream_t stream, int bn);
 int ozaki2_reconstruct_rows(int m, int r0, int rows, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws,
                             size_t ws_bytes, cudaStream_t stream);
 int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,

@@ -601,6 +601,7 @@ inline bool tc_regs_ok(const void* kernel) {
 // Options of the host launcher below.
 struct TcGemmOpts {
   int64_t a_plane_rows = 0;            // rows between consecutive A planes (0: m, the planes are m rows high)
+  int64_t b_plane_rows = 0;            // rows between consecutive B planes (0: n)
   int cfg_m = 0, cfg_n = 0, cfg_k = 0;  // shape whose tuning entry sets cluster and raster (0: this GEMM's)
 };
 

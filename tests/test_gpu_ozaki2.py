@@ -131,10 +131,12 @@ def test_host_entry_uses_modular_scheme(phpc, monkeypatch):
 
 
 
-@pytest.mark.parametrize("m,k,n", [(2500, 300, 200), (4096, 64, 256)])
+@pytest.mark.parametrize("m,k,n", [(2500, 300, 200), (4096, 64, 256), (5000, 48, 8200), (10000, 32, 16400)])
 def test_host_pipeline_panels_equal_device_call(phpc, torch_cuda, monkeypatch, m, k, n):
     """phpc_gemm_cublas runs the modular scheme over row panels of A and C
-    (ragged last panel here); the result equals the one-call device path."""
+    (ragged last panel here) and, for the two larger shapes, the first row
+    panel's GEMMs over four column panels of B (ragged last one); the result
+    equals the one-call device path."""
     monkeypatch.setenv("PHPC_MODULI", "15")
     rng = np.random.default_rng(m + k + n)
     a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
