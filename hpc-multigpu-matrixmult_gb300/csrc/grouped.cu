@@ -41,6 +41,7 @@ struct GSplitProb {
   int m, k, n;
   int row_start, col_start, sblock_start;  // prefix sums over the problems
   int rblock_start;                        // modular scheme: residue column blocks
+  int piece_start;                         // row pieces (8 consecutive k of one row of A)
   int cunit_start, crt_unit_start;         // prefix sums: column-scan units, CRT units
   int nblk_j;                              // 64-column blocks of B
   int64_t lda, ldb, ldp;
@@ -102,14 +103,28 @@ __global__ void g_scan_cols_kernel(const GSplitProb* __restrict__ P, int count, 
   if (nf) record_error(status, PHPC_ERR_NONFINITE);
 }
 
-__global__ void g_split_rows_kernel(const GSplitProb* __restrict__ P, int count, int total_rows, int s) {
-  const int r = blockIdx.x;
-  if (r >= total_rows) return;
-  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
-  const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
-  if (k0 >= p.ldp) return;
-  const int64_t row = r - p.row_start;
-  split_row_piece(p.A + row * p.lda, p.k, p.ea[row], s, p.pa + row * p.ldp, (int64_t)p.m * p.ldp, k0);
+// Row splits: one thread per row piece (8 consecutive k of one row of A),
+// pieces numbered row by row across the problems, so that every thread of
+// the launch has work whatever each problem's K.
+struct RowPiece {
+  const GSplitProb* p;
+  int64_t row, k0;
+};
+
+__device__ __forceinline__ RowPiece row_piece(const GSplitProb* __restrict__ P, int count, int t) {
+  const GSplitProb& p = P[locate(P, count, t, [](const GSplitProb& q) { return q.piece_start; })];
+  const int per_row = static_cast<int>(p.ldp >> 3);
+  const int local = t - p.piece_start;
+  return RowPiece{&p, local / per_row, static_cast<int64_t>(local % per_row) * 8};
+}
+
+__global__ void __launch_bounds__(256) g_split_rows_kernel(const GSplitProb* __restrict__ P, int count,
+                                                           int total_pieces, int s) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total_pieces) return;
+  const RowPiece rp = row_piece(P, count, t);
+  const GSplitProb& p = *rp.p;
+  split_row_piece(p.A + rp.row * p.lda, p.k, p.ea[rp.row], s, p.pa + rp.row * p.ldp, (int64_t)p.m * p.ldp, rp.k0);
 }
 
 __global__ void __launch_bounds__(256) g_split_cols_kernel(const GSplitProb* __restrict__ P, int count,
@@ -123,19 +138,20 @@ __global__ void __launch_bounds__(256) g_split_cols_kernel(const GSplitProb* __r
   split_col_block(p.B, p.ldb, p.k, p.n, p.eb, s, p.pb, p.ldp, (int64_t)p.n * p.ldp, k0, j0, st);
 }
 
-// Modular scheme: residue planes of one row piece of each row.
-__global__ void g_residue_rows_kernel(const GSplitProb* __restrict__ P, int count, int total_rows,
-                                      const __grid_constant__ ModTable T) {
-  const int r = blockIdx.x;
-  if (r >= total_rows) return;
-  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
-  const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
-  if (k0 >= p.ldp) return;
-  const int64_t row = r - p.row_start;
-  residue_row_piece(p.A + row * p.lda, p.k, p.ea[row], p.bits, T, p.pa + row * p.ldp, (int64_t)p.m * p.ldp, k0);
+// Modular scheme: residue planes of one row piece per thread. (Both residue
+// splits are held to 64 registers, four CTAs per SM: a few bytes of spill,
+// 4 % faster than at 79 registers and three CTAs.)
+__global__ void __launch_bounds__(256, 4) g_residue_rows_kernel(const GSplitProb* __restrict__ P, int count,
+                                                             int total_pieces, const __grid_constant__ ModTable T) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total_pieces) return;
+  const RowPiece rp = row_piece(P, count, t);
+  const GSplitProb& p = *rp.p;
+  residue_row_piece(p.A + rp.row * p.lda, p.k, p.ea[rp.row], p.bits, T, p.pa + rp.row * p.ldp,
+                    (int64_t)p.m * p.ldp, rp.k0);
 }
 
-__global__ void __launch_bounds__(256) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
+__global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
                                                              int total_blocks, const __grid_constant__ ModTable T) {
   const int b = blockIdx.x;
   if (b >= total_blocks) return;  // uniform over the CTA
@@ -239,7 +255,7 @@ PairList residue_pairs(const ModTable& T) {
 struct phpc_grouped_plan {
   int device;
   int count, s, moduli, bn;  // moduli > 0: modular scheme (s unused)
-  int total_rows, total_cols, total_sblocks, total_rblocks, total_tiles, max_kgroups, total_cunits,
+  int total_rows, total_cols, total_sblocks, total_rblocks, total_tiles, total_pieces, total_cunits,
       total_crt_units;
   phpc::GSplitProb* d_split;
   phpc::TcGroupTable table;
@@ -287,13 +303,13 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
     g_scan_cols_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
                                                                             pl->total_cunits, status);
     if (modular) {
-      g_residue_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
-                                                                                       pl->total_rows, pl->mods);
+      g_residue_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                                 pl->total_pieces, pl->mods);
       g_residue_cols_kernel<<<pl->total_rblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rblocks,
                                                                    pl->mods);
     } else {
-      g_split_rows_kernel<<<dim3(pl->total_rows, pl->max_kgroups), 128, 0, stream>>>(pl->d_split, pl->count,
-                                                                                     pl->total_rows, pl->s);
+      g_split_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                               pl->total_pieces, pl->s);
       g_split_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks, pl->s);
     }
     if (cudaGetLastError() != cudaSuccess) return PHPC_ERR_CUDA;
@@ -358,8 +374,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   std::vector<TcGroupProblem> ht(count);
   std::vector<CUtensorMap> hm(2 * (size_t)count);
   size_t off = T.end;
-  int rows = 0, cols = 0, sblocks = 0, rblocks = 0, tiles = 0, maxkg = 1;
-  int64_t cunits = 0, crt_units = 0;
+  int rows = 0, cols = 0, sblocks = 0, rblocks = 0, tiles = 0;
+  int64_t pieces = 0, cunits = 0, crt_units = 0;
   for (int i = 0; i < count && rc == PHPC_OK; ++i) {
     const phpc_gemm_problem& q = problems[i];
     const ProbLayout L = prob_layout(q, planes, modular);
@@ -373,6 +389,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     g.col_start = cols;
     g.sblock_start = sblocks;
     g.rblock_start = rblocks;
+    g.piece_start = static_cast<int>(std::min<int64_t>(pieces, INT32_MAX));
     g.cunit_start = static_cast<int>(cunits);
     g.crt_unit_start = static_cast<int>(crt_units);
     g.nblk_j = ceil_div(q.n, 64);
@@ -397,7 +414,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     cols += q.n;
     sblocks += g.nblk_j * ceil_div(q.k, 32);
     rblocks += ceil_div(q.n, kColBlockJ) * ceil_div((int)L.ldp, kColBlockK);
-    maxkg = std::max(maxkg, ceil_div(L.ldp / 8, 128));
+    pieces += (int64_t)q.m * (L.ldp / 8);
     cunits += (int64_t)q.n * ceil_div(q.k, kScanKChunk);
     if (modular) crt_units += (int64_t)q.m * ceil_div(q.n, kCrtUnitCols);
 
@@ -432,13 +449,13 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
       rc = PHPC_ERR_CUDA;
     off += L.end;
   }
-  if (cunits > INT32_MAX / 2 || crt_units > INT32_MAX / 2) rc = PHPC_ERR_ARG;
+  if (cunits > INT32_MAX / 2 || crt_units > INT32_MAX / 2 || pieces > INT32_MAX / 2) rc = PHPC_ERR_ARG;
   pl->total_rows = rows;
   pl->total_cols = cols;
   pl->total_sblocks = sblocks;
   pl->total_rblocks = rblocks;
   pl->total_tiles = tiles;
-  pl->max_kgroups = maxkg;
+  pl->total_pieces = static_cast<int>(std::min<int64_t>(pieces, INT32_MAX));
   pl->total_cunits = static_cast<int>(cunits);
   pl->total_crt_units = static_cast<int>(crt_units);
   pl->d_split = reinterpret_cast<GSplitProb*>(base + T.split);
