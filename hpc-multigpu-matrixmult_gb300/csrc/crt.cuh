@@ -200,4 +200,9 @@ __device__ __forceinline__ void crt_apply(double* c, double v, int shift_plus_e)
   *c = v == 0.0 ? *c + 0.0 : crt_add_scaled(*c, v, shift_plus_e);
 }
 
+// c + v * 2^(shift + e), the value form of crt_apply.
+__device__ __forceinline__ double crt_added(double c, double v, int shift_plus_e) {
+  return v == 0.0 ? c + 0.0 : crt_add_scaled(c, v, shift_plus_e);
+}
+
 }  // namespace phpc

