@@ -207,15 +207,24 @@ ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
 }
 
 struct TableLayout {
-  size_t split, tprob, maps, end;
+  size_t split, tprob, maps, tiles, end;
 };
 
-TableLayout table_layout(int count) {
+// Output tiles of the batch at the narrowest tile width (an upper bound for
+// the plan's).
+int64_t max_tiles(const phpc_gemm_problem* problems, int count) {
+  int64_t t = 0;
+  for (int i = 0; i < count; ++i) t += (int64_t)ceil_div(problems[i].m, kTcBM) * ceil_div(problems[i].n, 128);
+  return t;
+}
+
+TableLayout table_layout(int count, int64_t tiles) {
   TableLayout T;
   T.split = 0;
   T.tprob = align_up(sizeof(GSplitProb) * (size_t)count, 256);
   T.maps = align_up(T.tprob + sizeof(TcGroupProblem) * (size_t)count, 256);
-  T.end = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
+  T.tiles = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
+  T.end = align_up(T.tiles + sizeof(int2) * (size_t)tiles, 256);
   return T;
 }
 
@@ -245,6 +254,7 @@ PairList residue_pairs(const ModTable& T) {
     pl.a[i] = pl.b[i] = pl.g[i] = static_cast<uint8_t>(i);
     pl.mod[i] = static_cast<uint16_t>(T.m[i]);
     pl.magic[i] = T.magic[i];
+    pl.invm[i] = T.invm[i].x;
   }
   return pl;
 }
@@ -329,7 +339,7 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
 }
 
 size_t grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int planes, bool modular) {
-  size_t total = table_layout(count).end;
+  size_t total = table_layout(count, max_tiles(problems, count)).end;
   for (int i = 0; i < count; ++i) {
     if (!valid_problem(problems[i])) return 0;
     total += prob_layout(problems[i], planes, modular).end;
@@ -368,7 +378,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     pl->pairs = grouped_pairs(planes);
   }
 
-  const TableLayout T = table_layout(count);
+  const TableLayout T = table_layout(count, max_tiles(problems, count));
   uint8_t* base = static_cast<uint8_t*>(workspace);
   std::vector<GSplitProb> hs(count);
   std::vector<TcGroupProblem> ht(count);
@@ -464,6 +474,10 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->table.group_rows = 8;
   pl->table.probs = reinterpret_cast<const TcGroupProblem*>(base + T.tprob);
   pl->table.maps = reinterpret_cast<const CUtensorMap*>(base + T.maps);
+  pl->table.tiles = reinterpret_cast<const int2*>(base + T.tiles);
+  std::vector<int2> htiles(tiles);
+  for (int i = 0; i < count && rc == PHPC_OK; ++i)
+    for (int u = 0; u < ht[i].tm * ht[i].tn; ++u) htiles[ht[i].tile_start + u] = make_int2(i, u);
   if (rc == PHPC_OK) {
     if (modular)
       rc = pl->bn == 128 ? prepare_grouped_gemm<128, kResidue>() : prepare_grouped_gemm<256, kResidue>();
@@ -478,6 +492,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
            cudaSuccess ||
        cudaMemcpyAsync(base + T.maps, hm.data(), sizeof(CUtensorMap) * 2 * count, cudaMemcpyHostToDevice, st) !=
            cudaSuccess ||
+       (tiles > 0 && cudaMemcpyAsync(base + T.tiles, htiles.data(), sizeof(int2) * tiles, cudaMemcpyHostToDevice,
+                                     st) != cudaSuccess) ||
        cudaStreamSynchronize(st) != cudaSuccess))
     rc = PHPC_ERR_CUDA;
   if (rc != PHPC_OK) {

@@ -15,7 +15,10 @@
 //          modulus m_i; its exact int32 sum (f32 chunks of 512 products of
 //          |r| <= 181) is reduced mod m_i and stored as one 16-bit residue per
 //          element in residue plane i of R; the CRT pass (ozaki2.cu) combines
-//          them.
+//          them. A modulus whose K fits one chunk skips the integer
+//          conversion: the exact f32 chunk is reduced in FP32 (two elements
+//          per f32x2 instruction). Residues leave through the warp's scratch
+//          so that each store instruction writes four 128-byte row segments.
 //  kF32    3xBF16 split GEMM: all pairs accumulate into one f32 result. The
 //          tensor cores' f32 accumulation does not round to nearest, so its
 //          error grows with the number of MMAs summed; the accumulator is
@@ -62,6 +65,7 @@ struct PairList {
   uint8_t g[kTcMaxPairs];     // group id (Ozaki: diagonal p + q, 1-based digits); pairs of a group are contiguous
   uint16_t mod[kTcMaxPairs];  // kResidue: modulus of the group
   uint32_t magic[kTcMaxPairs];  // kResidue: floor(2^32 / modulus)
+  float invm[kTcMaxPairs];      // kResidue: 1 / modulus rounded to float
 };
 
 // x mod m for 0 <= x < 2^32, 2 <= m < 2^16, magic = floor(2^32 / m) (Barrett: the
@@ -72,6 +76,21 @@ __device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t m, uint32_t m
   if (r >= m) r -= m;
   return r;
 }
+// Residues in [0, m) of two integer-valued floats |x| < 2^24 (one exact f32
+// chunk), m <= 363: x - m round(x / m) by the 1.5 * 2^23 rounding constant
+// and one exact FMA (|.| <= 0.51 m), moved into [0, m), packed as two 16-bit
+// values read from the mantissas of r + 2^23 (lo in the low half).
+__device__ __forceinline__ uint32_t residue_pair_u16(float x0, float x1, float m, float invm) {
+  const float2 x = make_float2(x0, x1);
+  const float2 q = __fadd2_rn(__ffma2_rn(x, make_float2(invm, invm), make_float2(12582912.0f, 12582912.0f)),
+                              make_float2(-12582912.0f, -12582912.0f));
+  float2 r = __ffma2_rn(q, make_float2(-m, -m), x);
+  r.x = r.x < 0.0f ? r.x + m : r.x;
+  r.y = r.y < 0.0f ? r.y + m : r.y;
+  const float2 b = __fadd2_rn(r, make_float2(8388608.0f, 8388608.0f));
+  return __byte_perm(__float_as_uint(b.x), __float_as_uint(b.y), 0x5410);
+}
+
 // Residue in [0, m) of a signed 32-bit integer.
 __device__ __forceinline__ uint32_t mod_signed(int32_t x, uint32_t m, uint32_t magic) {
   const uint32_t mag = x < 0 ? 0u - static_cast<uint32_t>(x) : static_cast<uint32_t>(x);
@@ -116,6 +135,7 @@ struct TcGroupTable {
   int group_rows;
   const TcGroupProblem* probs;  // [count]
   const CUtensorMap* maps;      // [2 * count], 64-byte aligned
+  const int2* tiles;            // [ntiles]: (problem, tile index within the problem), one load per tile
 };
 
 // What one output tile needs: its problem's sizes, operands and position.
@@ -188,16 +208,13 @@ __device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap
     j.ldr = a.ldr;
     j.rplane = a.rplane;
   } else {
-    int lo = 0, hi = g.count - 1;
-    while (lo < hi) {  // last problem with tile_start <= t
-      const int mid = (lo + hi + 1) >> 1;
-      if (g.probs[mid].tile_start <= t) lo = mid; else hi = mid - 1;
-    }
+    const int2 e = g.tiles[t];
+    const int lo = e.x;
     const TcGroupProblem& p = g.probs[lo];
     j.M = p.M;
     j.N = p.N;
     j.nk = (p.K + kTcBK - 1) / kTcBK;
-    tc_tile_coords(p.tm, p.tn, g.group_rows, t - p.tile_start, j.rm, j.rn);
+    tc_tile_coords(p.tm, p.tn, g.group_rows, e.y, j.rm, j.rn);
     j.tmA = g.maps + 2 * lo;
     j.tmB = g.maps + 2 * lo + 1;
     j.C = p.C;
@@ -449,7 +466,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           if (!ok) break;
           tc_fence_after();
           const uint32_t taddr = tmem_base + ((uint32_t)(quad * 32) << 16) + buf * BN + half * HALF;
-          if (MODE != kF32) {
+          // kResidue with one chunk per modulus: the chunk (an exact f32) is the
+          // whole sum; keep its bits and reduce it in FP32 at the group end
+          const bool single = MODE == kResidue && nchunks == 1;
+          if (single) {
+#pragma unroll
+            for (int cb = 0; cb < HALF; cb += 32) {
+              uint32_t r[32];
+              tmem_ld_32x32b_x32(taddr + cb, r);
+              tc_wait_ld();
+#pragma unroll
+              for (int j = 0; j < 32; ++j) acc[cb + j] = static_cast<int32_t>(r[j]);
+            }
+          } else if (MODE != kF32) {
 #pragma unroll
             for (int cb = 0; cb < HALF; cb += 32) {
               uint32_t r[32];
@@ -490,26 +519,45 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               for (int u = 0; u < HALF; ++u) acc[u] = static_cast<int32_t>(mod_signed(acc[u], m, magic));
               continue;
             }
-            // One 16-bit residue per element: the thread's row segment of HALF
-            // columns is contiguous in the residue plane, reduced and stored 8
-            // columns (one 16-byte vector) at a time.
-            const int64_t grow = row0 + lane;
-            uint16_t* rp = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane + grow * job.ldr + col0;
+            // One 16-bit residue per element, 64 columns at a time: each lane
+            // reduces its row's 64 residues into the warp's scratch (32 words
+            // per row), then the warp stores 4 rows x 128 bytes per
+            // instruction (lane: row 4 i + lane / 8, 16-byte segment lane % 8).
+            uint16_t* rplane = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane;
+            const float mf = static_cast<float>(m), invm = pairs.invm[gstart];
 #pragma unroll
-            for (int u = 0; u < HALF; u += 8) {
-              uint32_t w[4];
+            for (int h = 0; h < HALF; h += 64) {
+              if (single) {
 #pragma unroll
-              for (int q = 0; q < 4; ++q)
-                w[q] = mod_signed(acc[u + 2 * q], m, magic) | (mod_signed(acc[u + 2 * q + 1], m, magic) << 16);
-              if (grow < job.M) {
-                if (col0 + u + 8 <= job.N) {
-                  *reinterpret_cast<uint4*>(rp + u) = make_uint4(w[0], w[1], w[2], w[3]);
-                } else {
+                for (int q = 0; q < 32; ++q)
+                  tr[lane * 33 + q] =
+                      residue_pair_u16(__int_as_float(acc[h + 2 * q]), __int_as_float(acc[h + 2 * q + 1]), mf, invm);
+              } else {
 #pragma unroll
-                  for (int q = 0; q < 8; ++q)
-                    if (col0 + u + q < job.N) rp[u + q] = static_cast<uint16_t>(w[q >> 1] >> (16 * (q & 1)));
+                for (int q = 0; q < 32; ++q)
+                  tr[lane * 33 + q] =
+                      mod_signed(acc[h + 2 * q], m, magic) | (mod_signed(acc[h + 2 * q + 1], m, magic) << 16);
+              }
+              __syncwarp();
+              const int seg = lane & 7;
+              const int col = col0 + h + seg * 8;
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                const int r = 4 * i + (lane >> 3);
+                const int64_t grow = row0 + r;
+                const uint32_t* src = tr + r * 33 + seg * 4;
+                if (grow < job.M) {
+                  uint16_t* dst = rplane + grow * job.ldr + col;
+                  if (col + 8 <= job.N) {
+                    *reinterpret_cast<uint4*>(dst) = make_uint4(src[0], src[1], src[2], src[3]);
+                  } else {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                      if (col + e < job.N) dst[e] = static_cast<uint16_t>(src[e >> 1] >> (16 * (e & 1)));
+                  }
                 }
               }
+              __syncwarp();
             }
 #pragma unroll
             for (int u = 0; u < HALF; ++u) acc[u] = 0;
