@@ -39,13 +39,13 @@ def main() -> int:
     p.add_argument("--sizes", default="1024,2048,4096,8192,16384")
     p.add_argument("--max-n", type=int, default=16384)
     p.add_argument("--slices", default="7", help="digit-scheme slice counts to try")
-    p.add_argument("--moduli", default="13,14,15", help="modular-scheme moduli counts to try")
+    p.add_argument("--moduli", default="12,13,14", help="modular-scheme moduli counts to try")
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--target", type=float, default=1e-14)
-    p.add_argument("--margin", type=float, default=4.0)
+    p.add_argument("--margin", type=float, default=2.5)
     p.add_argument("--rows", type=int, default=32)
     p.add_argument("--grouped-count", type=int, default=512)
-    p.add_argument("--grouped-moduli", type=int, default=14)
+    p.add_argument("--grouped-moduli", type=int, default=13)
     p.add_argument("--clusters", default="1,2")
     p.add_argument("--out", default=str(HERE / "tune_table.txt"))
     a = p.parse_args()

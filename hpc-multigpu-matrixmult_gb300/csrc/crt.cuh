@@ -11,7 +11,6 @@ constexpr int kCrtMaxModuli = 15;  // M < 2^127: weights in four 32-bit limbs, s
 
 struct CrtTable {
   int n;                          // number of moduli
-  int bits;                       // b: the operands' fixed-point grid (result scale 2^(ea + eb - 2b))
   uint32_t W[kCrtMaxModuli][4];   // CRT weights (M / m_i) ((M / m_i)^-1 mod m_i), little-endian 32-bit limbs
   uint32_t M[4];                  // product of the moduli
   uint32_t Mhalf[4];              // floor(M / 2)

@@ -54,7 +54,11 @@ struct GSplitProb {
   // modular scheme only
   uint16_t* R;      // residue planes [moduli][m][ldr], 16 bits per residue
   int64_t ldr;
-  int bits, fast;   // the grid width for this K and the CRT path it allows
+  int* ba;          // grid widths of the rows of A and the columns of B
+  int* bb;
+  int* pe;          // column scan partials [chunk][n]: exponents, scaled sums of squares
+  float* ps;
+  int fast;         // the CRT's path (1: one step)
   double* C;
   int64_t ldc;
 };
@@ -103,6 +107,62 @@ __global__ void g_scan_cols_kernel(const GSplitProb* __restrict__ P, int count, 
   if (nf) record_error(status, PHPC_ERR_NONFINITE);
 }
 
+// Modular scheme: one warp per row of A: ea[i] and the row's grid width.
+__global__ void g_scan_rows_grid_kernel(const GSplitProb* __restrict__ P, int count, int total_rows,
+                                        const __grid_constant__ ModTable T, int* status) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= total_rows) return;
+  const GSplitProb& p = P[locate(P, count, r, [](const GSplitProb& q) { return q.row_start; })];
+  const int64_t row = r - p.row_start;
+  const double* a = p.A + row * p.lda;
+  NormAcc acc;
+  bool nf = false;
+  for (int k = threadIdx.x & 31; k < p.k; k += 32) norm_add(acc, a[k], nf);
+  acc = norm_warp(acc);
+  if ((threadIdx.x & 31) == 0) {
+    p.ea[row] = acc.e;
+    p.ba[row] = grid_bits(acc.s, p.k, T.logT);
+  }
+  if (__any_sync(0xffffffffu, nf) && (threadIdx.x & 31) == 0) record_error(status, PHPC_ERR_NONFINITE);
+}
+
+// Modular scheme, column scan part 1: one thread per (column, 256-row chunk)
+// unit keeps the chunk's exponent and scaled sum of squares.
+__global__ void g_scan_cols_part_kernel(const GSplitProb* __restrict__ P, int count, int total_units, int* status) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= total_units) return;
+  const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.cunit_start; })];
+  const int w = u - p.cunit_start;
+  const int64_t col = w % p.n;
+  const int chunk = w / p.n;
+  const int k0 = chunk * kScanKChunk, k1 = min(p.k, k0 + kScanKChunk);
+  NormAcc acc;
+  bool nf = false;
+  for (int k = k0; k < k1; ++k) norm_add(acc, p.B[(int64_t)k * p.ldb + col], nf);
+  p.pe[(int64_t)chunk * p.n + col] = acc.e;
+  p.ps[(int64_t)chunk * p.n + col] = acc.s;
+  if (nf) record_error(status, PHPC_ERR_NONFINITE);
+}
+
+// Part 2: one thread per column merges its chunks in order: eb[j], bb[j].
+__global__ void g_scan_cols_merge_kernel(const GSplitProb* __restrict__ P, int count, int total_cols,
+                                         const __grid_constant__ ModTable T) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= total_cols) return;
+  const GSplitProb& p = P[locate(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
+  const int64_t col = c - p.col_start;
+  const int chunks = (p.k + kScanKChunk - 1) / kScanKChunk;
+  NormAcc acc;
+  for (int ch = 0; ch < chunks; ++ch) {
+    NormAcc q;
+    q.e = p.pe[(int64_t)ch * p.n + col];
+    q.s = p.ps[(int64_t)ch * p.n + col];
+    norm_merge(acc, q);
+  }
+  p.eb[col] = acc.e;
+  p.bb[col] = grid_bits(acc.s, p.k, T.logT);
+}
+
 // Row splits: one thread per row piece (8 consecutive k of one row of A),
 // pieces numbered row by row across the problems, so that every thread of
 // the launch has work whatever each problem's K.
@@ -147,7 +207,7 @@ __global__ void __launch_bounds__(256, 4) g_residue_rows_kernel(const GSplitProb
   if (t >= total_pieces) return;
   const RowPiece rp = row_piece(P, count, t);
   const GSplitProb& p = *rp.p;
-  residue_row_piece(p.A + rp.row * p.lda, p.k, p.ea[rp.row], p.bits, T, p.pa + rp.row * p.ldp,
+  residue_row_piece(p.A + rp.row * p.lda, p.k, p.ea[rp.row], p.ba[rp.row], T, p.pa + rp.row * p.ldp,
                     (int64_t)p.m * p.ldp, rp.k0);
 }
 
@@ -161,7 +221,7 @@ __global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb
   const int64_t col = (int64_t)(lb % nblk_j) * kColBlockJ + (threadIdx.x >> 3);
   const int64_t k0 = (int64_t)(lb / nblk_j) * kColBlockK + (threadIdx.x & 7) * 8;
   if (col >= p.n || k0 >= p.ldp) return;
-  residue_col_piece(p.B, p.ldb, p.k, col, p.eb[col], p.bits, T, p.pb + col * p.ldp, (int64_t)p.n * p.ldp, k0);
+  residue_col_piece(p.B, p.ldb, p.k, col, p.eb[col], p.bb[col], T, p.pb + col * p.ldp, (int64_t)p.n * p.ldp, k0);
 }
 
 constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one warp)
@@ -180,15 +240,15 @@ __global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict
   const int64_t c0 = (int64_t)(w % chunks) * kCrtUnitCols + (threadIdx.x & 31) * kCrtCols;
   if (c0 >= p.n) return;
   crt_cols(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
-           static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - 2 * p.bits,
-           p.eb + c0, p.C + row * p.ldc + c0);
+           static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - p.ba[row],
+           p.eb + c0, p.bb + c0, p.C + row * p.ldc + c0);
 }
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct ProbLayout {
   int64_t ldp, ldr;
-  size_t ea, eb, pa, pb, r, end;  // offsets relative to the problem's base
+  size_t ea, eb, ba, bb, pe, ps, pa, pb, r, end;  // offsets relative to the problem's base
 };
 
 // planes = slices (digit scheme) or moduli (modular scheme, which adds the
@@ -197,9 +257,14 @@ ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
   ProbLayout L;
   L.ldp = ((int64_t)q.k + 7) / 8 * 8;
   L.ldr = ((int64_t)q.n + 15) / 16 * 16;
+  const size_t chunks = modular ? (static_cast<size_t>(q.k) + kScanKChunk - 1) / kScanKChunk : 0;
   L.ea = 0;
   L.eb = align_up(sizeof(int) * (size_t)q.m, 256);
-  L.pa = align_up(L.eb + sizeof(int) * (size_t)q.n, 256);
+  L.ba = align_up(L.eb + sizeof(int) * (size_t)q.n, 256);  // modular scheme: grids and column partials
+  L.bb = align_up(L.ba + (modular ? sizeof(int) * (size_t)q.m : 0), 256);
+  L.pe = align_up(L.bb + (modular ? sizeof(int) * (size_t)q.n : 0), 256);
+  L.ps = align_up(L.pe + sizeof(int) * chunks * q.n, 256);
+  L.pa = align_up(L.ps + sizeof(float) * chunks * q.n, 256);
   L.pb = align_up(L.pa + (size_t)planes * q.m * L.ldp * 2, 256);
   L.r = align_up(L.pb + (size_t)planes * q.n * L.ldp * 2, 256);
   L.end = modular ? align_up(L.r + (size_t)planes * q.m * L.ldr * 2, 256) : L.r;
@@ -306,12 +371,21 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   int* status = device_status_ptr();
   const bool modular = pl->moduli > 0;
   if (pl->total_rows > 0) {
-    g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
-                                                                        status);
-    g_reset_cols_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, stream>>>(pl->d_split, pl->count,
-                                                                            pl->total_cols);
-    g_scan_cols_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
-                                                                            pl->total_cunits, status);
+    if (modular) {
+      g_scan_rows_grid_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                               pl->total_rows, pl->mods, status);
+      g_scan_cols_part_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                                   pl->total_cunits, status);
+      g_scan_cols_merge_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                                  pl->total_cols, pl->mods);
+    } else {
+      g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
+                                                                          status);
+      g_reset_cols_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                              pl->total_cols);
+      g_scan_cols_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
+                                                                              pl->total_cunits, status);
+    }
     if (modular) {
       g_residue_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
                                                                                  pl->total_pieces, pl->mods);
@@ -415,8 +489,11 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     if (modular) {
       g.R = reinterpret_cast<uint16_t*>(pb + L.r);
       g.ldr = L.ldr;
-      g.bits = mod_grid_bits(planes, q.k);
-      g.fast = mod_crt_fast(planes, q.k, g.bits);
+      g.ba = reinterpret_cast<int*>(pb + L.ba);
+      g.bb = reinterpret_cast<int*>(pb + L.bb);
+      g.pe = reinterpret_cast<int*>(pb + L.pe);
+      g.ps = reinterpret_cast<float*>(pb + L.ps);
+      g.fast = mod_crt_fast();
       g.C = static_cast<double*>(q.C);
       g.ldc = q.ldc;
     }

@@ -76,6 +76,7 @@ int ozaki2_reconstruct_rows(int m, int r0, int rows, int k, int n, double* dC, i
                             size_t ws_bytes, cudaStream_t stream);
 int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, const void* ws, size_t ws_bytes,
                        cudaStream_t stream);
+int ozaki2_grids(int m, int k, int n, int nmod, const void* ws, size_t ws_bytes, int* ea, int* eb, int* ba, int* bb);
 int ozaki_prepare2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int s, void* ws,
                    size_t ws_bytes, cudaStream_t stream_a, cudaStream_t stream_b);
 int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const void* ws, size_t ws_bytes,

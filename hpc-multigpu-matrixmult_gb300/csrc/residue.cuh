@@ -26,8 +26,9 @@ constexpr uint32_t kModuli[kMaxModuli] = {363, 362, 361, 359, 355, 353, 349, 347
                                           343, 337, 331, 317, 313, 311, 307};
 
 struct ModTable {
-  int n;     // number of moduli
-  int bits;  // b: operands are integers of magnitude <= 2^b
+  int n;       // number of moduli
+  int bits;    // worst-case grid width for this K (2 K 2^(2b) < M); the kernels use per-row/column widths
+  float logT;  // log2 of the norm bound T (T^2 = M (1/2 - 1/32)), less a 2^-8 safety margin
   uint32_t m[kMaxModuli];
   uint32_t magic[kMaxModuli];  // floor(2^32 / m)
   // Per modulus, each value twice (both lanes of a packed f32x2 FMA):
@@ -48,18 +49,14 @@ inline int mod_grid_bits(int nmod, int k) {
   return std::min(62, static_cast<int>(std::floor((log_m - 1.0 - log_k) / 2.0 - 1e-9)));
 }
 
-// 1 when every result of a k-deep product on the b-bit grid satisfies
-// |y| / M <= 1/2 - 1/32 (|y| <= k 2^(2b)): the CRT may take its one-step path
-// (the quotient estimate errs by less than 0.01).
-inline int mod_crt_fast(int nmod, int k, int bits) {
-  // PHPC_CRT_EXACT=1 forces the multi-step path (for checking it: with the
-  // library's moduli every shape leaves the margin)
+// 1: the CRT takes its one-step path, valid when every result satisfies
+// |y| / M <= 1/2 - 1/32 (the quotient estimate errs by less than 0.01), which
+// the per-row/column grids guarantee (grid_bits: |y_ij| <= |A'_i| |B'_j| <= T^2).
+// PHPC_CRT_EXACT=1 forces the multi-step path (to check that it gives the
+// same bits).
+inline int mod_crt_fast() {
   const char* env = getenv("PHPC_CRT_EXACT");
-  if (env && atoi(env) == 1) return 0;
-  double log_m = 0;
-  for (int i = 0; i < nmod; ++i) log_m += std::log2(static_cast<double>(kModuli[i]));
-  const double ratio = std::exp2(std::log2(static_cast<double>(k)) + 2.0 * bits - log_m);
-  return ratio <= 0.5 - 1.0 / 32 - 1e-9 ? 1 : 0;
+  return (env && atoi(env) == 1) ? 0 : 1;
 }
 
 inline ModTable make_table(int nmod, int k) {
@@ -69,6 +66,11 @@ inline ModTable make_table(int nmod, int k) {
   u128 M = 1;
   for (int i = 0; i < nmod; ++i) M *= kModuli[i];
   T.bits = mod_grid_bits(nmod, k);
+  {
+    double log_m = 0;
+    for (int i = 0; i < nmod; ++i) log_m += std::log2(static_cast<double>(kModuli[i]));
+    T.logT = static_cast<float>(0.5 * (log_m + std::log2(15.0 / 32.0)) - 1.0 / 256);
+  }
   for (int i = 0; i < nmod; ++i) {
     const uint32_t m = kModuli[i];
     T.m[i] = m;
@@ -100,9 +102,85 @@ inline ModTable make_table(int nmod, int k) {
   T.crt.qlimb = std::max(0, (bitlen - 51 + 31) / 32);
   T.crt.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.crt.qlimb))));
   T.crt.n = T.n;
-  T.crt.bits = T.bits;
-  T.crt.fast = mod_crt_fast(nmod, k, T.bits);
+  T.crt.fast = mod_crt_fast();
   return T;
+}
+
+// Per-row (column) grid widths. Row i of A is put on the grid
+// A'_ik = round(|a_ik| 2^(b_i - e_i)) with b_i chosen from the row's own
+// Euclidean norm so that |A'_i|_2 <= T, T^2 = M (1/2 - 1/32); the same for
+// the columns of B. By Cauchy-Schwarz every exact product then satisfies
+// |y_ij| <= |A'_i| |B'_j| <= M (1/2 - 1/32): the CRT recovers it in one step.
+// The norm is bounded from above in single precision: v = |a| 2^-e in [0, 1)
+// truncated to a float and raised by one ulp, squares summed with the running
+// exponent raised as larger elements appear (exact power-of-two rescaling),
+// the sum raised by (1 + K 2^-22) for its roundings; b = floor(log2 T -
+// log2(norm)) with a 2^-8 margin in log2 T for log2f and the rounding of
+// the elements themselves (at most sqrt(K) / 2 in norm, far below it).
+
+// Upper bound of |x| 2^-e as a float, for finite |x| < 2^e (0 for x = 0).
+__device__ __forceinline__ float scaled_abs_up(double x, int e) {
+  const uint64_t b = static_cast<uint64_t>(__double_as_longlong(x)) & 0x7FFFFFFFFFFFFFFFull;
+  if (b == 0) return 0.0f;
+  const int E = static_cast<int>(b >> 52);
+  uint64_t mant;  // |x| = mant 2^p, 2^52 <= mant < 2^53
+  int p;
+  if (E != 0) {
+    mant = (b & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+    p = E - 1075;
+  } else {  // subnormal
+    const int sh = __clzll(static_cast<long long>(b)) - 11;
+    mant = b << sh;
+    p = -1074 - sh;
+  }
+  const int ef = p + 52 - e + 127;  // biased float exponent of |x| 2^-e (<= 126)
+  if (ef <= 0) return 1.17549435e-38f;  // |x| 2^-e < 2^-126
+  return __uint_as_float(((static_cast<uint32_t>(ef) << 23) | static_cast<uint32_t>((mant >> 29) & 0x7FFFFFu)) + 1u);
+}
+
+// Running maximum exponent and sum of squares of |x| 2^-e of a set of values.
+struct NormAcc {
+  int e = kExpZero;
+  float s = 0.0f;
+};
+
+__device__ __forceinline__ void norm_add(NormAcc& a, double x, bool& nonfinite) {
+  const int ex = exponent_of(x, nonfinite);
+  if (ex > a.e) {
+    a.s = a.e > kExpZero ? ldexpf(a.s, 2 * (a.e - ex)) : 0.0f;
+    a.e = ex;
+  }
+  if (ex > kExpZero && ex < kExpNonFinite) {
+    const float v = scaled_abs_up(x, a.e);
+    a.s = fmaf(v, v, a.s);
+  }
+}
+
+__device__ __forceinline__ void norm_merge(NormAcc& a, const NormAcc& b) {
+  const int e = max(a.e, b.e);
+  const float sa = a.e > kExpZero ? ldexpf(a.s, 2 * (a.e - e)) : 0.0f;
+  const float sb = b.e > kExpZero ? ldexpf(b.s, 2 * (b.e - e)) : 0.0f;
+  a.e = e;
+  a.s = sa + sb;
+}
+
+// Merge over the 32 lanes of a warp (every lane gets the result).
+__device__ __forceinline__ NormAcc norm_warp(NormAcc a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    NormAcc b;
+    b.e = __shfl_xor_sync(0xffffffffu, a.e, o);
+    b.s = __shfl_xor_sync(0xffffffffu, a.s, o);
+    norm_merge(a, b);
+  }
+  return a;
+}
+
+// Grid width of a row/column with scaled sum of squares s over K elements.
+__device__ __forceinline__ int grid_bits(float s, int K, float logT) {
+  if (!(s > 0.0f)) return 62;  // all zero: any grid
+  const float su = s * (1.0f + static_cast<float>(K) * 2.384185791015625e-07f);
+  return min(62, static_cast<int>(floorf(logT - 0.5f * log2f(su))));
 }
 
 constexpr int kLimbs = 5;  // balanced 13-bit limbs of an operand integer
@@ -212,10 +290,12 @@ constexpr int kCrtCols = 4;  // consecutive columns per thread (one 8-byte load 
 
 // C[row][c0 .. c0 + 3] += the CRT of their residues (rp: plane 0 of the 16-bit
 // residue planes at the row and column c0; c0 a multiple of 4 inside a plane
-// row padded to 16), scaled by 2^(e_row + eb[c] - 2 bits). Columns at or
-// beyond ncols are left alone.
+// row padded to 16), scaled by 2^(row_shift + eb[c] - bb[c]) (row_shift: the
+// row's exponent less its grid width). Columns at or beyond ncols are left
+// alone.
 __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_t rplane, const CrtTable& T, int fast,
-                                         int ncols, int e_row_2b, const int* __restrict__ ebp, double* cp) {
+                                         int ncols, int row_shift, const int* __restrict__ ebp,
+                                         const int* __restrict__ bbp, double* cp) {
   uint2 rw[kCrtMaxModuli];
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i)
@@ -233,7 +313,7 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
       for (int i = 0; i < kCrtMaxModuli; ++i) r[i] = ((c < 2 ? rw[i].x : rw[i].y) >> (16 * (c & 1))) & 0xFFFFu;
       int shift;
       const double v = crt_value(r, T, fast, shift);
-      cv[c] = crt_added(cv[c], v, shift + e_row_2b + max(ebp[c], -20000));
+      cv[c] = crt_added(cv[c], v, shift + row_shift + max(ebp[c], -20000) - bbp[c]);
     }
 #pragma unroll
     for (int c = 0; c < kCrtCols; ++c) cp[c] = cv[c];
@@ -247,7 +327,7 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
     for (int i = 0; i < kCrtMaxModuli; ++i) r[i] = ((c < 2 ? rw[i].x : rw[i].y) >> (16 * (c & 1))) & 0xFFFFu;
     int shift;
     const double v = crt_value(r, T, fast, shift);
-    crt_apply(cp + c, v, shift + e_row_2b + max(ebp[c], -20000));
+    crt_apply(cp + c, v, shift + row_shift + max(ebp[c], -20000) - bbp[c]);
   }
 }
 

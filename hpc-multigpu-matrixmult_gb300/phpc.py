@@ -89,6 +89,9 @@ _lib.phpc_ozaki2_multiply_dev.restype = ct.c_int
 _lib.phpc_ozaki2_reconstruct_dev.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_int64, ct.c_int,
                                              ct.c_void_p, ct.c_size_t, ct.c_void_p]
 _lib.phpc_ozaki2_reconstruct_dev.restype = ct.c_int
+_lib.phpc_ozaki2_grids.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_void_p, ct.c_size_t, ct.c_void_p,
+                                   ct.c_void_p, ct.c_void_p, ct.c_void_p]
+_lib.phpc_ozaki2_grids.restype = ct.c_int
 _lib.phpc_default_moduli.argtypes = [ct.c_int, ct.c_int, ct.c_int]
 _lib.phpc_default_moduli.restype = ct.c_int
 
@@ -233,6 +236,18 @@ def ozaki2_multiply_dev(m, k, n, moduli, workspace, workspace_bytes, stream=None
 def ozaki2_reconstruct_dev(m, k, n, C, ldc, moduli, workspace, workspace_bytes, stream=None) -> None:
     _check(_lib.phpc_ozaki2_reconstruct_dev(m, k, n, _dptr(C), ldc, moduli, _dptr(workspace), workspace_bytes,
                                             _stream(stream)), "phpc_ozaki2_reconstruct_dev")
+
+
+def ozaki2_grids(m, k, n, moduli, workspace, workspace_bytes):
+    """(ea, eb, ba, bb) of the last modular prepare on this workspace: the rows'
+    and columns' largest exponents and grid widths (numpy int32 arrays)."""
+    import numpy as np
+
+    ea, ba = np.zeros(m, dtype=np.int32), np.zeros(m, dtype=np.int32)
+    eb, bb = np.zeros(n, dtype=np.int32), np.zeros(n, dtype=np.int32)
+    _check(_lib.phpc_ozaki2_grids(m, k, n, moduli, _dptr(workspace), workspace_bytes, ea.ctypes.data,
+                                  eb.ctypes.data, ba.ctypes.data, bb.ctypes.data), "phpc_ozaki2_grids")
+    return ea, eb, ba, bb
 
 
 def ozaki_prepare_dev(m, k, n, A, lda, B, ldb, slices, workspace, workspace_bytes, stream=None) -> None:

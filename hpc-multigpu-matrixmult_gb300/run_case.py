@@ -3,7 +3,7 @@
 Used to reproduce single launches for profiling (ncu) and timing:
 
     python hpc-multigpu-matrixmult_gb300/run_case.py --method ozaki --n 4096 --slices 7 --reps 2
-    python hpc-multigpu-matrixmult_gb300/run_case.py --method ozaki2 --n 4096 --moduli 14 --reps 2
+    python hpc-multigpu-matrixmult_gb300/run_case.py --method ozaki2 --n 4096 --moduli 13 --reps 2
     python hpc-multigpu-matrixmult_gb300/run_case.py --method dmma --n 2048
     python hpc-multigpu-matrixmult_gb300/run_case.py --method bf16x3 --m 32768 --n 8192 --k 4096
     python hpc-multigpu-matrixmult_gb300/run_case.py --method grouped --count 512
@@ -34,8 +34,8 @@ def main() -> int:
     p.add_argument("--m", type=int, default=0)
     p.add_argument("--k", type=int, default=0)
     p.add_argument("--slices", type=int, default=7)
-    p.add_argument("--moduli", type=int, default=14, help="ozaki2: number of residue GEMMs")
-    p.add_argument("--grouped-moduli", type=int, default=14,
+    p.add_argument("--moduli", type=int, default=13, help="ozaki2: number of residue GEMMs")
+    p.add_argument("--grouped-moduli", type=int, default=13,
                    help="grouped: modular scheme with this many moduli (0 = digit scheme with --slices)")
     p.add_argument("--reps", type=int, default=2)
     p.add_argument("--emin", type=int, default=-20)

@@ -92,26 +92,34 @@ int phpc_dgemm_ozaki_dev(int m, int k, int n, const double *dA, int64_t lda, con
 
 /* FP64-accurate GEMM by the modular (Chinese-remainder) Ozaki scheme:
  * C += A * B from `moduli` (8..15) residue GEMMs. Each operand element becomes
- * an integer on the fixed-point grid of its row (A) / column (B), b bits wide
- * with b the largest width for which 2 K 2^(2b) < M = product of the moduli
- * (moduli = 14: b = 51, moduli = 15: b = 55 at K = 16384); its residues
- * modulo the pairwise-coprime moduli 363, 362, 361, 359, 355, 353, 349, 347,
- * 343, 337, 331, 317, 313, 311, 307 (the first `moduli`; |r| <= 181) are exact in
- * BF16, the residue products run on tcgen05, and the exact integer product is
- * recovered by the CRT and rounded once to double. */
+ * an integer on the fixed-point grid of its row (A) / column (B): b_i bits
+ * below the row's largest power of two, b_i chosen from the row's Euclidean
+ * norm so that |A'_i| <= T and |B'_j| <= T with T^2 = M (1/2 - 1/32),
+ * M = product of the moduli (at least the worst-case width, 2 K 2^(2b) < M:
+ * moduli = 14 gives b >= 51 at K = 16384; spread-out rows get up to ~4 bits
+ * more); its residues modulo the pairwise-coprime moduli 363, 362, 361, 359,
+ * 355, 353, 349, 347, 343, 337, 331, 317, 313, 311, 307 (the first `moduli`;
+ * |r| <= 181) are exact in BF16, the residue products run on tcgen05, and the
+ * exact integer product is recovered by the CRT and rounded once to double. */
 size_t phpc_ozaki2_workspace_bytes(int m, int k, int n, int moduli);
 int phpc_dgemm_ozaki2_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
                           double *dC, int64_t ldc, int moduli, void *workspace, size_t workspace_bytes, void *stream);
 
 /* The three phases of phpc_dgemm_ozaki2_dev (same workspace):
- * prepare = exponent scans + residue split of A and B;
+ * prepare = exponent and grid scans + residue split of A and B;
  * multiply = the residue GEMMs (one 16-bit residue per element and modulus, in the
- * workspace); reconstruct = CRT, rounding and C += result * 2^(ea + eb - 2b). */
+ * workspace); reconstruct = CRT, rounding and
+ * C += result * 2^(ea[i] - ba[i] + eb[j] - bb[j]). */
 int phpc_ozaki2_prepare_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,
                             int moduli, void *workspace, size_t workspace_bytes, void *stream);
 int phpc_ozaki2_multiply_dev(int m, int k, int n, int moduli, void *workspace, size_t workspace_bytes, void *stream);
 int phpc_ozaki2_reconstruct_dev(int m, int k, int n, double *dC, int64_t ldc, int moduli, void *workspace,
                                 size_t workspace_bytes, void *stream);
+/* The grids of the last prepare on this workspace, copied to host arrays
+ * (synchronous): ea[m] / eb[n] the largest exponents (|x| < 2^e) of the rows
+ * of A / columns of B, ba[m] / bb[n] their grid widths. */
+int phpc_ozaki2_grids(int m, int k, int n, int moduli, const void *workspace, size_t workspace_bytes, int *ea,
+                      int *eb, int *ba, int *bb);
 
 /* The two phases of phpc_dgemm_ozaki_dev, for callers that reuse the digit
  * planes of A and B or time the phases separately:

@@ -94,11 +94,14 @@ def test_plan_validation(phpc, torch_cuda):
 
 
 def single_modular(phpc, torch, A, B, C, q):
+    """The single-problem modular call; returns its grids (ea, eb, ba, bb)."""
     m, k = A.shape
     n = B.shape[1]
     ws = phpc.ozaki2_workspace_bytes(m, k, n, q)
     W = torch.empty(ws, dtype=torch.uint8, device="cuda")
     phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, q, W, ws)
+    torch.cuda.synchronize()
+    return phpc.ozaki2_grids(m, k, n, q, W, ws)
 
 
 @pytest.mark.parametrize("bn", ["128", "256"])
@@ -125,11 +128,10 @@ def test_grouped_modular_equals_single(phpc, oracle, torch_cuda, monkeypatch, bn
     for i, (a, b, c0, A, B, C) in enumerate(batch):
         got = C.cpu().numpy()
         C1 = torch.from_numpy(c0).cuda()
-        single_modular(phpc, torch, A, B, C1, q)
-        torch.cuda.synchronize()
+        grid = single_modular(phpc, torch, A, B, C1, q)
         np.testing.assert_array_equal(got, C1.cpu().numpy(), err_msg=f"problem {i} {shapes[i]}")
         if a.size * b.shape[1] <= 200000:
-            np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, q), err_msg=f"model, problem {i}")
+            np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, q, grid), err_msg=f"model, problem {i}")
         if i < 6:
             err = oracle.rel_errors(got, oracle.gemm_dd(a, b, c0))
             assert err["frob"] <= 1e-14, (i, err)

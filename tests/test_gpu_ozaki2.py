@@ -1,10 +1,13 @@
 """Parity of the modular (CRT) Ozaki GEMM with the oracle.
 
 Bit-exact against tests/ozaki2_model.py (exact integer product of the
-fixed-point operands, rounded once to double): checks the residue split, the
-exactness of the residue GEMMs on tcgen05, the CRT reconstruction and its
-rounding. Also exact on the reference's index inputs and within 1e-14
-(Frobenius) of the double-double oracle on wide-exponent inputs.
+fixed-point operands on the grids the device chose, rounded once to double):
+checks the residue split, the exactness of the residue GEMMs on tcgen05, the
+CRT reconstruction and its rounding. The device's grids are checked on their
+own: exponents equal to the model's, grid widths within one of the
+double-precision rule, and the norm bound that makes the CRT exact, in exact
+integer arithmetic. Also exact on the reference's index inputs and within
+1e-14 (Frobenius) of the double-double oracle on wide-exponent inputs.
 """
 import numpy as np
 import pytest
@@ -17,7 +20,28 @@ pytestmark = pytest.mark.gpu
 
 
 
-def run_dev(phpc, torch, a, b, c0, nmod):
+def check_grid(a, b, grid, nmod):
+    """The device's grids: exponents as the model's, widths within one of the
+    double-precision rule, and |A'_i|^2, |B'_j|^2 <= T^2 = M (1/2 - 1/32)
+    exactly (so every |C_int| <= M (1/2 - 1/32))."""
+    ea, eb, ba, bb = (np.asarray(x, dtype=np.int64) for x in grid)
+    mea, meb, mba, mbb = ozaki2_model.grids(a, b, nmod)
+    np.testing.assert_array_equal(ea, mea)
+    np.testing.assert_array_equal(eb, meb)
+    assert np.abs(ba - mba).max() <= 1 and np.abs(bb - mbb).max() <= 1, (ba - mba, bb - mbb)
+    M = 1
+    for q in ozaki2_model.MODULI[:nmod]:
+        M *= q
+    ai = ozaki2_model.to_int(a, ea[:, None], ba[:, None])
+    bi = ozaki2_model.to_int(b, eb[None, :], bb[None, :])
+    for i in range(a.shape[0]):
+        assert 32 * sum(int(x) * int(x) for x in ai[i]) <= 15 * M, i
+    for j in range(b.shape[1]):
+        assert 32 * sum(int(x) * int(x) for x in bi[:, j]) <= 15 * M, j
+
+
+def run_dev_grid(phpc, torch, a, b, c0, nmod):
+    """The device call; returns C and the grids the device chose."""
     m, k = a.shape
     n = b.shape[1]
     A = torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -28,7 +52,11 @@ def run_dev(phpc, torch, a, b, c0, nmod):
     phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, nmod, W, nbytes)
     torch.cuda.synchronize()
     assert phpc.device_status() == 0
-    return C.cpu().numpy()
+    return C.cpu().numpy(), phpc.ozaki2_grids(m, k, n, nmod, W, nbytes)
+
+
+def run_dev(phpc, torch, a, b, c0, nmod):
+    return run_dev_grid(phpc, torch, a, b, c0, nmod)[0]
 
 
 @pytest.mark.parametrize("nmod", [8, 12, 14, 15])
@@ -38,8 +66,34 @@ def test_bitexact_vs_model(phpc, torch_cuda, nmod, m, k, n):
     a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
     b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-20, 21, (k, n)))
     c0 = rng.uniform(-1, 1, (m, n))
-    got = run_dev(phpc, torch_cuda, a, b, c0, nmod)
-    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, nmod))
+    got, grid = run_dev_grid(phpc, torch_cuda, a, b, c0, nmod)
+    check_grid(a, b, grid, nmod)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, nmod, grid))
+
+
+@pytest.mark.parametrize("kind", ["uniform", "constant", "one-large", "subnormal"])
+def test_grids_bound_and_rule(phpc, torch_cuda, kind):
+    """Grids on inputs that stress the norm bound: all entries equal (the
+    norm at its largest, sqrt(K) times the largest entry), one large entry per
+    row, subnormal entries."""
+    rng = np.random.default_rng(5)
+    m, k, n = 33, 777, 41
+    a = rng.uniform(-1, 1, (m, k))
+    b = rng.uniform(-1, 1, (k, n))
+    if kind == "constant":
+        a[:] = 0.7
+        b[:] = -(2.0 ** 40)
+    elif kind == "one-large":
+        a *= 1e-9
+        a[np.arange(m), rng.integers(0, k, m)] = 3.0
+        b *= 1e-12
+        b[rng.integers(0, k, n), np.arange(n)] = -5.0
+    elif kind == "subnormal":
+        a *= 2.0 ** -1060
+        b *= 2.0 ** -1050
+    got, grid = run_dev_grid(phpc, torch_cuda, a, b, np.zeros((m, n)), 14)
+    check_grid(a, b, grid, 14)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 14, grid))
 
 
 @pytest.mark.parametrize("cluster,bn", [("1", "128"), ("2", "256")])
@@ -49,8 +103,8 @@ def test_bitexact_tile_variants(phpc, torch_cuda, monkeypatch, cluster, bn):
     rng = np.random.default_rng(77)
     a = rng.uniform(-1, 1, (300, 400))
     b = rng.uniform(-1, 1, (400, 520))
-    got = run_dev(phpc, torch_cuda, a, b, np.zeros((300, 520)), 15)
-    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 15))
+    got, grid = run_dev_grid(phpc, torch_cuda, a, b, np.zeros((300, 520)), 15)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 15, grid))
 
 
 @pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] == "index"], ids=lambda c: c["name"])
@@ -83,8 +137,8 @@ def test_zero_rows_columns_and_argument_errors(phpc, torch_cuda):
     a[3] = 0.0
     b[:, 7] = 0.0
     c0 = rng.uniform(-1, 1, (64, 80))
-    got = run_dev(phpc, torch_cuda, a, b, c0, 15)
-    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 15))
+    got, grid = run_dev_grid(phpc, torch_cuda, a, b, c0, 15)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 15, grid))
     np.testing.assert_array_equal(got[3], c0[3])
     torch = torch_cuda
     A = torch.zeros(64, 64, dtype=torch.float64, device="cuda")
@@ -117,13 +171,14 @@ def test_phases_equal_one_call(phpc, torch_cuda):
     np.testing.assert_array_equal(C.cpu().numpy(), want)
 
 
-def test_host_entry_uses_modular_scheme(phpc, monkeypatch):
+def test_host_entry_uses_modular_scheme(phpc, torch_cuda, monkeypatch):
     """phpc_gemm_cublas with PHPC_MODULI=q computes the modular scheme's bits."""
     rng = np.random.default_rng(10)
     a = rng.uniform(-1, 1, (150, 333)) * np.exp2(rng.integers(-20, 21, (150, 333)))
     b = rng.uniform(-1, 1, (333, 170))
     c = rng.uniform(-1, 1, (150, 170))
-    want = ozaki2_model.gemm(a, b, c, 13)
+    _, grid = run_dev_grid(phpc, torch_cuda, a, b, np.zeros((150, 170)), 13)
+    want = ozaki2_model.gemm(a, b, c, 13, grid)
     monkeypatch.setenv("PHPC_MODULI", "13")
     assert phpc.default_moduli(150, 333, 170) == 13
     phpc.gemm_host("ozaki", a, b, c)
@@ -176,9 +231,9 @@ def test_crt_multi_step_path_same_bits(phpc, torch_cuda, monkeypatch, nmod):
     c0 = rng.uniform(-1, 1, (m, n))
     fast = run_dev(phpc, torch_cuda, a, b, c0, nmod)
     monkeypatch.setenv("PHPC_CRT_EXACT", "1")
-    exact = run_dev(phpc, torch_cuda, a, b, c0, nmod)
+    exact, grid = run_dev_grid(phpc, torch_cuda, a, b, c0, nmod)
     np.testing.assert_array_equal(exact, fast)
-    np.testing.assert_array_equal(exact, ozaki2_model.gemm(a, b, c0, nmod))
+    np.testing.assert_array_equal(exact, ozaki2_model.gemm(a, b, c0, nmod, grid))
 
 
 def test_long_k_intermediate_reduction(phpc, torch_cuda):
@@ -190,8 +245,8 @@ def test_long_k_intermediate_reduction(phpc, torch_cuda):
     a = rng.uniform(-1, 1, (m, k))
     b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-8, 9, (k, n)))
     c0 = rng.uniform(-1, 1, (m, n))
-    got = run_dev(phpc, torch_cuda, a, b, c0, 14)
-    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 14))
+    got, grid = run_dev_grid(phpc, torch_cuda, a, b, c0, 14)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 14, grid))
 
 
 def test_strided_leading_dimensions(phpc, torch_cuda):
@@ -204,7 +259,6 @@ def test_strided_leading_dimensions(phpc, torch_cuda):
     B_full = rng.uniform(-1, 1, (k, n + 7))
     C_full = rng.uniform(-1, 1, (m, n + 5))
     a, b, c0 = A_full[:, :k], B_full[:, :n], C_full[:, :n]
-    want = ozaki2_model.gemm(np.ascontiguousarray(a), np.ascontiguousarray(b), np.ascontiguousarray(c0), 14)
     A, B, C = (torch.from_numpy(x).cuda() for x in (A_full, B_full, C_full))
     ws = phpc.ozaki2_workspace_bytes(m, k, n, 14)
     W = torch.empty(ws, dtype=torch.uint8, device="cuda")
@@ -212,5 +266,7 @@ def test_strided_leading_dimensions(phpc, torch_cuda):
     torch.cuda.synchronize()
     assert phpc.device_status() == 0
     got = C.cpu().numpy()
+    grid = phpc.ozaki2_grids(m, k, n, 14, W, ws)
+    want = ozaki2_model.gemm(np.ascontiguousarray(a), np.ascontiguousarray(b), np.ascontiguousarray(c0), 14, grid)
     np.testing.assert_array_equal(got[:, :n], want)
     np.testing.assert_array_equal(got[:, n:], C_full[:, n:])
