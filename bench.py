@@ -62,7 +62,8 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 # (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by
 # (N, "slices" | "moduli", count).
 NCU_TRAFFIC_BYTES = {(16384, "slices", 7): 426.25e9 + 15.28e9,
-                     (16384, "moduli", 14): 153.23e9 + 7.52e9}
+                     (16384, "moduli", 14): 153.23e9 + 7.52e9,
+                     (16384, "moduli", 13): 145.21e9 + 7.00e9}
 UNIT = "TFLOP/s"
 
 
@@ -361,15 +362,32 @@ def run_ours(args, world, rank, local):
     torch.cuda.empty_cache()
     an, bn, cn = Ah.numpy(), Bh.numpy(), Ch.numpy()
     phpc.gemm_cublas(an, n, bn, n, cn, n, n, n, n)  # warm: allocations, tensor maps
-    e2e_s, e2e_kernel_s, link_gbs = [], [], []
+    e2e_s, e2e_kernel_s, link_gbs, link_waits = [], [], [], []
     probe = torch.empty((n, n), dtype=torch.float64, device=dev)
-    for _ in range(max(1, args.e2e_steps)):
-        # the host link's state just before the call: one pinned 2 GiB copy (untimed by the metric)
-        barrier()
+
+    def link_probe() -> float:
         w0 = time.perf_counter()
         probe.copy_(Ah, non_blocking=True)
         torch.cuda.synchronize()
-        link_gbs.append(n * n * 8 / (time.perf_counter() - w0) / 1e9)
+        return n * n * 8 / (time.perf_counter() - w0) / 1e9
+
+    best_link = 0.0
+    for _ in range(max(1, args.e2e_steps)):
+        # the host link's state just before the call: one pinned 2 GiB copy
+        # (untimed by the metric). The link is shared with other jobs on the
+        # host: a call starts once a probe reaches 80 % of the best probe
+        # seen, after at most 20 probes 50 ms apart; every call is timed
+        # and counted, whatever its probe.
+        barrier()
+        waits = 0
+        g = link_probe()
+        while g < 0.8 * max(best_link, g) and waits < 20:
+            time.sleep(0.05)
+            waits += 1
+            g = link_probe()
+        best_link = max(best_link, g)
+        link_gbs.append(g)
+        link_waits.append(waits)
         barrier()
         w0 = time.perf_counter()
         e2e_kernel_s.append(phpc.gemm_cublas(an, n, bn, n, cn, n, n, n, n))
@@ -438,7 +456,8 @@ def run_ours(args, world, rank, local):
                 "wall_ms_each": [round(x * 1e3, 1) for x in e2e_s],
                 "note": "host-link bound; the link is shared with other jobs on the host, so wall times vary",
                 "kernel_ms_each": [round(x * 1e3, 1) for x in e2e_kernel_s],
-                "h2d_link_gbs_before_each": [round(x, 1) for x in link_gbs]},
+                "h2d_link_gbs_before_each": [round(x, 1) for x in link_gbs],
+                "link_probe_waits_each": link_waits},
         "gpu_launches": sch.launches * args.steps,
         "clocks": clocks.summary(),
     }
