@@ -117,7 +117,7 @@ __global__ void g_scan_rows_grid_kernel(const GSplitProb* __restrict__ P, int co
   const double* a = p.A + row * p.lda;
   NormAcc acc;
   bool nf = false;
-  for (int k = threadIdx.x & 31; k < p.k; k += 32) norm_add(acc, a[k], nf);
+  norm_row_lane(a, p.k, threadIdx.x & 31, acc, nf);
   acc = norm_warp(acc);
   if ((threadIdx.x & 31) == 0) {
     p.ea[row] = acc.e;
@@ -138,7 +138,7 @@ __global__ void g_scan_cols_part_kernel(const GSplitProb* __restrict__ P, int co
   const int k0 = chunk * kScanKChunk, k1 = min(p.k, k0 + kScanKChunk);
   NormAcc acc;
   bool nf = false;
-  for (int k = k0; k < k1; ++k) norm_add(acc, p.B[(int64_t)k * p.ldb + col], nf);
+  norm_col_chunk(p.B, p.ldb, col, k0, k1, acc, nf);
   p.pe[(int64_t)chunk * p.n + col] = acc.e;
   p.ps[(int64_t)chunk * p.n + col] = acc.s;
   if (nf) record_error(status, PHPC_ERR_NONFINITE);

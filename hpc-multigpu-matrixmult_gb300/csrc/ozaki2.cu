@@ -46,7 +46,7 @@ __global__ void scan_rows_grid_kernel(const double* __restrict__ A, int64_t lda,
   const double* a = A + row * lda;
   NormAcc acc;
   bool nf = false;
-  for (int k = threadIdx.x & 31; k < K; k += 32) norm_add(acc, a[k], nf);
+  norm_row_lane(a, K, threadIdx.x & 31, acc, nf);
   acc = norm_warp(acc);
   if ((threadIdx.x & 31) == 0) {
     ea[row] = acc.e;
@@ -66,7 +66,7 @@ __global__ void scan_cols_part_kernel(const double* __restrict__ B, int64_t ldb,
   const int k0 = blockIdx.y * kGridKChunk, k1 = min(K, k0 + kGridKChunk);
   NormAcc acc;
   bool nf = false;
-  for (int k = k0; k < k1; ++k) norm_add(acc, B[(int64_t)k * ldb + col], nf);
+  norm_col_chunk(B, ldb, col, k0, k1, acc, nf);
   pe[blockIdx.y * ldpart + col] = acc.e;
   ps[blockIdx.y * ldpart + col] = acc.s;
   if (nf) record_error(status, PHPC_ERR_NONFINITE);

@@ -176,6 +176,36 @@ __device__ __forceinline__ NormAcc norm_warp(NormAcc a) {
   return a;
 }
 
+// One lane's share of a row's scan: elements lane, lane + 32, ... in that
+// order, four loads issued before they are accumulated.
+__device__ __forceinline__ void norm_row_lane(const double* __restrict__ a, int K, int lane, NormAcc& acc,
+                                              bool& nonfinite) {
+  int k = lane;
+  for (; k + 96 < K; k += 128) {
+    const double x0 = a[k], x1 = a[k + 32], x2 = a[k + 64], x3 = a[k + 96];
+    norm_add(acc, x0, nonfinite);
+    norm_add(acc, x1, nonfinite);
+    norm_add(acc, x2, nonfinite);
+    norm_add(acc, x3, nonfinite);
+  }
+  for (; k < K; k += 32) norm_add(acc, a[k], nonfinite);
+}
+
+// Rows k0 .. k1 - 1 of column col of B, in order, four loads at a time.
+__device__ __forceinline__ void norm_col_chunk(const double* __restrict__ B, int64_t ldb, int64_t col, int k0, int k1,
+                                               NormAcc& acc, bool& nonfinite) {
+  int k = k0;
+  for (; k + 3 < k1; k += 4) {
+    const double x0 = B[(int64_t)k * ldb + col], x1 = B[(int64_t)(k + 1) * ldb + col];
+    const double x2 = B[(int64_t)(k + 2) * ldb + col], x3 = B[(int64_t)(k + 3) * ldb + col];
+    norm_add(acc, x0, nonfinite);
+    norm_add(acc, x1, nonfinite);
+    norm_add(acc, x2, nonfinite);
+    norm_add(acc, x3, nonfinite);
+  }
+  for (; k < k1; ++k) norm_add(acc, B[(int64_t)k * ldb + col], nonfinite);
+}
+
 // Grid width of a row/column with scaled sum of squares s over K elements.
 __device__ __forceinline__ int grid_bits(float s, int K, float logT) {
   if (!(s > 0.0f)) return 62;  // all zero: any grid
