@@ -12,7 +12,7 @@ split + exact BF16 slice products + FP64 fold). --moduli / --slices override.
 Reported (one JSON line on rank 0):
   value      2 N^3 / (device time per step), inputs resident in HBM, TFLOP/s
              (FP64-equivalent); every step reads 3 x 2 GiB of FP64 operands and
-             writes the split planes (8 GiB per operand at 15 moduli), far
+             writes the split planes (7 GB per operand at 13 moduli), far
              larger than the 129 MB L2.
   e2e        the same metric through the reference-facing C ABI call
              phpc_gemm_cublas with pinned host buffers: host->device copies of
@@ -31,6 +31,11 @@ Reported (one JSON line on rank 0):
   other_scheme  the digit (or modular) scheme on the same inputs, for context.
   cpu_baseline  the reference's CPU loop (src/iterative.c:8-13, oracle port)
              on all host cores, on a bounded sample of rows of the same product.
+
+--cpu-scaling (opt-in, a few minutes of CPU) times the reference's sequential
+program (bin/iterative.out at -O2 and bin/iterative_noopt.out at the
+reference Makefile's flags) on one core at N = 1024, 2048, 4096 and
+extrapolates to N = 16384 (pure N^3 from the largest N, and a log-log fit).
 
 --impl reference times the reference's own CPU implementation of the path
 (the src/iterative.c loop, oracle port) on all host cores, on rank 0 only,
@@ -80,6 +85,8 @@ def parse_args():
     p.add_argument("--dmma-steps", type=int, default=1)
     p.add_argument("--e2e-steps", type=int, default=9)
     p.add_argument("--seed", type=int, default=20241203)
+    p.add_argument("--cpu-scaling", action="store_true",
+                   help="time the single-thread reference program at N = 1024, 2048, 4096 and exit")
     p.add_argument("--ref-gpu-kernel", type=int, default=1,
                    help="--impl reference: also time the reference's own CUDA kernel for context (1/0)")
     return p.parse_args()
@@ -554,8 +561,41 @@ def reference_gpu_context() -> dict:
         return {"unavailable": str(e).splitlines()[0]}
 
 
+def run_cpu_scaling() -> None:
+    """Single-thread CPU baseline: the reference's sequential program (index
+    inputs, one host thread) at two optimisation levels, N = 1024, 2048, 4096,
+    extrapolated to N = 16384."""
+    binr = ROOT / "hpc-multigpu-matrixmult_gb300" / "bin"
+    out = {"baseline": "reference sequential program (src/iterative.c), one host thread", "cores": 1,
+           "n_target": 16384, "builds": {}}
+    for name, exe in (("no optimisation (the reference Makefile's flags)", "iterative_noopt.out"),
+                      ("-O2", "iterative.out")):
+        pts = []
+        for n in (1024, 2048, 4096):
+            r = subprocess.run([str(binr / exe), str(n)], capture_output=True, text=True, timeout=1800)
+            if r.returncode != 0:
+                raise SystemExit(f"{exe} {n} failed: {r.stderr}")
+            pts.append((n, float(r.stdout.strip().split(",")[1])))
+        ns = np.array([p[0] for p in pts], dtype=float)
+        ts = np.array([p[1] for p in pts])
+        slope, icept = np.polyfit(np.log(ns), np.log(ts), 1)
+        t_fit = float(np.exp(icept + slope * np.log(16384.0)))
+        t_cubic = pts[-1][1] * (16384 / pts[-1][0]) ** 3
+        out["builds"][name] = {
+            "seconds": {str(n): round(t, 3) for n, t in pts},
+            "gflops": {str(n): round(2.0 * n ** 3 / t / 1e9, 3) for n, t in pts},
+            "loglog_exponent": round(float(slope), 3),
+            "n16384_seconds_cubic_from_4096": round(t_cubic, 1),
+            "n16384_seconds_loglog_fit": round(t_fit, 1),
+            "n16384_tflops_cubic_from_4096": round(2.0 * 16384 ** 3 / t_cubic / 1e12, 6)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.cpu_scaling:
+        run_cpu_scaling()
+        return
     world, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, world, rank)

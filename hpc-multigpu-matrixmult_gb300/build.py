@@ -6,7 +6,10 @@ Outputs (all git-ignored, rebuilt on the GPU host by ``__graft_entry__.build()``
 * ``lib/libphpc_summa.so``  the SUMMA layer + utils compiled against the single-rank
                              MPI shim (include/phpc_summa.h, include/phpc_utils.h).
 * ``bin/main.out``          the reference-compatible command line driver;
-* ``bin/iterative.out``     the reference's sequential timing program;
+* ``bin/iterative.out``     the reference's sequential timing program (-O2);
+* ``bin/iterative_noopt.out`` the same program at the reference Makefile's
+                             flags (gcc -Wall, no optimisation), for the
+                             single-thread CPU baseline;
 * ``bin/family.out``        a test family (tests/*.csv format) as one grouped call.
 * ``../oracle/liboracle.so`` the CPU oracle (see oracle/).
 
@@ -87,6 +90,10 @@ def build_host() -> None:
             _run(["gcc", *cflags, "-o", str(exe), str(HOST / f"{prog}.c"), f"-L{LIB}", "-lphpc_summa",
                   "-lphpc_gemm", f"-L{CUDA_HOME / 'lib64'}", "-lcudart", "-lm", "-Wl,-rpath,$ORIGIN/../lib",
                   f"-Wl,-rpath,{CUDA_HOME / 'lib64'}"])
+    noopt = BIN / "iterative_noopt.out"
+    srcs = [HOST / "iterative.c", HOST / "utils.c"]
+    if not _newer(noopt, srcs):
+        _run(["gcc", "-Wall", f"-I{INC}", "-o", str(noopt), *map(str, srcs), "-lm"])
 
 
 def build_oracle() -> None:
