@@ -189,6 +189,45 @@ def test_moduli_pairwise_coprime_and_bits():
             assert 2 * k * 2 ** (2 * b) < math.prod(mods[:nmod])
 
 
+@pytest.mark.parametrize("kind", ["uniform", "wide", "constant", "one-large", "subnormal", "zero-row"])
+def test_norm_grid_rule_bound(kind):
+    """The per-row/column grid rule: |A'_i|^2 <= M (1/2 - 1/32) exactly (so by
+    Cauchy-Schwarz every exact product fits the CRT's one-step margin), never
+    below the worst-case width, and ~3.7 bits above it for entries spread over
+    2^-20 .. 2^20."""
+    import math
+
+    import ozaki2_model
+    import ozaki_model
+
+    rng = np.random.default_rng(8)
+    m, k, nmod = 12, 1500, 13
+    a = rng.uniform(-1, 1, (m, k))
+    if kind == "wide":
+        a *= np.exp2(rng.integers(-20, 21, (m, k)))
+    elif kind == "constant":
+        a[:] = -3.25
+    elif kind == "one-large":
+        a *= 1e-8
+        a[:, 7] = 2.0
+    elif kind == "subnormal":
+        a *= 2.0 ** -1065
+    elif kind == "zero-row":
+        a[4] = 0.0
+    e = ozaki_model.exponents(a, axis=1)
+    bw = ozaki2_model.grid_widths(a, e, 1, nmod)
+    M = math.prod(ozaki2_model.MODULI[:nmod])
+    ai = ozaki2_model.to_int(a, e[:, None], bw[:, None])
+    for i in range(m):
+        assert 32 * sum(int(x) * int(x) for x in ai[i]) <= 15 * M, (kind, i)
+    assert (bw >= ozaki2_model.bits_for(nmod, k) - 1).all()
+    assert (bw <= 62).all()
+    if kind == "wide":
+        assert bw.mean() >= ozaki2_model.bits_for(nmod, k) + 3
+    if kind == "zero-row":
+        assert bw[4] == 62
+
+
 @pytest.mark.parametrize("dist,nmod,bound", [("uniform", 15, 1e-16), ("wide", 15, 1e-16), ("wide", 13, 5e-15),
                                              ("uniform", 11, 2e-13)])
 def test_crt_model_error_vs_dd_oracle(oracle, dist, nmod, bound):
