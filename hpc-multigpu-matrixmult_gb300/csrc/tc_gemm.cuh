@@ -110,6 +110,7 @@ struct TcArgs {
   uint16_t* R;                // kResidue: residue planes [pairs][M][ldr] (one 16-bit residue per element)
   int64_t ldr;                // kResidue: row stride of a residue plane in elements (multiple of 16)
   int64_t rplane;             // kResidue: plane stride in elements
+  int split_pairs;            // kResidue, one CTA per tile: a work unit is one (tile, modulus), moduli outer
 };
 
 // Grouped mode: many independent problems in one persistent launch. The
@@ -306,7 +307,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     pair_ok = peer_base == tmem_base;
     if (!pair_ok && threadIdx.x == 0) record_error(status, PHPC_ERR_UNSUPPORTED | (15 << 8));
   }
-  const int nunits = pair_ok ? ntiles : 0;
+  // kResidue: the moduli are independent, so with split_pairs a work unit is
+  // one (tile, modulus): pairs.n times as many units, for problems with too
+  // few tiles to fill the SMs evenly
+  const bool split = MODE == kResidue && !GROUPED && CLUSTER == 1 && args.split_pairs != 0;
+  const int nunits = pair_ok ? ntiles * (split ? pairs.n : 1) : 0;
   // Each role's code is dominated by its own setmaxnreg, so the compiler can
   // allocate up to kTcRegsHigh registers in the epilogue branch.
   if (warp < kTcFirstEpiWarp) {
@@ -322,10 +327,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t phase = 0;
       int issued = 0;
       bool ok = true;
-      for (int t = unit0; t < nunits && ok; t += ustride) {
+      for (int u = unit0; u < nunits && ok; u += ustride) {
+        const int t = split ? u % ntiles : u;
+        const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
         TcJob job;
         tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
-        for (int pi = 0; pi < pairs.n && ok; ++pi) {
+        for (int pi = p0; pi < p1 && ok; ++pi) {
           const int pa = pairs.a[pi], pb = pairs.b[pi];
           for (int kb = 0; kb < job.nk; ++kb) {
             if (!wait_parity(&empty[stage], phase ^ 1, status, 11)) { ok = false; break; }
@@ -368,16 +375,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t tphase[2] = {0, 0};
       int buf = 0;
       bool ok = true;
-      for (int t = unit0; t < nunits && ok; t += ustride) {
+      for (int u = unit0; u < nunits && ok; u += ustride) {
+        const int t = split ? u % ntiles : u;
+        const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
         TcJob job;
         tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
-        int gstart = 0;
-        while (gstart < pairs.n && ok) {
+        int gstart = p0;
+        while (gstart < p1 && ok) {
           int gend = gstart + 1;
           if (MODE != kF32)
-            while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
+            while (gend < p1 && pairs.g[gend] == pairs.g[gstart]) ++gend;
           else
-            gend = pairs.n;
+            gend = p1;
           const int total = (gend - gstart) * job.nk;
           const int chunk = MODE == kOzaki ? kTcChunkSteps : MODE == kResidue ? kTcResidueChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
@@ -440,7 +449,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
     for (int j = 0; j < HALF; ++j) acc[j] = 0;
 
-    for (int t = unit0; t < nunits && ok; t += ustride) {
+    for (int u = unit0; u < nunits && ok; u += ustride) {
+      const int t = split ? u % ntiles : u;
+      const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
       TcJob job;
       tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
       const int64_t row0 = (int64_t)job.rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
@@ -450,13 +461,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int64_t r = row0 + lane;
         my_ea = r < job.M ? max(job.ea[r], -20000) : -20000;
       }
-      int gstart = 0;
-      while (gstart < pairs.n && ok) {
+      int gstart = p0;
+      while (gstart < p1 && ok) {
         int gend = gstart + 1;
         if (MODE != kF32)
-          while (gend < pairs.n && pairs.g[gend] == pairs.g[gstart]) ++gend;
+          while (gend < p1 && pairs.g[gend] == pairs.g[gstart]) ++gend;
         else
-          gend = pairs.n;
+          gend = p1;
         const int total = (gend - gstart) * job.nk;
         const int chunk = MODE == kOzaki ? kTcChunkSteps : MODE == kResidue ? kTcResidueChunkSteps : kTcF32ChunkSteps;
         const int nchunks = (total + chunk - 1) / chunk;
@@ -651,6 +662,9 @@ struct TcGemmOpts {
   int64_t a_plane_rows = 0;            // rows between consecutive A planes (0: m, the planes are m rows high)
   int64_t b_plane_rows = 0;            // rows between consecutive B planes (0: n)
   int cfg_m = 0, cfg_n = 0, cfg_k = 0;  // shape whose tuning entry sets cluster and raster (0: this GEMM's)
+  int split_pairs = -1;                 // kResidue: (tile, modulus) work units; -1: when the tiles fill a
+                                        // wave of SMs and the last one less than 98 % (PHPC_SPLIT_MODULI
+                                        // = 0/1 forces)
 };
 
 // Host launcher of tc_slice_gemm_kernel (ozaki.cu) over bf16 planes

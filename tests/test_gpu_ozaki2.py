@@ -71,6 +71,23 @@ def test_bitexact_vs_model(phpc, torch_cuda, nmod, m, k, n):
     np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, nmod, grid))
 
 
+@pytest.mark.parametrize("split", ["0", "1"])
+@pytest.mark.parametrize("bn", ["128", "256"])
+def test_bitexact_split_moduli(phpc, torch_cuda, monkeypatch, split, bn):
+    """The residue GEMM's moduli as separate (tile, modulus) work units
+    (PHPC_SPLIT_MODULI=1, the default for shapes with a ragged last wave) or
+    within one unit per tile: the same bits as the model."""
+    monkeypatch.setenv("PHPC_SPLIT_MODULI", split)
+    monkeypatch.setenv("PHPC_OZAKI_BN", bn)
+    rng = np.random.default_rng(404)
+    m, k, n = 390, 700, 530
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
+    b = rng.uniform(-1, 1, (k, n))
+    c0 = rng.uniform(-1, 1, (m, n))
+    got, grid = run_dev_grid(phpc, torch_cuda, a, b, c0, 13)
+    np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, c0, 13, grid))
+
+
 @pytest.mark.parametrize("kind", ["uniform", "constant", "one-large", "subnormal"])
 def test_grids_bound_and_rule(phpc, torch_cuda, kind):
     """Grids on inputs that stress the norm bound: all entries equal (the
