@@ -83,7 +83,7 @@ def parse_args():
                    help="modular scheme with this many moduli (8..16); 0 = digit scheme; -1 = library default")
     p.add_argument("--slices", type=int, default=0, help="digit scheme slices; 0 = library default")
     p.add_argument("--dmma-steps", type=int, default=1)
-    p.add_argument("--e2e-steps", type=int, default=9)
+    p.add_argument("--e2e-steps", type=int, default=15)
     p.add_argument("--seed", type=int, default=20241203)
     p.add_argument("--cpu-scaling", action="store_true",
                    help="time the single-thread reference program at N = 1024, 2048, 4096 and exit")
