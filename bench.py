@@ -68,7 +68,7 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 # (N, "slices" | "moduli", count).
 NCU_TRAFFIC_BYTES = {(16384, "slices", 7): 426.25e9 + 15.28e9,
                      (16384, "moduli", 14): 153.23e9 + 7.52e9,
-                     (16384, "moduli", 13): 145.21e9 + 7.00e9}
+                     (16384, "moduli", 13): 112.23e9 + 7.31e9}
 UNIT = "TFLOP/s"
 
 

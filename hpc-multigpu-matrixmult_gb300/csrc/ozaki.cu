@@ -132,16 +132,15 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.ldr = ldr;
   a.rplane = rplane;
   if (MODE == kResidue && cluster == 1) {
-    // split the moduli into separate work units when the tiles fill at least
-    // one wave of SMs but leave the last wave more than 2 % short of full
-    // (N = 4096: 512 tiles, 3.4 waves, 14 % faster; N = 8192: 3 %; below
-    // one wave of tiles the split measured 2-7 % slower)
+    // split the moduli into separate work units, moduli outer, when the
+    // tiles fill at least one wave of SMs: consecutive waves then work on the
+    // same modulus and share its planes in L2, and a ragged last wave is
+    // spread over 13x more units (N = 4096: 14 % faster, DRAM traffic 2.1x ->
+    // 1.06x the algorithmic bytes; N = 8192: 3 %; N = 16384: 1-2 %, DRAM reads
+    // 145 -> 112 GB). Below one wave of tiles it measured 2-7 % slower.
     int split = opt.split_pairs;
     if (const char* env = getenv("PHPC_SPLIT_MODULI")) split = atoi(env) != 0 ? 1 : 0;
-    if (split < 0) {
-      const int64_t tiles = (int64_t)a.tm * a.tn, waves = (tiles + dev->sm_count - 1) / dev->sm_count;
-      split = (tiles >= dev->sm_count && (waves * dev->sm_count - tiles) * 50 > waves * dev->sm_count) ? 1 : 0;
-    }
+    if (split < 0) split = (int64_t)a.tm * a.tn >= dev->sm_count ? 1 : 0;
     a.split_pairs = split;
   }
   if (cluster == 1) {

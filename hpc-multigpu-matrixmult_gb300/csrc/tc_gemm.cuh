@@ -663,8 +663,7 @@ struct TcGemmOpts {
   int64_t b_plane_rows = 0;            // rows between consecutive B planes (0: n)
   int cfg_m = 0, cfg_n = 0, cfg_k = 0;  // shape whose tuning entry sets cluster and raster (0: this GEMM's)
   int split_pairs = -1;                 // kResidue: (tile, modulus) work units; -1: when the tiles fill a
-                                        // wave of SMs and the last one less than 98 % (PHPC_SPLIT_MODULI
-                                        // = 0/1 forces)
+                                        // wave of SMs (PHPC_SPLIT_MODULI = 0/1 forces)
 };
 
 // Host launcher of tc_slice_gemm_kernel (ozaki.cu) over bf16 planes
