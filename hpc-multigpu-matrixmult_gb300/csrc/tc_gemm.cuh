@@ -19,6 +19,10 @@
 //          conversion: the exact f32 chunk is reduced in FP32 (two elements
 //          per f32x2 instruction). Residues leave through the warp's scratch
 //          so that each store instruction writes four 128-byte row segments.
+//          The moduli are independent: with split_pairs a work unit is one
+//          (tile, modulus), moduli outer, so that consecutive waves of CTAs
+//          share one modulus's planes in L2 and a ragged last wave is spread
+//          over more units.
 //  kF32    3xBF16 split GEMM: all pairs accumulate into one f32 result. The
 //          tensor cores' f32 accumulation does not round to nearest, so its
 //          error grows with the number of MMAs summed; the accumulator is
