@@ -350,6 +350,10 @@ int launch_grouped_gemm(const phpc_grouped_plan* pl, cudaStream_t stream) {
   if (!dev) return PHPC_ERR_CUDA;
   TcArgs a{};
   a.status = device_status_ptr();
+  if (MODE == kResidue) {  // (tile, modulus) work units, moduli outer, unless PHPC_SPLIT_MODULI=0
+    const char* env = getenv("PHPC_SPLIT_MODULI");
+    a.split_pairs = env ? (atoi(env) != 0 ? 1 : 0) : 1;
+  }
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
   const int grid = std::min(pl->total_tiles, dev->sm_count);

@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // kResidue: the moduli are independent, so with split_pairs a work unit is
   // one (tile, modulus): pairs.n times as many units, for problems with too
   // few tiles to fill the SMs evenly
-  const bool split = MODE == kResidue && !GROUPED && CLUSTER == 1 && args.split_pairs != 0;
+  const bool split = MODE == kResidue && CLUSTER == 1 && args.split_pairs != 0;
   const int nunits = pair_ok ? ntiles * (split ? pairs.n : 1) : 0;
   // Each role's code is dominated by its own setmaxnreg, so the compiler can
   // allocate up to kTcRegsHigh registers in the epilogue branch.
