@@ -191,6 +191,24 @@ int MPI_Bcast(void *buf, int count, MPI_Datatype type, int root, MPI_Comm comm) 
   if (root != 0 || count < 0 || base_size(type) == 0) return MPI_ERR_ARG;
   return MPI_SUCCESS;
 }
+/* Non-blocking form: complete on return (there is nothing to wait for). */
+int MPI_Ibcast(void *buf, int count, MPI_Datatype type, int root, MPI_Comm comm, MPI_Request *request) {
+  if (!request) return MPI_ERR_ARG;
+  *request = MPI_REQUEST_NULL;
+  return MPI_Bcast(buf, count, type, root, comm);
+}
+int MPI_Wait(MPI_Request *request, MPI_Status *status) {
+  (void)status;
+  if (!request) return MPI_ERR_ARG;
+  *request = MPI_REQUEST_NULL;
+  return MPI_SUCCESS;
+}
+int MPI_Waitall(int count, MPI_Request requests[], MPI_Status statuses[]) {
+  (void)statuses;
+  if (count < 0 || (count > 0 && !requests)) return MPI_ERR_ARG;
+  for (int i = 0; i < count; ++i) requests[i] = MPI_REQUEST_NULL;
+  return MPI_SUCCESS;
+}
 int MPI_Reduce(const void *sendbuf, void *recvbuf, int count, MPI_Datatype type, MPI_Op op, int root, MPI_Comm comm) {
   if (!comm_ok(comm)) return MPI_ERR_COMM;
   const int bs = base_size(type);

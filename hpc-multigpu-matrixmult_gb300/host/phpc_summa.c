@@ -7,10 +7,22 @@
  * Panel t of A lives on process column t mod c, panel t of B on process row
  * t mod r. At step t the owners broadcast their panels (strided vector types
  * on the sender, contiguous buffers on the receivers) and every process adds
- * A_t * B_t into its C block with the local GEMM. Rank 0 then collects the
- * C blocks. On one rank (the `mpirun -np 1` drop-in) L = 1: one local GEMM of
- * the whole matrices, every broadcast is to itself and nothing is gathered;
- * the k-panel loop then runs on the device, inside the persistent kernel.
+ * A_t * B_t into its C block. Rank 0 then collects the C blocks.
+ *
+ * Differences from the reference's loop, same results:
+ *  - the broadcasts are non-blocking (MPI_Ibcast) into two alternating
+ *    receive buffers per operand: panel t+1 is posted before panel t is
+ *    multiplied, so it travels while the device computes;
+ *  - with more than one panel the rank's C block stays on the device for the
+ *    whole loop (phpc_panels_*: C copied in once and out once, each step
+ *    copies only its two panels), where the reference's local GEMM copies
+ *    the C block in and out at every step; the per-panel arithmetic is that
+ *    of the local GEMM, so the result is bit-identical;
+ *  - on one rank (the `mpirun -np 1` drop-in) L = 1: one local GEMM call of
+ *    the whole matrices, whose copies and compute overlap inside the call;
+ *  - a local error skips the remaining products but not the broadcasts and
+ *    the gather, so the other ranks are not left waiting; the first error is
+ *    kept for phpc_summa_last_error().
  */
 #include "phpc_summa.h"
 
@@ -39,81 +51,127 @@ static int mpi_check(int rc) {
   return rc;
 }
 
-static void summa(local_gemm_fn gemm, MPI_Comm grid, const double *A, const double *B, double *C, int N,
-                  int gpu_count, int grid_width, int grid_height, int block_width, float *seconds) {
-  int rank = 0, nprocs = 1, dims[2], periods[2], coords[2];
+static void keep_error(int rc) {
+  if (rc != PHPC_OK && t_summa_error == 0) t_summa_error = rc;
+}
+
+/* One step's panels as this rank multiplies them. */
+typedef struct {
+  const double *a, *b;
+  int lda, ldb;
+} step_panels;
+
+typedef struct {
+  int N, mr, kp, nc, row0, col0;
+  int dims[2], coords[2];
+  const double *A, *B;
+  double *abuf[2], *bbuf[2];
+  MPI_Datatype a_panel, b_panel;
+  MPI_Comm row_comm, col_comm;
+} summa_grid;
+
+/* Posts the broadcasts of panel t: the owner column sends A's rows
+ * [row0, row0 + mr) x columns [t kp, (t+1) kp) along the process row, the
+ * owner row B's rows [t kp, (t+1) kp) x columns [col0, col0 + nc) along the
+ * process column; the others receive into the buffers of parity t & 1. */
+static step_panels post_step(const summa_grid *g, int t, MPI_Request req[2]) {
+  step_panels sp;
+  const int a_owner = t % g->dims[1], b_owner = t % g->dims[0];
+  if (g->coords[1] == a_owner) {
+    sp.a = g->A + (size_t)g->row0 * g->N + (size_t)t * g->kp;
+    sp.lda = g->N;
+    mpi_check(MPI_Ibcast((void *)sp.a, 1, g->a_panel, a_owner, g->row_comm, &req[0]));
+  } else {
+    sp.a = g->abuf[t & 1];
+    sp.lda = g->kp;
+    mpi_check(MPI_Ibcast(g->abuf[t & 1], g->mr * g->kp, MPI_DOUBLE, a_owner, g->row_comm, &req[0]));
+  }
+  if (g->coords[0] == b_owner) {
+    sp.b = g->B + (size_t)t * g->kp * g->N + g->col0;
+    sp.ldb = g->N;
+    mpi_check(MPI_Ibcast((void *)sp.b, 1, g->b_panel, b_owner, g->col_comm, &req[1]));
+  } else {
+    sp.b = g->bbuf[t & 1];
+    sp.ldb = g->nc;
+    mpi_check(MPI_Ibcast(g->bbuf[t & 1], g->kp * g->nc, MPI_DOUBLE, b_owner, g->col_comm, &req[1]));
+  }
+  return sp;
+}
+
+static void summa(int method, MPI_Comm grid, const double *A, const double *B, double *C, int N, int gpu_count,
+                  int grid_width, int grid_height, int block_width, float *seconds) {
+  const local_gemm_fn gemm = method == PHPC_PANELS_CUDA ? phpc_gemm_cuda : phpc_gemm_cublas;
+  int rank = 0, nprocs = 1, periods[2];
+  summa_grid g;
   t_summa_error = 0;
   *seconds = 0.f;
   mpi_check(MPI_Comm_rank(grid, &rank));
   mpi_check(MPI_Comm_size(grid, &nprocs));
-  mpi_check(MPI_Cart_get(grid, 2, dims, periods, coords));
+  mpi_check(MPI_Cart_get(grid, 2, g.dims, periods, g.coords));
   if (t_summa_error) return;
 
+  const int steps = g.dims[0] / gcd_int(g.dims[0], g.dims[1]) * g.dims[1];
+  g.N = N;
+  g.mr = N / g.dims[0]; /* rows of my C block and of my A panels    */
+  g.kp = N / steps;     /* panel width                              */
+  g.nc = N / g.dims[1]; /* columns of my C block and of my B panels */
+  g.row0 = g.coords[0] * g.mr;
+  g.col0 = g.coords[1] * g.nc;
+  g.A = A;
+  g.B = B;
+  double *my_c = C + (size_t)g.row0 * N + g.col0;
+
+  if (steps == 1) {
+    /* 1 x 1 grid: every panel broadcast is to this rank itself */
+    float s = 0.f;
+    gemm(A, N, B, N, C, N, N, N, N, gpu_count, grid_width, grid_height, block_width, &s);
+    keep_error(phpc_last_error());
+    *seconds = s;
+    return;
+  }
+
   const int keep_cols[2] = {0, 1}, keep_rows[2] = {1, 0};
-  MPI_Comm row_comm, col_comm;
-  mpi_check(MPI_Cart_sub(grid, keep_cols, &row_comm)); /* the processes of my grid row    */
-  mpi_check(MPI_Cart_sub(grid, keep_rows, &col_comm)); /* the processes of my grid column */
-
-  const int steps = dims[0] / gcd_int(dims[0], dims[1]) * dims[1];
-  const int mr = N / dims[0];  /* rows of my C block and of my A panels    */
-  const int kp = N / steps;    /* panel width                              */
-  const int nc = N / dims[1];  /* columns of my C block and of my B panels */
-
-  /* The first A panel this process owns is panel coords[1]; its next one is
-   * dims[1] panels further right. Likewise for B, dims[0] panels further down. */
-  const double *my_a = A + (size_t)coords[0] * mr * N + (size_t)coords[1] * kp;
-  const double *my_b = B + (size_t)coords[0] * kp * N + (size_t)coords[1] * nc;
-  double *my_c = C + (size_t)coords[0] * mr * N + (size_t)coords[1] * nc;
-
-  double *recv_a = NULL, *recv_b = NULL;
-  if (dims[1] > 1) recv_a = (double *)malloc(sizeof(double) * (size_t)mr * kp);
-  if (dims[0] > 1) recv_b = (double *)malloc(sizeof(double) * (size_t)kp * nc);
-
-  MPI_Datatype a_panel, b_panel, c_block;
-  mpi_check(MPI_Type_vector(mr, kp, N, MPI_DOUBLE, &a_panel));
-  mpi_check(MPI_Type_vector(kp, nc, N, MPI_DOUBLE, &b_panel));
-  mpi_check(MPI_Type_vector(mr, nc, N, MPI_DOUBLE, &c_block));
-  mpi_check(MPI_Type_commit(&a_panel));
-  mpi_check(MPI_Type_commit(&b_panel));
+  mpi_check(MPI_Cart_sub(grid, keep_cols, &g.row_comm)); /* the processes of my grid row    */
+  mpi_check(MPI_Cart_sub(grid, keep_rows, &g.col_comm)); /* the processes of my grid column */
+  for (int i = 0; i < 2; ++i) {
+    g.abuf[i] = g.dims[1] > 1 ? (double *)malloc(sizeof(double) * (size_t)g.mr * g.kp) : NULL;
+    g.bbuf[i] = g.dims[0] > 1 ? (double *)malloc(sizeof(double) * (size_t)g.kp * g.nc) : NULL;
+    if ((g.dims[1] > 1 && !g.abuf[i]) || (g.dims[0] > 1 && !g.bbuf[i])) keep_error(PHPC_ERR_NOMEM);
+  }
+  MPI_Datatype c_block;
+  mpi_check(MPI_Type_vector(g.mr, g.kp, N, MPI_DOUBLE, &g.a_panel));
+  mpi_check(MPI_Type_vector(g.kp, g.nc, N, MPI_DOUBLE, &g.b_panel));
+  mpi_check(MPI_Type_vector(g.mr, g.nc, N, MPI_DOUBLE, &c_block));
+  mpi_check(MPI_Type_commit(&g.a_panel));
+  mpi_check(MPI_Type_commit(&g.b_panel));
   mpi_check(MPI_Type_commit(&c_block));
 
-  for (int t = 0; t < steps && !t_summa_error; ++t) {
-    const int a_owner = t % dims[1], b_owner = t % dims[0];
-    const double *pa, *pb;
-    int lda, ldb;
-    if (coords[1] == a_owner) {
-      pa = my_a;
-      lda = N;
-      my_a += (size_t)dims[1] * kp;
-      mpi_check(MPI_Bcast((void *)pa, 1, a_panel, a_owner, row_comm));
-    } else {
-      pa = recv_a;
-      lda = kp;
-      mpi_check(MPI_Bcast(recv_a, mr * kp, MPI_DOUBLE, a_owner, row_comm));
-    }
-    if (coords[0] == b_owner) {
-      pb = my_b;
-      ldb = N;
-      my_b += (size_t)dims[0] * kp * N;
-      mpi_check(MPI_Bcast((void *)pb, 1, b_panel, b_owner, col_comm));
-    } else {
-      pb = recv_b;
-      ldb = nc;
-      mpi_check(MPI_Bcast(recv_b, kp * nc, MPI_DOUBLE, b_owner, col_comm));
-    }
-    if (t_summa_error) break;
-    float step_seconds = 0.f;
-    gemm(pa, lda, pb, ldb, my_c, N, mr, kp, nc, gpu_count, grid_width, grid_height, block_width, &step_seconds);
-    const int rc = phpc_last_error();
-    if (rc != PHPC_OK && t_summa_error == 0) t_summa_error = rc;
-    *seconds += step_seconds;
+  phpc_panels *acc = NULL;
+  if (!t_summa_error)
+    keep_error(phpc_panels_begin(&acc, method, my_c, N, g.mr, g.nc, g.kp, gpu_count, grid_width, grid_height,
+                                 block_width));
+
+  /* step t: wait for panel t, post panel t+1, multiply panel t */
+  MPI_Request req[2][2];
+  step_panels cur = post_step(&g, 0, req[0]);
+  for (int t = 0; t < steps; ++t) {
+    mpi_check(MPI_Waitall(2, req[t & 1], MPI_STATUSES_IGNORE));
+    step_panels next = cur;
+    if (t + 1 < steps) next = post_step(&g, t + 1, req[(t + 1) & 1]);
+    if (acc && !t_summa_error) keep_error(phpc_panels_add(acc, cur.a, cur.lda, cur.b, cur.ldb, g.kp));
+    cur = next;
+  }
+  if (acc) {
+    float s = 0.f;
+    keep_error(phpc_panels_end(acc, &s));
+    if (!t_summa_error) *seconds = s;
   }
 
   if (rank == 0) {
-    for (int p = 1; p < nprocs && !t_summa_error; ++p) {
+    for (int p = 1; p < nprocs; ++p) {
       int pc[2];
       mpi_check(MPI_Cart_coords(grid, p, 2, pc));
-      mpi_check(MPI_Recv(C + (size_t)pc[0] * mr * N + (size_t)pc[1] * nc, 1, c_block, p, 0, grid,
+      mpi_check(MPI_Recv(C + (size_t)pc[0] * g.mr * N + (size_t)pc[1] * g.nc, 1, c_block, p, 0, grid,
                          MPI_STATUS_IGNORE));
     }
   } else {
@@ -121,20 +179,22 @@ static void summa(local_gemm_fn gemm, MPI_Comm grid, const double *A, const doub
   }
 
   MPI_Type_free(&c_block);
-  MPI_Type_free(&b_panel);
-  MPI_Type_free(&a_panel);
-  free(recv_b);
-  free(recv_a);
-  MPI_Comm_free(&row_comm);
-  MPI_Comm_free(&col_comm);
+  MPI_Type_free(&g.b_panel);
+  MPI_Type_free(&g.a_panel);
+  for (int i = 0; i < 2; ++i) {
+    free(g.bbuf[i]);
+    free(g.abuf[i]);
+  }
+  MPI_Comm_free(&g.row_comm);
+  MPI_Comm_free(&g.col_comm);
 }
 
 void phpc_gemm_summa_cuda(MPI_Comm grid_comm, const double *A, const double *B, double *C, int n, int gpu_count,
                           int grid_width, int grid_height, int block_width, float *compute_time) {
-  summa(phpc_gemm_cuda, grid_comm, A, B, C, n, gpu_count, grid_width, grid_height, block_width, compute_time);
+  summa(PHPC_PANELS_CUDA, grid_comm, A, B, C, n, gpu_count, grid_width, grid_height, block_width, compute_time);
 }
 
 void phpc_gemm_summa_cublas(MPI_Comm grid_comm, const double *A, const double *B, double *C, int n, int gpu_count,
                             float *compute_time) {
-  summa(phpc_gemm_cublas, grid_comm, A, B, C, n, gpu_count, 0, 0, 0, compute_time);
+  summa(PHPC_PANELS_CUBLAS, grid_comm, A, B, C, n, gpu_count, 0, 0, 0, compute_time);
 }

@@ -118,6 +118,10 @@ _lib.phpc_grouped_graph_launch.argtypes = [ct.c_void_p, ct.c_void_p]
 _lib.phpc_grouped_graph_launch.restype = ct.c_int
 _lib.phpc_grouped_plan_destroy.argtypes = [ct.c_void_p]
 _lib.phpc_grouped_plan_destroy.restype = None
+_lib.phpc_panels_begin.argtypes = [ct.POINTER(ct.c_void_p), ct.c_int, ct.c_void_p, ct.c_int, ct.c_int, ct.c_int,
+                                   ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+_lib.phpc_panels_add.argtypes = [ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_int]
+_lib.phpc_panels_end.argtypes = [ct.c_void_p, ct.POINTER(ct.c_float)]
 
 
 class PhpcError(RuntimeError):
@@ -177,6 +181,42 @@ def gemm_host(method: str, a: np.ndarray, b: np.ndarray, c: np.ndarray, grid_wid
     if method == "ozaki":
         return gemm_cublas(a, k, b, n, c, n, m, k, n, 1)
     raise ValueError(method)
+
+
+def _rows(x: np.ndarray) -> tuple[int, int]:
+    """(address, leading dimension) of a float64 matrix with unit column stride."""
+    if x.dtype != np.float64 or x.ndim != 2 or (x.shape[1] > 1 and x.strides[1] != 8) or x.strides[0] % 8:
+        raise TypeError("float64 row-major matrix (unit column stride) required")
+    return x.ctypes.data, x.strides[0] // 8
+
+
+class PanelAccumulator:
+    """phpc_panels_*: a host C block kept on the device across k-panel updates
+    C += A_t @ B_t ('dmma' as phpc_gemm_cuda, 'ozaki' as phpc_gemm_cublas).
+    `c` is written back by end(); panels may be strided views (unit column
+    stride)."""
+
+    def __init__(self, method: str, c: np.ndarray, max_k: int, gpu_count=1, grid_width=1, grid_height=1,
+                 block_width=32):
+        if method not in ("dmma", "ozaki"):
+            raise ValueError(method)
+        self._c = c
+        ptr, ldc = _rows(c)
+        self._h = ct.c_void_p()
+        _check(_lib.phpc_panels_begin(ct.byref(self._h), 0 if method == "dmma" else 1, ptr, ldc, c.shape[0],
+                                      c.shape[1], max_k, gpu_count, grid_width, grid_height, block_width),
+               "phpc_panels_begin")
+
+    def add(self, a: np.ndarray, b: np.ndarray) -> None:
+        pa, lda = _rows(a)
+        pb, ldb = _rows(b)
+        _check(_lib.phpc_panels_add(self._h, pa, lda, pb, ldb, a.shape[1]), "phpc_panels_add")
+
+    def end(self) -> float:
+        t = ct.c_float(0.0)
+        h, self._h = self._h, None
+        _check(_lib.phpc_panels_end(h, ct.byref(t)), "phpc_panels_end")
+        return t.value
 
 
 # --------------------------------------------------------------- device API

@@ -21,6 +21,7 @@ extern "C" {
 typedef int MPI_Comm;
 typedef int MPI_Datatype;
 typedef int MPI_Op;
+typedef int MPI_Request;
 typedef struct {
   int MPI_SOURCE, MPI_TAG, MPI_ERROR;
 } MPI_Status;
@@ -38,6 +39,8 @@ typedef struct {
 #define MPI_SUM 1
 #define MPI_IN_PLACE ((void *)1)
 #define MPI_STATUS_IGNORE ((MPI_Status *)0)
+#define MPI_STATUSES_IGNORE ((MPI_Status *)0)
+#define MPI_REQUEST_NULL 0
 
 int MPI_Init(int *argc, char ***argv);
 int MPI_Finalize(void);
@@ -55,6 +58,9 @@ int MPI_Type_vector(int count, int blocklength, int stride, MPI_Datatype old, MP
 int MPI_Type_commit(MPI_Datatype *type);
 int MPI_Type_free(MPI_Datatype *type);
 int MPI_Bcast(void *buf, int count, MPI_Datatype type, int root, MPI_Comm comm);
+int MPI_Ibcast(void *buf, int count, MPI_Datatype type, int root, MPI_Comm comm, MPI_Request *request);
+int MPI_Wait(MPI_Request *request, MPI_Status *status);
+int MPI_Waitall(int count, MPI_Request requests[], MPI_Status statuses[]);
 int MPI_Reduce(const void *sendbuf, void *recvbuf, int count, MPI_Datatype type, MPI_Op op, int root, MPI_Comm comm);
 int MPI_Send(const void *buf, int count, MPI_Datatype type, int dest, int tag, MPI_Comm comm);
 int MPI_Recv(void *buf, int count, MPI_Datatype type, int source, int tag, MPI_Comm comm, MPI_Status *status);

@@ -72,6 +72,35 @@ void phpc_gemm_cuda(const double *a, int lda, const double *b, int ldb, double *
 void phpc_gemm_cublas(const double *a, int lda, const double *b, int ldb, double *c, int ldc, int m, int k, int n,
                       int gpu_count, int grid_width, int grid_height, int block_width, float *gpu_time);
 
+/*
+ * Device-resident C block for a sequence of k-panel updates: the SUMMA step
+ * loop of one rank (reference src/phpc_summa.c:63-95), which calls the local
+ * GEMM once per panel (src/phpc_summa.c:93) and so copies the rank's C block
+ * to the device and back at every step. phpc_panels_begin copies C (m x n,
+ * leading dimension ldc) to the device once. Each phpc_panels_add copies one
+ * A panel (m x k, lda) and one B panel (k x n, ldb), k <= max_k, into one of
+ * two device panel buffers and queues C += A * B; it returns as soon as both
+ * host panels have been copied (the caller may then reuse them), with the
+ * product possibly still running, so that the next panel's exchange between
+ * ranks overlaps it. phpc_panels_end waits for the last product, copies C
+ * back, releases everything and reports the products' device time in
+ * seconds. PHPC_PANELS_CUDA computes each panel as phpc_gemm_cuda does (same
+ * argument checks and logical grid_width x grid_height block grid),
+ * PHPC_PANELS_CUBLAS as phpc_gemm_cublas does (the FP64-accurate Ozaki GEMM
+ * for the panel's shape; a panel holding inf/NaN in IEEE FP64), so the result
+ * is bit-identical to calling that function once per panel. Errors are
+ * sticky: after a failed add the later adds do nothing, and phpc_panels_end
+ * returns the first error and leaves the host C unchanged. Not re-entrant:
+ * one accumulator at a time per device, as for the calls above.
+ */
+#define PHPC_PANELS_CUDA 0
+#define PHPC_PANELS_CUBLAS 1
+typedef struct phpc_panels phpc_panels;
+int phpc_panels_begin(phpc_panels **acc, int method, double *c, int ldc, int m, int n, int max_k, int gpu_count,
+                      int grid_width, int grid_height, int block_width);
+int phpc_panels_add(phpc_panels *acc, const double *a, int lda, const double *b, int ldb, int k);
+int phpc_panels_end(phpc_panels *acc, float *seconds);
+
 /* ---------------------------------------------- device-pointer entry points */
 
 /* Plain FP64 GEMM (phpc_gemm_cuda's kernel; DFMA pipe, or DMMA with

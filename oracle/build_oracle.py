@@ -8,6 +8,14 @@
   and ``-Dmain=phpc_ref_iterative_main`` so that its CLI entry point does not
   clash; it exports the reference's phpc_gemm_iterative(A, B, C, n).
   tests/golden/make_golden.py calls it to produce the golden vectors.
+* ``oracle/libsumma_threads.so``: this library's SUMMA layer
+  (hpc-multigpu-matrixmult_gb300/host/phpc_summa.c) linked with the
+  thread-per-rank MPI (mpi_threads.c) and the CPU local GEMM of
+  summa_threads.c, for the multi-rank SUMMA tests on CPU.
+* ``oracle/_ref/libref_summa_threads.so`` (only where the reference sources
+  are present): the reference's own src/phpc_summa.c, compiled unchanged from
+  where it lies, in the same harness; tests/golden/make_summa_golden.py runs
+  it to produce the multi-rank SUMMA golden vectors.
 * ``oracle/_ref/ref_phpc_gemm.cubin`` (same condition): the device code of the
   reference's src/phpc_gemm.cu (its ``gemm_kernel``) compiled unchanged for
   sm_103a (``nvcc -cubin``); a device-only image that runs on the GPU host
@@ -23,6 +31,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 REF_SRC = Path(os.environ.get("PHPC_REFERENCE_DIR", "/root/reference")) / "src"
 REF_OUT = HERE / "_ref"
+INCLUDE = HERE.parent / "include"
 
 
 def _run(cmd: list[str]) -> None:
@@ -41,6 +50,20 @@ def build() -> None:
     if _stale(so, [src]):
         _run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", str(so), str(src), "-lm",
               "-lpthread"])
+    harness = [HERE / "mpi_threads.c", HERE / "summa_threads.c"]
+    hflags = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-Wl,-Bsymbolic",
+              f"-I{HERE / 'mpi_threads'}", f"-I{INCLUDE}"]
+    summa_src = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "host" / "phpc_summa.c"
+    so = HERE / "libsumma_threads.so"
+    hdeps = harness + [HERE / "mpi_threads" / "mpi.h", INCLUDE / "phpc_gemm.h", INCLUDE / "phpc_summa.h"]
+    if _stale(so, hdeps + [summa_src]):
+        _run([*hflags, "-o", str(so), str(summa_src), *map(str, harness), "-lpthread"])
+    if (REF_SRC / "phpc_summa.c").exists():
+        REF_OUT.mkdir(exist_ok=True)
+        ref_so = REF_OUT / "libref_summa_threads.so"
+        if _stale(ref_so, hdeps + [REF_SRC / "phpc_summa.c"]):
+            _run([*hflags, "-Wno-unused-variable", "-o", str(ref_so), str(REF_SRC / "phpc_summa.c"),
+                  *map(str, harness), "-lpthread"])
     if (REF_SRC / "iterative.c").exists():
         REF_OUT.mkdir(exist_ok=True)
         ref_so = REF_OUT / "libref_iterative.so"

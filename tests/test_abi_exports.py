@@ -66,3 +66,23 @@ def test_argument_validation_needs_no_gpu(phpc):
     assert L.phpc_ozaki_workspace_bytes(0, 4, 4, 7) == 0
     assert L.phpc_ozaki_workspace_bytes(64, 64, 64, 7) > 2 * 7 * 64 * 64 * 2
     assert phpc.error_string(4) == "bounded device wait expired"
+
+
+def test_panel_accumulator_argument_errors_need_no_gpu(phpc):
+    """phpc_panels_* reject invalid arguments before any device work."""
+    import ctypes as ct
+
+    L = phpc.lib()
+    h = ct.c_void_p()
+    c = (ct.c_double * 4)()
+    assert L.phpc_panels_begin(None, 0, c, 2, 2, 2, 2, 1, 1, 1, 32) == 1  # no handle
+    assert L.phpc_panels_begin(ct.byref(h), 2, c, 2, 2, 2, 2, 1, 1, 1, 32) == 1  # no such method
+    assert L.phpc_panels_begin(ct.byref(h), 0, c, 2, 2, 2, 2, 1, 1, 1, 33) == 1  # block_width > 32
+    assert L.phpc_panels_begin(ct.byref(h), 0, c, 2, 2, 2, 2, 1, 0, 1, 32) == 1  # grid_width < 1
+    assert L.phpc_panels_begin(ct.byref(h), 1, c, 2, 2, 2, 2, 0, 0, 0, 0) == 1  # gpu_count < 1
+    assert L.phpc_panels_begin(ct.byref(h), 1, c, 1, 2, 2, 2, 1, 0, 0, 0) == 1  # ldc < n
+    assert L.phpc_panels_begin(ct.byref(h), 1, None, 2, 2, 2, 2, 1, 0, 0, 0) == 1  # no C
+    assert h.value is None
+    assert L.phpc_panels_add(None, None, 0, None, 0, 0) == 1
+    assert L.phpc_panels_end(None, None) == 1
+    assert L.phpc_last_error() == 1

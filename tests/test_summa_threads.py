@@ -1,0 +1,143 @@
+"""Multi-rank SUMMA on CPU: the SUMMA layer on r x c grids of thread ranks.
+
+host/phpc_summa.c (this library's SUMMA layer, built as
+oracle/libsumma_threads.so with the thread-per-rank MPI of
+oracle/mpi_threads.c and the reference's CPU loop as local GEMM) against:
+
+* the golden vectors of tests/golden/summa_golden.json, made by the
+  reference's own src/phpc_summa.c in the same harness
+  (tests/golden/make_summa_golden.py), bit for bit;
+* the reference's SUMMA itself, where its harness library was built here;
+* oracle_gemm_iterative on the whole matrices: applying the k panels in order
+  with that loop adds every product into C in the same order, so the SUMMA
+  result is bit-identical to it.
+
+Also: the time each rank reports is the sum over its steps; with more than one
+panel every rank keeps its C block in one panel accumulator (phpc_panels_*)
+instead of calling the local GEMM per step; a local failure on one rank leaves
+the other ranks' blocks correct and every rank finishes (no rank is left
+waiting in a broadcast or the gather); argument errors reach every rank.
+"""
+import ctypes as ct
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import summa_harness as H
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+PHPC_ERR_ARG, PHPC_ERR_NOMEM = 1, 8
+
+
+@pytest.fixture(scope="module")
+def ours(built):
+    return H.load(H.OURS)
+
+
+@pytest.fixture(scope="module")
+def reference(built):
+    if not H.REFERENCE.exists():
+        pytest.skip("the reference's SUMMA harness is built only where the reference sources exist")
+    return H.load(H.REFERENCE)
+
+
+def oracle_product(a, b, c0):
+    from oracle_py import lib as oracle_lib  # oracle/oracle_py.py
+
+    dp = ct.POINTER(ct.c_double)
+    c = np.ascontiguousarray(c0, dtype=np.float64).copy()
+    f = oracle_lib().oracle_gemm_iterative
+    f.argtypes = [dp, dp, dp, ct.c_int]
+    f(np.ascontiguousarray(a).ctypes.data_as(dp), np.ascontiguousarray(b).ctypes.data_as(dp), c.ctypes.data_as(dp),
+      a.shape[0])
+    return c
+
+
+def sha(x):
+    return hashlib.sha256(np.ascontiguousarray(x).tobytes()).hexdigest()
+
+
+CASES = json.loads((GOLDEN / "summa_golden.json").read_text())
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+@pytest.mark.parametrize("method", [0, 1], ids=["cuda", "cublas"])
+def test_summa_matches_reference_golden(ours, case, method):
+    a, b, c0 = H.inputs(case["n"], case["seed"], case["dist"])
+    assert (sha(a), sha(b), sha(c0)) == (case["sha_a"], case["sha_b"], case["sha_c0"])
+    res = H.run(ours, method, case["rows"], case["cols"], a, b, c0)
+    assert res.status == 0
+    assert not res.summa_error.any()
+    golden = np.load(GOLDEN / case["npy"])
+    assert sha(golden) == case["sha_c"]
+    assert np.array_equal(res.c, golden)
+    # every rank reports the sum of its steps' times, as the reference's ranks do
+    assert res.seconds.tolist() == case["seconds"]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_reference_summa_reproduces_golden(reference, case):
+    a, b, c0 = H.inputs(case["n"], case["seed"], case["dist"])
+    res = H.run(reference, 0, case["rows"], case["cols"], a, b, c0)
+    assert res.status == 0
+    assert sha(res.c) == case["sha_c"]
+    assert res.calls.tolist() == case["calls"]
+
+
+@pytest.mark.parametrize("grid", [(1, 1), (2, 2), (2, 4), (4, 2), (3, 3), (2, 6), (6, 2), (5, 3), (1, 8), (8, 8)],
+                         ids=str)
+def test_summa_matches_oracle_loop(ours, oracle, grid):
+    r, c = grid
+    n = 120 if r * c <= 16 else 64  # divisible by r, c and lcm(r, c) for every grid above
+    a, b, c0 = H.inputs(n, 7000 + 10 * r + c, "wide")
+    res = H.run(ours, 1, r, c, a, b, c0)
+    assert res.status == 0 and not res.summa_error.any()
+    assert np.array_equal(res.c, oracle_product(a, b, c0))
+
+
+@pytest.mark.parametrize("grid", [(1, 1), (2, 3), (4, 4)], ids=str)
+def test_summa_keeps_c_on_device_across_panels(ours, grid):
+    r, c = grid
+    a, b, c0 = H.inputs(24, 1, "uniform")
+    res = H.run(ours, 0, r, c, a, b, c0)
+    L = H.steps(r, c)
+    assert res.status == 0
+    if L == 1:  # one local GEMM call of the whole matrices
+        assert res.calls.tolist() == [1] and res.adds.tolist() == [0]
+    else:  # one accumulator per rank, one panel added per step, no per-step local GEMM calls
+        assert res.calls.tolist() == [0] * (r * c) and res.adds.tolist() == [L] * (r * c)
+    assert np.all(res.seconds == np.float32(L * H.STEP_SECONDS))
+
+
+@pytest.mark.parametrize("method", [0, 1], ids=["cuda", "cublas"])
+def test_failure_on_one_rank_leaves_others_correct(ours, oracle, method):
+    """Rank 4 of a 3 x 3 grid fails to set up its local GEMM (an allocation
+    failure made on the host): it still takes part in every broadcast and in
+    the gather, so every rank finishes; its block keeps C0 and reports the
+    error, the other blocks are the product."""
+    r = c = 3
+    n = 36
+    a, b, c0 = H.inputs(n, 11, "uniform")
+    res = H.run(ours, method, r, c, a, b, c0, fail_rank=4)
+    assert res.status == 0  # no rank timed out, no message or broadcast left over
+    expect_err = [PHPC_ERR_NOMEM if p == 4 else 0 for p in range(9)]
+    assert res.summa_error.tolist() == expect_err
+    want = oracle_product(a, b, c0)
+    mr, nc = n // r, n // c
+    blk = (slice(1 * mr, 2 * mr), slice(1 * nc, 2 * nc))  # rank 4 = coordinates (1, 1)
+    assert np.array_equal(res.c[blk], c0[blk])
+    mask = np.ones((n, n), bool)
+    mask[blk] = False
+    assert np.array_equal(res.c[mask], want[mask])
+
+
+def test_argument_error_reaches_every_rank(ours):
+    a, b, c0 = H.inputs(24, 3, "uniform")
+    res = H.run(ours, 0, 2, 3, a, b, c0, block_width=0)  # block_width must be 1..32
+    assert res.status == 0
+    assert res.summa_error.tolist() == [PHPC_ERR_ARG] * 6
+    assert np.array_equal(res.c, c0)
+    assert res.adds.tolist() == [0] * 6
