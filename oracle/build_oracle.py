@@ -12,6 +12,10 @@
   (hpc-multigpu-matrixmult_gb300/host/phpc_summa.c) linked with the
   thread-per-rank MPI (mpi_threads.c) and the CPU local GEMM of
   summa_threads.c, for the multi-rank SUMMA tests on CPU.
+* ``oracle/libmain_threads.so``: this library's command-line driver
+  (host/main.c as ``phpc_cli_main``, host/utils.c) on the same harness, with
+  main_threads.c's stubs for its two outside calls, to run it as a multi-rank
+  job on CPU.
 * ``oracle/_ref/libref_summa_threads.so`` (only where the reference sources
   are present): the reference's own src/phpc_summa.c, compiled unchanged from
   where it lies, in the same harness; tests/golden/make_summa_golden.py runs
@@ -51,13 +55,27 @@ def build() -> None:
         _run(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", str(so), str(src), "-lm",
               "-lpthread"])
     harness = [HERE / "mpi_threads.c", HERE / "summa_threads.c"]
-    hflags = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-Wl,-Bsymbolic",
-              f"-I{HERE / 'mpi_threads'}", f"-I{INCLUDE}"]
+    cflags = ["-O2", "-ffp-contract=off", "-fPIC", "-Wall", f"-I{HERE / 'mpi_threads'}", f"-I{INCLUDE}"]
+    hflags = ["gcc", *cflags, "-shared", "-Wl,-Bsymbolic"]
     summa_src = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "host" / "phpc_summa.c"
     so = HERE / "libsumma_threads.so"
     hdeps = harness + [HERE / "mpi_threads" / "mpi.h", INCLUDE / "phpc_gemm.h", INCLUDE / "phpc_summa.h"]
     if _stale(so, hdeps + [summa_src]):
         _run([*hflags, "-o", str(so), str(summa_src), *map(str, harness), "-lpthread"])
+    cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
+    if (cuda_inc / "cuda_runtime_api.h").exists():
+        host = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "host"
+        cli_so = HERE / "libmain_threads.so"
+        cli_srcs = [host / "main.c", host / "utils.c", summa_src, *harness, HERE / "main_threads.c"]
+        if _stale(cli_so, hdeps + cli_srcs + [INCLUDE / "phpc_utils.h"]):
+            objs = []
+            for src in cli_srcs:
+                obj = HERE / "_build" / (src.stem + ".o")
+                obj.parent.mkdir(exist_ok=True)
+                extra = ["-Dmain=phpc_cli_main"] if src.name == "main.c" else []
+                _run(["gcc", *cflags, f"-I{cuda_inc}", *extra, "-c", "-o", str(obj), str(src)])
+                objs.append(obj)
+            _run(["gcc", "-shared", "-Wl,-Bsymbolic", "-o", str(cli_so), *map(str, objs), "-lm", "-lpthread"])
     if (REF_SRC / "phpc_summa.c").exists():
         REF_OUT.mkdir(exist_ok=True)
         ref_so = REF_OUT / "libref_summa_threads.so"

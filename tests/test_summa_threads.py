@@ -17,6 +17,9 @@ panel every rank keeps its C block in one panel accumulator (phpc_panels_*)
 instead of calling the local GEMM per step; a local failure on one rank leaves
 the other ranks' blocks correct and every rank finishes (no rank is left
 waiting in a broadcast or the gather); argument errors reach every rank.
+Last, the command-line driver (host/main.c) runs as a job of 1 to 8 ranks:
+process grid, CSV row and file name, device times averaged over ranks, the
+exact index-input check, and its collective error exits.
 """
 import ctypes as ct
 import hashlib
@@ -141,3 +144,62 @@ def test_argument_error_reaches_every_rank(ours):
     assert res.summa_error.tolist() == [PHPC_ERR_ARG] * 6
     assert np.array_equal(res.c, c0)
     assert res.adds.tolist() == [0] * 6
+
+
+# ---- the command-line driver as a multi-rank job ----------------------------
+# host/main.c runs as phpc_cli_main on thread ranks (oracle/libmain_threads.so),
+# in a child process whose working directory receives csv/.
+
+_CLI = """
+import ctypes as ct, sys
+L = ct.CDLL(sys.argv[1])
+args = [b"main.out"] + [a.encode() for a in sys.argv[3:]]
+argv = (ct.c_char_p * (len(args) + 1))(*args, None)
+sys.exit(L.main_threads_run(int(sys.argv[2]), len(args), argv))
+"""
+
+
+def _run_cli(tmp_path, procs, *args, dist="index"):
+    import os
+    import subprocess
+    import sys
+
+    lib = H.ROOT / "oracle" / "libmain_threads.so"
+    if not lib.exists():
+        pytest.skip("libmain_threads.so needs the CUDA runtime headers to build")
+    env = dict(os.environ, PHPC_DIST=dist)
+    return subprocess.run([sys.executable, "-c", _CLI, str(lib), str(procs), *map(str, args)], cwd=tmp_path,
+                          env=env, capture_output=True, text=True, timeout=120)
+
+
+@pytest.mark.parametrize("procs,grid", [(1, (1, 1)), (4, (2, 2)), (6, (3, 2)), (8, (4, 2))], ids=str)
+def test_main_out_multi_rank(built, tmp_path, procs, grid):
+    """The driver's process grid (1 x 1 for one rank, MPI_Dims_create
+    otherwise), the 9-column row with the process count, device times averaged
+    over the ranks (each rank reports lcm(r, c) steps), and the exact
+    closed-form check of the reference's index inputs on the gathered C."""
+    n, tw, gw, gh = 24, 16, 2, 3
+    r = _run_cli(tmp_path, procs, n, tw, gw, gh, "mr")
+    assert r.returncode == 0, r.stderr
+    stem = f"mr_N{n}_T{procs}_G1_TW{tw}_GW{gw}_GH{gh}"
+    row = (tmp_path / "csv" / f"{stem}.csv").read_text().strip().split(",")
+    assert len(row) == 9
+    assert [int(x) for x in row[:6]] == [n, procs, 1, gw * gh, tw * tw, gw * gh * tw * tw]
+    steps = H.steps(*grid)
+    assert float(row[7]) == pytest.approx(steps * H.STEP_SECONDS)
+    ext = (tmp_path / "csv" / f"{stem}_ext.csv").read_text().strip().splitlines()
+    assert ext[0] == "method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err"
+    for line, method in zip(ext[1:], ("dmma", "ozaki_split")):
+        f = line.split(",")
+        assert f[0] == method and int(f[1]) == n
+        assert float(f[3]) == pytest.approx(steps * H.STEP_SECONDS)
+        assert float(f[5]) == 0.0 and float(f[6]) == 0.0
+
+
+def test_main_out_multi_rank_divisibility_and_usage(built, tmp_path):
+    r = _run_cli(tmp_path, 4, 25, 16, 2, 2, "bad")  # 2 x 2 grid, 25 not divisible
+    assert r.returncode == 1
+    assert "must be divisible by process grid dimensions (2 x 2)" in r.stderr
+    r = _run_cli(tmp_path, 6, 24, 16, 2, 2)  # missing test name
+    assert r.returncode == 1 and "Usage:" in r.stderr
+    assert not (tmp_path / "csv").exists() or not any((tmp_path / "csv").iterdir())
