@@ -184,7 +184,10 @@ def gemm_host(method: str, a: np.ndarray, b: np.ndarray, c: np.ndarray, grid_wid
 
 
 def _rows(x: np.ndarray) -> tuple[int, int]:
-    """(address, leading dimension) of a float64 matrix with unit column stride."""
+    """(address, leading dimension) of a float64 matrix with unit column stride
+    (an array without elements: its column count)."""
+    if x.dtype == np.float64 and x.ndim == 2 and x.size == 0:
+        return x.ctypes.data, x.shape[1]
     if x.dtype != np.float64 or x.ndim != 2 or (x.shape[1] > 1 and x.strides[1] != 8) or x.strides[0] % 8:
         raise TypeError("float64 row-major matrix (unit column stride) required")
     return x.ctypes.data, x.strides[0] // 8
