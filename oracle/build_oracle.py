@@ -10,8 +10,9 @@
   tests/golden/make_golden.py calls it to produce the golden vectors.
 * ``oracle/libsumma_threads.so``: this library's SUMMA layer
   (hpc-multigpu-matrixmult_gb300/host/phpc_summa.c) linked with the
-  thread-per-rank MPI (mpi_threads.c) and the CPU local GEMM of
-  summa_threads.c, for the multi-rank SUMMA tests on CPU.
+  thread-per-rank MPI (mpi_threads.c), the CPU local GEMM of
+  summa_threads.c and the MPI-rule checks of mpi_threads_check.c, for the
+  multi-rank SUMMA tests on CPU.
 * ``oracle/libmain_threads.so``: this library's command-line driver
   (host/main.c as ``phpc_cli_main``, host/utils.c) on the same harness, with
   main_threads.c's stubs for its two outside calls, to run it as a multi-rank
@@ -60,8 +61,9 @@ def build() -> None:
     summa_src = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "host" / "phpc_summa.c"
     so = HERE / "libsumma_threads.so"
     hdeps = harness + [HERE / "mpi_threads" / "mpi.h", INCLUDE / "phpc_gemm.h", INCLUDE / "phpc_summa.h"]
-    if _stale(so, hdeps + [summa_src]):
-        _run([*hflags, "-o", str(so), str(summa_src), *map(str, harness), "-lpthread"])
+    check = HERE / "mpi_threads_check.c"
+    if _stale(so, hdeps + [summa_src, check]):
+        _run([*hflags, "-o", str(so), str(summa_src), *map(str, harness), str(check), "-lpthread"])
     cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
     if (cuda_inc / "cuda_runtime_api.h").exists():
         host = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "host"

@@ -66,6 +66,15 @@ def sha(x):
 CASES = json.loads((GOLDEN / "summa_golden.json").read_text())
 
 
+@pytest.mark.parametrize("grid", [(1, 1), (2, 3), (3, 2), (4, 4), (1, 5), (5, 1), (8, 8)], ids=str)
+def test_thread_ranks_follow_mpi_rules(ours, grid):
+    """The harness's MPI against the standard's rules for the calls used here
+    (oracle/mpi_threads_check.c: Dims_create, Cartesian coordinates and
+    sub-communicators, strided / contiguous broadcasts, non-blocking
+    broadcasts, tag matching, reductions); 0 = every check passed."""
+    assert ours.mpi_threads_check(*grid) == 0
+
+
 @pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
 @pytest.mark.parametrize("method", [0, 1], ids=["cuda", "cublas"])
 def test_summa_matches_reference_golden(ours, case, method):
