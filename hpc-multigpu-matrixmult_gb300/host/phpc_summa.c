@@ -77,6 +77,7 @@ typedef struct {
 static step_panels post_step(const summa_grid *g, int t, MPI_Request req[2]) {
   step_panels sp;
   const int a_owner = t % g->dims[1], b_owner = t % g->dims[0];
+  req[0] = req[1] = MPI_REQUEST_NULL; /* what MPI_Waitall sees if a post fails */
   if (g->coords[1] == a_owner) {
     sp.a = g->A + (size_t)g->row0 * g->N + (size_t)t * g->kp;
     sp.lda = g->N;
