@@ -7,6 +7,7 @@ Used to reproduce single launches for profiling (ncu) and timing:
     python hpc-multigpu-matrixmult_gb300/run_case.py --method dmma --n 2048
     python hpc-multigpu-matrixmult_gb300/run_case.py --method bf16x3 --m 32768 --n 8192 --k 4096
     python hpc-multigpu-matrixmult_gb300/run_case.py --method grouped --count 512
+    python hpc-multigpu-matrixmult_gb300/run_case.py --method summa_rank --n 16384 --grid 2x2
 
 FP64 methods (ozaki, ozaki2, dmma) use A_ij = u * 2^e (u uniform [-1, 1), e uniform
 in [emin, emax]) from the library's device generator; FP32 methods (bf16x3,
@@ -28,7 +29,11 @@ sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 def main() -> int:
     p = argparse.ArgumentParser()
-    p.add_argument("--method", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma", "grouped"], default="ozaki")
+    p.add_argument("--method", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma", "grouped", "summa_rank"],
+                   default="ozaki")
+    p.add_argument("--grid", default="2x2", help="summa_rank: process grid r x c")
+    p.add_argument("--rank-method", choices=["ozaki", "dmma"], default="ozaki",
+                   help="summa_rank: phpc_gemm_cublas or phpc_gemm_cuda as the local GEMM")
     p.add_argument("--count", type=int, default=512, help="grouped: number of problems")
     p.add_argument("--n", type=int, default=4096)
     p.add_argument("--m", type=int, default=0)
@@ -48,6 +53,8 @@ def main() -> int:
 
     if a.method == "grouped":
         return run_grouped(a, torch, phpc)
+    if a.method == "summa_rank":
+        return run_summa_rank(a, torch, phpc)
     n = a.n
     m = a.m or n
     k = a.k or n
@@ -193,6 +200,71 @@ def run_grouped(a, torch, phpc) -> int:
                       "per_problem_dmma_ms": round(t_dmma, 3), "per_problem_dmma_tflops": round(flops / t_dmma / 1e9, 3),
                       "grouped_frob_rel_err_max_over_8": max(errs), "status": status}))
     return 0 if status == 0 else 1
+
+
+def run_summa_rank(a, torch, phpc) -> int:
+    """Rank (0, 0) of the SUMMA on an r x c grid at N: its L = lcm(r, c) panel
+    steps on its (N/r) x (N/c) C block, with host panels (strided views of
+    its rows of A and columns of B, as an owner sends them), run (1) as the
+    reference's loop does, one local GEMM call per step on host buffers (the
+    C block copied in and out by every call), and (2) through the panel
+    accumulator (C block resident on the device, only the panels copied per
+    step). Each variant runs once untimed, then once timed by the wall clock;
+    prints both times, their FP64-equivalent rates and whether the two
+    results are bitwise equal."""
+    import math
+    import time
+
+    import numpy as np
+
+    r, c = (int(x) for x in a.grid.lower().split("x"))
+    n = a.n
+    L = r // math.gcd(r, c) * c
+    if n % L:
+        raise SystemExit(f"N = {n} is not divisible by lcm({r}, {c}) = {L}")
+    mr, kp, nc = n // r, n // L, n // c
+    st = torch.cuda.current_stream()
+    dA = torch.empty((mr, n), dtype=torch.float64, device="cuda")
+    dB = torch.empty((n, nc), dtype=torch.float64, device="cuda")
+    phpc.fill_wide_dev(dA, mr * n, 1, 0, a.emin, a.emax, st)
+    phpc.fill_wide_dev(dB, n * nc, 2, 0, a.emin, a.emax, st)
+    A = dA.cpu().numpy()
+    B = dB.cpu().numpy()
+    del dA, dB
+    C0 = np.random.default_rng(3).uniform(-1.0, 1.0, (mr, nc))
+    local = phpc.gemm_cublas if a.rank_method == "ozaki" else phpc.gemm_cuda
+
+    def per_step_calls():
+        C = C0.copy()
+        dev = 0.0
+        t0 = time.perf_counter()
+        for t in range(L):
+            dev += local(A[:, t * kp:], n, B[t * kp:], nc, C, nc, mr, kp, nc)
+        return C, (time.perf_counter() - t0) * 1e3, dev * 1e3
+
+    def accumulator():
+        C = C0.copy()
+        t0 = time.perf_counter()
+        acc = phpc.PanelAccumulator(a.rank_method, C, kp)
+        for t in range(L):
+            acc.add(A[:, t * kp:(t + 1) * kp], B[t * kp:(t + 1) * kp])
+        dev = acc.end()
+        return C, (time.perf_counter() - t0) * 1e3, dev * 1e3
+
+    per_step_calls()
+    accumulator()
+    c1, ms1, dev1 = per_step_calls()
+    c2, ms2, dev2 = accumulator()
+    flops = 2.0 * mr * nc * n
+    status = phpc.device_status()
+    print(json.dumps({"method": "summa_rank", "local_gemm": a.rank_method, "grid": f"{r}x{c}", "n": n, "steps": L,
+                      "block": [mr, nc], "panel_k": kp,
+                      "per_step_calls_ms": round(ms1, 2), "per_step_calls_tflops": round(flops / ms1 / 1e9, 3),
+                      "per_step_calls_device_ms": round(dev1, 2),
+                      "accumulator_ms": round(ms2, 2), "accumulator_tflops": round(flops / ms2 / 1e9, 3),
+                      "accumulator_device_ms": round(dev2, 2),
+                      "bitwise_equal": bool(np.array_equal(c1, c2)), "status": status}))
+    return 0 if status == 0 and np.array_equal(c1, c2) else 1
 
 
 if __name__ == "__main__":
