@@ -1,7 +1,8 @@
 /*
  * oracle.c - CPU oracle for the GEMM hot path. TEST INFRASTRUCTURE ONLY:
  * used by tests/, __graft_entry__.smoke() and the cpu_baseline / reference
- * legs of bench.py as the checker and the CPU baseline, never by the product.
+ * legs of bench.py as the reference result and the CPU baseline, never by the
+ * product.
  *
  * Parity pins: oracle_gemm_iterative is checked bit-for-bit against outputs of
  * the reference's own src/iterative.c (compiled from the reference sources by
