@@ -58,6 +58,17 @@ def test_single_rank_cartesian_and_collectives(summa_lib):
     assert list(buf) == [1, 2, 3, 4]
     assert summa_lib.MPI_Bcast(buf, 4, 2, 1, comm.value) != 0  # root 1 does not exist
     assert summa_lib.MPI_Send(buf, 4, 2, 1, 0, comm.value) != 0
+    # non-blocking broadcast: complete at once, the request becomes MPI_REQUEST_NULL (0)
+    req = (ct.c_int * 2)(-5, -5)
+    assert summa_lib.MPI_Ibcast(buf, 4, 2, 0, comm.value, ct.byref(req, 0)) == 0
+    assert summa_lib.MPI_Ibcast(buf, 4, 2, 0, comm.value, ct.byref(req, 4)) == 0
+    assert list(req) == [0, 0] and list(buf) == [1, 2, 3, 4]
+    req[0] = 7
+    assert summa_lib.MPI_Waitall(2, req, None) == 0 and list(req) == [0, 0]
+    one = ct.c_int(3)
+    assert summa_lib.MPI_Wait(ct.byref(one), None) == 0 and one.value == 0
+    assert summa_lib.MPI_Ibcast(buf, 4, 2, 1, comm.value, ct.byref(one)) != 0  # root 1 does not exist
+    assert summa_lib.MPI_Ibcast(buf, 4, 2, 0, comm.value, None) != 0  # no request
 
 
 def test_generators_deterministic_and_in_range(summa_lib):
