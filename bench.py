@@ -31,18 +31,28 @@ Reported (one JSON line on rank 0):
   other_scheme  the digit (or modular) scheme on the same inputs, for context.
   cpu_baseline  the reference's CPU loop (src/iterative.c:8-13, oracle port)
              on all host cores, on a bounded sample of rows of the same product.
+  rect_fp32 / batched  the other two measured workloads, after the timed
+             region (workloads.py): the FP32-accurate 3xBF16 GEMM at
+             M=32768 N=8192 K=4096 against the FP32 FFMA kernel, and 512
+             FP64-accurate GEMMs of log-uniform shapes as one grouped CUDA
+             graph against one plain FP64 launch per GEMM; each with its
+             errors against a higher-precision reference.
 
+--impl reference times the reference's own CPU implementation of the path
+(the src/iterative.c loop, oracle port) on all host cores, on rank 0 only, on
+rows of the same product with the same seeded inputs (the generator restated
+in the oracle); it loads no library of this project and uses no GPU.
+Multi-GPU (torchrun): every rank runs an independent replica (the GEMM path
+has no exchange on a one-GPU-per-process node); value = total work / max time.
+
+Other modes (one JSON line each): --peaks (throughput of the arithmetic pipes:
+DFMA, the FP64 tensor-core mma.sync shapes, IMMA, FFMA), --case METHOD (one
+method at one size, for profiling one launch), --summa-rank RxC (one SUMMA
+rank's panel steps, per-step calls against the panel accumulator).
 --cpu-scaling (opt-in, a few minutes of CPU) times the reference's sequential
 program (bin/iterative.out at -O2 and bin/iterative_noopt.out at the
 reference Makefile's flags) on one core at N = 1024, 2048, 4096 and
 extrapolates to N = 16384 (pure N^3 from the largest N, and a log-log fit).
-
---impl reference times the reference's own CPU implementation of the path
-(the src/iterative.c loop, oracle port) on all host cores, on rank 0 only,
-and adds the reference's own CUDA kernel (src/phpc_gemm.cu, compiled
-unchanged for sm_103a) at configs 1-2 as context.
-Multi-GPU (torchrun): every rank runs an independent replica (the GEMM path
-has no exchange on a one-GPU-per-process node); value = total work / max time.
 """
 from __future__ import annotations
 
@@ -63,9 +73,8 @@ sys.path.insert(0, str(ROOT / "hpc-multigpu-matrixmult_gb300"))
 METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel err≤1e-14"
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
-# dominant kernel, from a one-pass ncu capture of this workload
-# (profiles/dram_traffic_tc_slice_gemm_n16384.md); keyed by
-# (N, "slices" | "moduli", count).
+# dominant kernel, from a one-pass ncu capture of this workload on a GB300;
+# keyed by (N, "slices" | "moduli", count).
 NCU_TRAFFIC_BYTES = {(16384, "slices", 7): 426.25e9 + 15.28e9,
                      (16384, "moduli", 14): 153.23e9 + 7.52e9,
                      (16384, "moduli", 13): 112.23e9 + 7.31e9}
@@ -87,8 +96,19 @@ def parse_args():
     p.add_argument("--seed", type=int, default=20241203)
     p.add_argument("--cpu-scaling", action="store_true",
                    help="time the single-thread reference program at N = 1024, 2048, 4096 and exit")
-    p.add_argument("--ref-gpu-kernel", type=int, default=1,
-                   help="--impl reference: also time the reference's own CUDA kernel for context (1/0)")
+    p.add_argument("--configs", type=int, default=1,
+                   help="also run the rectangular FP32 and the batched workloads after the timed region (1/0)")
+    p.add_argument("--peaks", action="store_true", help="throughput probes of the arithmetic pipes, then exit")
+    p.add_argument("--case", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma"], default=None,
+                   help="time one method at one size (--m/--k/--n, --reps) and exit")
+    p.add_argument("--m", type=int, default=0)
+    p.add_argument("--k", type=int, default=0)
+    p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--check-rows", type=int, default=0)
+    p.add_argument("--grid", default="1x1", help="--case dmma: logical SUMMA block grid (width x height)")
+    p.add_argument("--summa-rank", default=None, metavar="RxC",
+                   help="one SUMMA rank's panel steps on an r x c process grid at --n, then exit")
+    p.add_argument("--rank-method", choices=["ozaki", "dmma"], default="ozaki")
     return p.parse_args()
 
 
@@ -174,6 +194,18 @@ def reduce_max(x: float, world: int, device=None) -> float:
 def replica_throughput(flops_per_rank: float, seconds_per_step: float, world: int) -> float:
     """Whole-job TFLOP/s of `world` independent replicas: total work / slowest rank's time."""
     return world * flops_per_rank / seconds_per_step / 1e12
+
+
+DATA = "synthetic: seeded A_ij, B_ij = u*2^e, u~U[-1,1), e~U{-20..20} (counter-based generator)"
+
+
+def workload_config(n: int, world: int) -> dict:
+    """The `config` of both arms' JSON lines (the same workload, whichever
+    implementation runs it)."""
+    return {"workload": f"FP64-accurate GEMM C += A B, square N={n}, wide-exponent inputs",
+            "m": n, "n": n, "k": n, "inputs": "A, B wide-exponent; C accumulated",
+            "parallelism": f"replicas x{world}" if world > 1 else "single process",
+            "l2": "inputs larger than L2 (3 x 2 GiB FP64 operands per step)"}
 
 
 def ozaki_pairs(s: int) -> int:
@@ -426,12 +458,11 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None,
         "dtype": ("f64 (bf16 residue products, exact f32/int32 accumulation, CRT, f64 rounding)" if sch.moduli
                   else "f64 (bf16 digit products, int32/f32 exact accumulation, f64 fold)"),
-        "data": "synthetic: seeded A_ij = u*2^e, u~U[-1,1), e~U{-20..20} (device generator)",
-        "config": {"workload": f"Ozaki FP64-accurate GEMM C += A B ({sch.name}), N={n}, wide-exponent inputs",
-                   "m": n, "n": n, "k": n, "scheme": "modular" if sch.moduli else "digits",
-                   "moduli": sch.moduli, "slices": sch.slices, "tensor_core_gemms": sch.gemms,
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (3 x 2 GiB FP64 operands + split planes per step)"},
+        "data": DATA,
+        "config": workload_config(n, world),
+        "method": {"name": f"Ozaki split GEMM on tcgen05 ({sch.name})",
+                   "scheme": "modular" if sch.moduli else "digits", "moduli": sch.moduli, "slices": sch.slices,
+                   "tensor_core_gemms": sch.gemms},
         "dmma_tflops": round(flops / dmma_s / 1e12, 4),
         "dmma_ms": round(dmma_s * 1e3, 1),
         "split_vs_dmma": round(value / world / (flops / dmma_s / 1e12), 2),
@@ -470,7 +501,19 @@ def run_ours(args, world, rank, local):
     }
     if rank == 0 and world == 1:
         result["cpu_baseline"] = cpu_baseline(n, seed, an, bn)
+    del Ah, Bh, Ch, an, bn, cn
+    if rank == 0 and args.configs:
+        import workloads
+
+        torch.cuda.empty_cache()
+        for key, fn in (("rect_fp32", lambda: workloads.rect_fp32(torch, phpc)),
+                        ("batched", lambda: workloads.batched(torch, phpc))):
+            try:
+                result[key] = fn()
+            except (torch.OutOfMemoryError, phpc.PhpcError) as e:
+                result[key] = {"unavailable": str(e).splitlines()[0]}
     if world > 1:
+        torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -505,14 +548,21 @@ def cpu_baseline(n, seed, a_host, b_host) -> dict:
 
 
 def run_reference(args, world, rank):
+    """The reference's own CPU implementation of the path (the i-j-k loop of
+    src/iterative.c:8-13, oracle port) on all host cores, on rows of the same
+    product as the other arm: the same seeded inputs (the library's generator
+    restated in the oracle), the same config. No library of this project is
+    loaded and no GPU is used."""
     if rank != 0:
         return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py
+
     n = args.n
     threads = os.cpu_count() or 1
-    rng = np.random.default_rng(args.seed)
     rows_max = 32 * threads
-    a = rng.uniform(-1, 1, (rows_max, n)) * np.exp2(rng.integers(-20, 21, (rows_max, n)))
-    b = rng.uniform(-1, 1, (n, n)) * np.exp2(rng.integers(-20, 21, (n, n)))
+    a = oracle_py.fill((rows_max, n), args.seed, 0, -20, 20)
+    b = oracle_py.fill((n, n), args.seed + 1, 0, -20, 20)
     for _ in range(args.warmup):
         reference_sample(n, a, b, threads, target_s=0.2)
     vals, samples = [], []
@@ -528,37 +578,58 @@ def run_reference(args, world, rank):
         "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total / args.steps * 1e3, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-        "data": "synthetic: seeded A_ij = u*2^e, u~U[-1,1), e~U{-20..20} (numpy)",
-        "config": {"workload": f"reference CPU GEMM loop (src/iterative.c:8-13) on rows of the N={n} product",
-                   "m": n, "n": n, "k": n, "parallelism": f"{threads} host threads, row blocks"},
+        "data": DATA,
+        "config": workload_config(n, world),
+        "method": {"name": "reference CPU GEMM loop (src/iterative.c:8-13), oracle port, rows split over "
+                           f"{threads} host threads"},
         "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{rows} rows of the N={n} product per step, {dt:.2f} s"},
+                         "sample": f"{rows} rows of the N={n} product per step (each step a bounded sample of "
+                                   f"the workload), {dt:.2f} s"},
         "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
-    if args.ref_gpu_kernel:
-        result["reference_gpu_kernel"] = reference_gpu_context()
     print(json.dumps(result), flush=True)
 
 
-def reference_gpu_context() -> dict:
-    """Context only (not the arm's value): the reference's own CUDA kernel
-    (src/phpc_gemm.cu gemm_kernel, compiled unchanged for sm_103a) at config 1
-    (N = 1024, 32 x 32 tiles, grid 1 x 1) and config 2's N = 4096 with the 2 x 2
-    and 4 x 4 grids, plus a grid covering every 32 x 32 tile at once."""
-    try:
-        import torch
+def run_peaks(args) -> None:
+    import torch
+    import phpc
+    import workloads
 
-        if not torch.cuda.is_available():
-            return {"unavailable": "no CUDA device"}
-        sys.path.insert(0, str(ROOT / "oracle"))
-        import ref_gpu_kernel
+    torch.cuda.init()
+    sm = torch.cuda.get_device_properties(0).multi_processor_count
+    with ClockSampler(0) as clocks:
+        out = workloads.pipe_peaks(phpc, sm)
+    print(json.dumps({"probe": "arithmetic pipe throughput (register-only loops, CUDA events)", "sm_count": sm,
+                      "pipes": out, "clocks": clocks.summary()}), flush=True)
 
-        cfgs = [(1024, 32, 1, 1), (4096, 32, 2, 2), (4096, 32, 4, 4), (4096, 32, 128, 128)]
-        return {"kernel": "reference gemm_kernel (SIMT FP64, shared-memory tiles)",
-                "runs": ref_gpu_kernel.time_reference_kernel(cfgs)}
-    except (FileNotFoundError, RuntimeError, OSError, ImportError) as e:
-        return {"unavailable": str(e).splitlines()[0]}
+
+def run_case(args) -> None:
+    import torch
+    import phpc
+    import workloads
+
+    n = args.n
+    gw, gh = (int(x) for x in args.grid.lower().split("x"))
+    r = workloads.single_case(torch, phpc, args.case, args.m or n, args.k or n, n, reps=args.reps,
+                              slices=args.slices or 7, moduli=args.moduli if args.moduli > 0 else 13,
+                              check_rows=args.check_rows, grid=(gw, gh))
+    r["fp64_pipe"] = os.environ.get("PHPC_FP64_PIPE", "default")
+    print(json.dumps(r), flush=True)
+    if r["status"] != 0:
+        raise SystemExit(1)
+
+
+def run_summa_rank(args) -> None:
+    import torch
+    import phpc
+    import workloads
+
+    r, c = (int(x) for x in args.summa_rank.lower().split("x"))
+    out = workloads.summa_rank(torch, phpc, args.n, r, c, args.rank_method)
+    print(json.dumps(out), flush=True)
+    if out["status"] != 0 or not out["bitwise_equal"]:
+        raise SystemExit(1)
 
 
 def run_cpu_scaling() -> None:
@@ -595,6 +666,15 @@ def main():
     args = parse_args()
     if args.cpu_scaling:
         run_cpu_scaling()
+        return
+    if args.peaks:
+        run_peaks(args)
+        return
+    if args.case:
+        run_case(args)
+        return
+    if args.summa_rank:
+        run_summa_rank(args)
         return
     world, rank, local = dist_env()
     if args.impl == "reference":

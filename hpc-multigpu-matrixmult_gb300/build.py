@@ -36,7 +36,7 @@ OBJ = PKG / "_build"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["runtime.cu", "dmma_gemm.cu", "ozaki.cu", "capi.cu", "tune.cu", "refgemm.cu", "bf16x3.cu", "grouped.cu", "ozaki2.cu", "panels.cu"]
+CU_SOURCES = ["runtime.cu", "dmma_gemm.cu", "ozaki.cu", "capi.cu", "tune.cu", "refgemm.cu", "bf16x3.cu", "grouped.cu", "ozaki2.cu", "panels.cu", "peaks.cu"]
 
 
 def _run(cmd: list[str]) -> None:

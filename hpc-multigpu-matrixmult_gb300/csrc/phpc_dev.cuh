@@ -104,18 +104,6 @@ __device__ __forceinline__ void tma_load_3d(void* smem_dst, const void* tmap, in
       : "memory");
 }
 
-// Same load, delivered to the same shared-memory offset of every CTA in
-// cta_mask (thread-block cluster), each destination's mbarrier at the same
-// offset receiving the bytes.
-__device__ __forceinline__ void tma_load_3d_multicast(void* smem_dst, const void* tmap, int32_t x, int32_t y,
-                                                      int32_t z, uint64_t* bar, uint16_t cta_mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%2, %3, %4}], [%5], %6;" ::"r"(smem_u32(smem_dst)),
-      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)), "h"(cta_mask)
-      : "memory");
-}
-
 // ------------------------------------------------------------------ cluster
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;

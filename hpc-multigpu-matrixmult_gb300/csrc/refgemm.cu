@@ -17,10 +17,15 @@
 namespace phpc {
 namespace {
 
+// Every operation of TwoSum and TwoProduct is written as an explicitly rounded
+// intrinsic: nvcc contracts a plain `a * b` followed by `+` into one fused
+// multiply-add (-fmad=true is its default), which would make p differ from
+// the rounded product that the error term e = fma(a, b, -p) is computed
+// against, and the pair (p, e) would no longer sum to a*b exactly.
 __device__ __forceinline__ void two_sum(double a, double b, double& s, double& t) {
-  s = a + b;
-  const double z = s - a;
-  t = (a - (s - z)) + (b - z);
+  s = __dadd_rn(a, b);
+  const double z = __dsub_rn(s, a);
+  t = __dadd_rn(__dsub_rn(a, __dsub_rn(s, z)), __dsub_rn(b, z));
 }
 
 __global__ void dd_rows_kernel(int k, int n, const double* __restrict__ A, int64_t lda, const double* __restrict__ B,
@@ -35,14 +40,14 @@ __global__ void dd_rows_kernel(int k, int n, const double* __restrict__ A, int64
   for (int y = 0; y < k; ++y) {
     const double av = a[y];
     const double bv = B[(int64_t)y * ldb + j];
-    const double p = av * bv;
-    const double e = fma(av, bv, -p);
+    const double p = __dmul_rn(av, bv);
+    const double e = __fma_rn(av, bv, -p);
     double s, t;
     two_sum(hi, p, s, t);
     hi = s;
-    lo += t + e;
+    lo = __dadd_rn(lo, __dadd_rn(t, e));
   }
-  R[(int64_t)r * ldr + j] = hi + lo;
+  R[(int64_t)r * ldr + j] = __dadd_rn(hi, lo);
 }
 
 __device__ __forceinline__ uint64_t mix64(uint64_t x) {

@@ -120,8 +120,9 @@ int default_bn(int m, int k, int n) {
   return 256;
 }
 
-// CTAs per cluster of the single-problem slice GEMM (1, or 2 = B multicast
-// between vertically adjacent tiles): PHPC_CLUSTER, else the table, else 1.
+// CTAs per cluster of the single-problem slice GEMM (1, or 2 = a CTA pair
+// computing one 256-row tile with cta_group::2 MMAs, each CTA loading its own
+// half of the operands): PHPC_CLUSTER, else the table, else 1.
 int default_cluster(int m, int k, int n) {
   const char* env = getenv("PHPC_CLUSTER");
   if (env && (atoi(env) == 1 || atoi(env) == 2)) return atoi(env);

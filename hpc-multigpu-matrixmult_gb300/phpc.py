@@ -94,6 +94,9 @@ _lib.phpc_ozaki2_grids.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_
 _lib.phpc_ozaki2_grids.restype = ct.c_int
 _lib.phpc_default_moduli.argtypes = [ct.c_int, ct.c_int, ct.c_int]
 _lib.phpc_default_moduli.restype = ct.c_int
+_lib.phpc_pipe_probe.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_float),
+                                 ct.POINTER(ct.c_double)]
+_lib.phpc_pipe_probe.restype = ct.c_int
 
 
 class GemmProblem(ct.Structure):
@@ -390,6 +393,18 @@ def grouped_shapes(count=512, seed=5, lo=64, hi=2048, multiple=16):
     x = np.exp(rng.uniform(np.log(lo), np.log(hi), (count, 3)))
     x = np.maximum(multiple, np.rint(x / multiple) * multiple).astype(int)
     return [tuple(int(v) for v in row) for row in x]
+
+
+PIPE_PROBES = {0: "DFMA", 1: "DMMA m8n8k4", 2: "DMMA m16n8k4", 3: "DMMA m16n8k8", 4: "DMMA m16n8k16",
+               5: "IMMA m16n8k32 s8", 6: "FFMA", 7: "DFMA + DMMA m16n8k4 (half the warps each)"}
+
+
+def pipe_probe(kind: int, blocks: int, threads: int, iters: int, iters2: int = 0) -> tuple[float, float]:
+    """phpc_pipe_probe: (milliseconds, flops) of one register-only throughput launch."""
+    ms, fl = ct.c_float(0.0), ct.c_double(0.0)
+    _check(_lib.phpc_pipe_probe(kind, blocks, threads, iters, iters2, ct.byref(ms), ct.byref(fl)),
+           "phpc_pipe_probe")
+    return ms.value, fl.value
 
 
 def device_status() -> int:

@@ -254,6 +254,17 @@ int phpc_dgemm_dd_rows_dev(int m, int k, int n, const double *dA, int64_t lda, c
 int phpc_fill_uniform_dev(double *dx, size_t n, uint64_t seed, uint64_t offset, void *stream);
 int phpc_fill_wide_dev(double *dx, size_t n, uint64_t seed, uint64_t offset, int emin, int emax, void *stream);
 
+/* Throughput probe of one arithmetic pipe (no reference counterpart: the
+ * reference reports no rates; its report only quotes wall times). Runs a
+ * register-only loop of `iters` iterations on `blocks` x `threads` threads
+ * (threads a multiple of 32) and returns the device time of the launch in
+ * *ms and its work in *flops (2 per multiply-add). kind: 0 DFMA (8 chains per
+ * thread), 1-4 FP64 tensor-core mma.sync m8n8k4 / m16n8k4 / m16n8k8 /
+ * m16n8k16 (4 accumulator tiles per warp), 5 INT8 mma.sync m16n8k32, 6 FFMA,
+ * 7 even warps DFMA for iters2 iterations and odd warps DMMA m16n8k4 for
+ * iters. Synchronous; allocates a sink of blocks * threads doubles. */
+int phpc_pipe_probe(int kind, int blocks, int threads, int64_t iters, int64_t iters2, float *ms, double *flops);
+
 /* Last kernel status of the calling thread's device (reads and clears the
  * device status word; synchronises the device). */
 int phpc_device_status(void);

@@ -1,8 +1,8 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 * ``oracle/liboracle.so`` from oracle/oracle.c (gcc -O2 -ffp-contract=off).
-* ``oracle/_ref/libref_iterative.so`` (only where the reference sources are
-  present, i.e. not on the GPU host): the reference's own src/iterative.c and
+* ``oracle/_ref/libref_iterative.so`` (only where PHPC_REFERENCE_DIR names a
+  checkout of the reference sources; the GPU host has none): the reference's own src/iterative.c and
   src/utils.c compiled unchanged from where they lie, with the reference
   Makefile's flags (Makefile:9: gcc ... -Wall, no optimisation) plus -fPIC,
   and ``-Dmain=phpc_ref_iterative_main`` so that its CLI entry point does not
@@ -34,7 +34,9 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_SRC = Path(os.environ.get("PHPC_REFERENCE_DIR", "/root/reference")) / "src"
+# The reference checkout (its src/ is compiled unchanged into _ref/); the
+# _ref parts are skipped when PHPC_REFERENCE_DIR is unset or has no sources.
+REF_SRC = Path(os.environ.get("PHPC_REFERENCE_DIR", "")) / "src" if os.environ.get("PHPC_REFERENCE_DIR") else None
 REF_OUT = HERE / "_ref"
 INCLUDE = HERE.parent / "include"
 
@@ -78,13 +80,13 @@ def build() -> None:
                 _run(["gcc", *cflags, f"-I{cuda_inc}", *extra, "-c", "-o", str(obj), str(src)])
                 objs.append(obj)
             _run(["gcc", "-shared", "-Wl,-Bsymbolic", "-o", str(cli_so), *map(str, objs), "-lm", "-lpthread"])
-    if (REF_SRC / "phpc_summa.c").exists():
+    if REF_SRC and (REF_SRC / "phpc_summa.c").exists():
         REF_OUT.mkdir(exist_ok=True)
         ref_so = REF_OUT / "libref_summa_threads.so"
         if _stale(ref_so, hdeps + [REF_SRC / "phpc_summa.c"]):
             _run([*hflags, "-Wno-unused-variable", "-o", str(ref_so), str(REF_SRC / "phpc_summa.c"),
                   *map(str, harness), "-lpthread"])
-    if (REF_SRC / "iterative.c").exists():
+    if REF_SRC and (REF_SRC / "iterative.c").exists():
         REF_OUT.mkdir(exist_ok=True)
         ref_so = REF_OUT / "libref_iterative.so"
         deps = [REF_SRC / "iterative.c", REF_SRC / "utils.c"]
@@ -92,7 +94,7 @@ def build() -> None:
             _run(["gcc", "-Wall", "-fPIC", "-shared", "-Dmain=phpc_ref_iterative_main", f"-I{REF_SRC}", "-o",
                   str(ref_so), *map(str, deps)])
     nvcc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "bin" / "nvcc"
-    if (REF_SRC / "phpc_gemm.cu").exists() and nvcc.exists():
+    if REF_SRC and (REF_SRC / "phpc_gemm.cu").exists() and nvcc.exists():
         REF_OUT.mkdir(exist_ok=True)
         cubin = REF_OUT / "ref_phpc_gemm.cubin"
         deps = [REF_SRC / "phpc_gemm.cu", REF_SRC / "phpc_gemm.cuh"]

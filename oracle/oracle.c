@@ -79,6 +79,33 @@ int oracle_gemm_iterative_rows_mt(int m, int k, int n, const double *A, int64_t 
   return started;
 }
 
+/* ---- seeded inputs ---------------------------------------------------------
+ * The counter-based generator the library uses for its benchmark inputs
+ * (phpc_fill_uniform / phpc_fill_wide of phpc_utils.h, and their device
+ * versions), restated here so that the CPU arms of the benchmark can make the
+ * same inputs without loading the library: element i of stream `seed` is
+ * built from h = mix(mix(seed) + offset + i), mix the splitmix64 output
+ * function (Steele, Lea and Flood, "Fast splittable pseudorandom number
+ * generators", OOPSLA 2014); u = (top 53 bits of h - 2^52) * 2^-52, uniform
+ * on [-1, 1); with emin <= emax, x = u * 2^e, e = emin + mix(h) mod
+ * (emax - emin + 1). */
+static uint64_t oracle_mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+void oracle_fill(double *x, size_t n, uint64_t seed, uint64_t offset, int emin, int emax) {
+  const uint64_t key = oracle_mix64(seed);
+  for (size_t i = 0; i < n; ++i) {
+    const uint64_t h = oracle_mix64(key + offset + i);
+    double v = (double)((int64_t)(h >> 11) - ((int64_t)1 << 52)) * 0x1p-52;
+    if (emin <= emax) v = ldexp(v, emin + (int)(oracle_mix64(h) % (uint64_t)(emax - emin + 1)));
+    x[i] = v;
+  }
+}
+
 /* ---- higher-precision oracle: double-double accumulation ------------------
  * TwoSum (Knuth) and TwoProduct via fma (Ogita, Rump and Oishi, "Accurate sum
  * and dot product", SIAM J. Sci. Comput. 26(6), 2005, Algorithm 3.1 / 3.3):

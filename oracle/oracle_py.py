@@ -34,6 +34,8 @@ def lib() -> ct.CDLL:
         L.oracle_gemm_dd_rows.argtypes = [ct.c_int, ct.c_int, _dp, ct.c_int64, _dp, ct.c_int64, _dp, ct.c_int64,
                                           ct.POINTER(ct.c_int), ct.c_int, _dp, ct.c_int64]
         L.oracle_error_terms.argtypes = [ct.c_int, ct.c_int, _dp, ct.c_int64, _dp, ct.c_int64, _dp]
+        L.oracle_fill.argtypes = [_dp, ct.c_size_t, ct.c_uint64, ct.c_uint64, ct.c_int, ct.c_int]
+        L.oracle_fill.restype = None
         _LIB = L
     return _LIB
 
@@ -73,6 +75,15 @@ def gemm_dd(a: np.ndarray, b: np.ndarray, c0: np.ndarray | None = None, rows=Non
     lib().oracle_gemm_dd_rows(k, n, _p(a), k, _p(b), n, c0p, n, rows.ctypes.data_as(ct.POINTER(ct.c_int)),
                               len(rows), _p(out), n)
     return out
+
+
+def fill(shape, seed: int, offset: int = 0, emin: int = 1, emax: int = 0) -> np.ndarray:
+    """Seeded inputs of the library's generator: uniform [-1, 1) (emin > emax)
+    or u * 2^e with e uniform in [emin, emax]; element i of the flattened
+    array is element offset + i of stream `seed`."""
+    x = np.empty(shape, dtype=np.float64)
+    lib().oracle_fill(_p(x), x.size, seed, offset, emin, emax)
+    return x
 
 
 def rel_errors(c: np.ndarray, ref: np.ndarray) -> dict:

@@ -1,4 +1,4 @@
-"""The reference's own GPU kernel, timed for context (test infrastructure).
+"""The reference's own GPU kernel (test infrastructure).
 
 Loads ``oracle/_ref/ref_phpc_gemm.cubin`` (the reference's src/phpc_gemm.cu
 device code, compiled unchanged for sm_103a by build_oracle.py) through the
@@ -6,7 +6,8 @@ CUDA driver API and launches its ``gemm_kernel(A, B, C, M, N, K)`` exactly as
 the reference's host wrapper does (src/phpc_gemm.cu:82-84,116): a
 grid_width x grid_height grid of tile_width x tile_width threads with
 2 * tile_width^2 doubles of dynamic shared memory, on dense row-major device
-matrices, C += A * B. Only ``bench.py --impl reference`` uses it.
+matrices, C += A * B. Only the GPU tests use it, to check that the plain FP64
+GEMM gives the bits of the reference's kernel.
 """
 from __future__ import annotations
 
@@ -47,37 +48,3 @@ class RefGemmKernel:
         self._check(self.cu.cuLaunchKernel(self.fn, ct.c_uint(grid_width), ct.c_uint(grid_height), ct.c_uint(1),
                                            ct.c_uint(tile_width), ct.c_uint(tile_width), ct.c_uint(1),
                                            ct.c_uint(smem), ct.c_void_p(stream), params, None), "cuLaunchKernel")
-
-
-def time_reference_kernel(configs, seed: int = 7) -> list[dict]:
-    """Times gemm_kernel on seeded uniform [-1, 1) inputs for each
-    (n, tile_width, grid_width, grid_height); checks the result against the
-    library's DMMA GEMM on the same inputs (max relative difference)."""
-    import torch
-
-    import phpc  # the library's seeded device generator and DMMA GEMM, for inputs and the check
-
-    torch.cuda.init()
-    st = torch.cuda.current_stream()
-    ref = RefGemmKernel()
-    out = []
-    for n, tw, gw, gh in configs:
-        A = torch.empty((n, n), dtype=torch.float64, device="cuda")
-        B = torch.empty((n, n), dtype=torch.float64, device="cuda")
-        phpc.fill_uniform_dev(A, n * n, seed, 0, st)
-        phpc.fill_uniform_dev(B, n * n, seed + 1, 0, st)
-        C = torch.zeros((n, n), dtype=torch.float64, device="cuda")
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        ref.launch(A.data_ptr(), B.data_ptr(), C.data_ptr(), n, n, n, tw, gw, gh, st.cuda_stream)
-        e1.record(st)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        D = torch.zeros_like(C)
-        phpc.dgemm_dmma_dev(n, n, n, A, n, B, n, D, n, 1, 1, 256, st)
-        torch.cuda.synchronize()
-        diff = float((C - D).abs().max() / D.abs().max())
-        out.append({"n": n, "tile_width": tw, "grid": f"{gw}x{gh}", "ms": round(ms, 3),
-                    "tflops": round(2.0 * n ** 3 / ms / 1e9, 4), "max_rel_diff_vs_dmma": diff})
-        del A, B, C, D
-    return out

@@ -12,9 +12,9 @@ oracle/build_oracle.py) on:
 
 For every case golden.json records the shape, the generator and seed, the
 SHA-256 of the input and output bytes; outputs of order <= 64 are also
-stored as .npy files. Run here (where /root/reference exists):
+stored as .npy files. Run where the reference sources are checked out, naming that checkout:
 
-    python tests/golden/make_golden.py
+    PHPC_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

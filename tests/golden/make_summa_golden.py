@@ -9,9 +9,9 @@ and C0, the local GEMM being the reference's CPU loop (src/iterative.c:8-13).
 For every grid summa_golden.json records the inputs' generator and seed, the
 SHA-256 of rank 0's C and of the inputs, and per rank the reported time sum
 and the number of local GEMM calls; rank 0's C is stored as a .npy file.
-Run here (where the reference sources exist):
+Run where the reference sources are checked out, naming that checkout:
 
-    python tests/golden/make_summa_golden.py
+    PHPC_REFERENCE_DIR=<reference checkout> python tests/golden/make_summa_golden.py
 """
 from __future__ import annotations
 

@@ -17,8 +17,17 @@ pytestmark = pytest.mark.gpu
 TOL_FROB = 1e-13
 
 
+@pytest.fixture(params=["dfma", "dmma"])
+def pipe(request, monkeypatch):
+    """The plain FP64 GEMM on each of its two pipes: the scalar FP64 FMA units
+    (DFMA) and the FP64 tensor cores (mma.sync f64, DMMA). The library reads
+    PHPC_FP64_PIPE at every call."""
+    monkeypatch.setenv("PHPC_FP64_PIPE", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("case", golden_cases(), ids=lambda c: c["name"])
-def test_golden(case, phpc, oracle):
+def test_golden(case, phpc, oracle, pipe):
     a, b, c = golden_inputs(case)
     ref = c.copy()
     oracle.gemm_iterative(a, b, ref)  # bit-identical to the reference (pinned in test_oracle_golden)
@@ -30,7 +39,7 @@ def test_golden(case, phpc, oracle):
         assert err["frob"] <= TOL_FROB and err["max"] <= 4 * TOL_FROB, err
 
 
-def test_config1_n1024_vs_iterative(phpc, oracle):
+def test_config1_n1024_vs_iterative(phpc, oracle, pipe):
     """N = 1024, uniform [-1, 1), tile_width 32, grid 1x1: elementwise rel err <= 1e-13."""
     rng = np.random.default_rng(1)
     n = 1024
@@ -49,7 +58,7 @@ def test_config1_n1024_vs_iterative(phpc, oracle):
 
 @pytest.mark.parametrize("m,k,n", [(1, 1, 1), (7, 13, 5), (33, 65, 17), (100, 3, 250), (129, 257, 130),
                                    (64, 1000, 64), (300, 17, 2)])
-def test_odd_shapes_accumulate(phpc, oracle, m, k, n):
+def test_odd_shapes_accumulate(phpc, oracle, pipe, m, k, n):
     rng = np.random.default_rng(m * 1000 + k + n)
     a = rng.uniform(-1, 1, (m, k))
     b = rng.uniform(-1, 1, (k, n))
@@ -91,7 +100,7 @@ def test_strided_host_leading_dimensions(phpc, oracle):
     np.testing.assert_array_equal(cc[:, 7 + n:], big_c[:, 7 + n:])
 
 
-def test_summa_grid_and_panel_do_not_change_bits(phpc, torch_cuda):
+def test_summa_grid_and_panel_do_not_change_bits(phpc, torch_cuda, pipe):
     """The logical SUMMA grid and k-panel width only reorder tiles: results are bit-identical."""
     torch = torch_cuda
     g = torch.Generator(device="cuda").manual_seed(3)
@@ -131,7 +140,7 @@ def test_empty_problems_are_noops(phpc):
     np.testing.assert_array_equal(c, 2.0)
 
 
-def test_nonfinite_propagate(phpc):
+def test_nonfinite_propagate(phpc, pipe):
     a = np.ones((8, 8))
     b = np.ones((8, 8))
     a[2, 3] = np.inf
@@ -145,7 +154,7 @@ def test_nonfinite_propagate(phpc):
 
 @pytest.mark.parametrize("m,k,n,tw,gw,gh", [(1024, 1024, 1024, 32, 4, 4), (384, 512, 256, 16, 3, 2),
                                             (256, 1000, 512, 32, 8, 8)])
-def test_bit_identical_to_reference_gpu_kernel(phpc, torch_cuda, m, k, n, tw, gw, gh):
+def test_bit_identical_to_reference_gpu_kernel(phpc, torch_cuda, pipe, m, k, n, tw, gw, gh):
     """The DMMA kernel reproduces the reference's own CUDA kernel
     (src/phpc_gemm.cu gemm_kernel, compiled unchanged for sm_103a into
     oracle/_ref by build_oracle.py) bit for bit, C accumulation included: both
@@ -173,3 +182,35 @@ def test_bit_identical_to_reference_gpu_kernel(phpc, torch_cuda, m, k, n, tw, gw
     torch.cuda.synchronize()
     assert phpc.device_status() == 0
     np.testing.assert_array_equal(C_ours.cpu().numpy(), C_ref.cpu().numpy())
+
+
+@pytest.mark.parametrize("gw,gh", [(2, 2), (4, 4)])
+def test_square_4096_summa_grids_vs_dd_oracle(phpc, oracle, torch_cuda, gw, gh):
+    """Square N = 4096, uniform [-1, 1), the logical SUMMA grid 2x2 or 4x4 with
+    k-panel 256: both FP64 pipes give the same bits, and sampled rows agree
+    with the double-double oracle (Frobenius and elementwise max <= 1e-13)."""
+    import os
+
+    torch = torch_cuda
+    n = 4096
+    A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    B = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    phpc.fill_uniform_dev(A, n * n, 41, 0)
+    phpc.fill_uniform_dev(B, n * n, 42, 0)
+    outs = {}
+    for p in ("dfma", "dmma"):
+        os.environ["PHPC_FP64_PIPE"] = p
+        try:
+            C = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+            phpc.dgemm_dmma_dev(n, n, n, A, n, B, n, C, n, gw, gh, 256)
+            torch.cuda.synchronize()
+            assert phpc.device_status() == 0
+            outs[p] = C
+        finally:
+            os.environ.pop("PHPC_FP64_PIPE", None)
+    assert torch.equal(outs["dfma"], outs["dmma"])
+    rows = np.arange(0, n, 257)
+    a = A[rows].cpu().numpy()
+    ref = oracle.gemm_dd(a, B.cpu().numpy())
+    err = oracle.rel_errors(outs["dmma"][rows].cpu().numpy(), ref)
+    assert err["frob"] <= 1e-13 and err["max"] <= 1e-13, err

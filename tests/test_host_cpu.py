@@ -281,3 +281,18 @@ def test_report_pipeline(tmp_path):
     charts = report.write_charts(recs, out)
     assert (out / "summary.csv").read_text().startswith("test,matrix_size")
     assert len(charts) == 3 and all(p.read_text().startswith("<svg") for p in charts)
+
+
+@pytest.mark.parametrize("count,seed,offset,emin,emax", [(50000, 20241203, 0, -20, 20), (4099, 20241204, 777, -20, 20),
+                                                         (3000, 7, 5, 1, 0), (2000, 11, 0, -1060, 1000)])
+def test_oracle_generator_equals_library_generator(summa_lib, oracle, count, seed, offset, emin, emax):
+    """The benchmark's CPU arm makes its inputs with the oracle's restatement of
+    the library's seeded generator (so that it loads no library of the
+    project); both give the same bits."""
+    dp = ct.POINTER(ct.c_double)
+    lib_x = np.empty(count)
+    if emin > emax:
+        summa_lib.phpc_fill_uniform(lib_x.ctypes.data_as(dp), count, seed, offset)
+    else:
+        summa_lib.phpc_fill_wide(lib_x.ctypes.data_as(dp), count, seed, offset, emin, emax)
+    np.testing.assert_array_equal(oracle.fill(count, seed, offset, emin, emax), lib_x)
