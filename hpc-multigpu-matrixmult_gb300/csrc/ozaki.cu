@@ -348,14 +348,22 @@ std::mutex g_noalloc_mu;
 // Device address of g_noalloc_scratch on the current device. The name of the
 // array in host code is only a host-side handle, not a device address, so it
 // is resolved once per device with cudaGetSymbolAddress (the set-up done by
-// the first call on each device).
+// the first call on each device). With lazy module loading (the CUDA default)
+// that first lookup may also be what loads the module onto the device, and
+// with it the array's PHPC_NOALLOC_SCRATCH_BYTES; if the device has no room
+// left for them the lookup fails with cudaErrorMemoryAllocation, reported as
+// PHPC_ERR_NOMEM.
 int noalloc_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return PHPC_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PHPC_ERR_CUDA;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return e == cudaErrorMemoryAllocation ? PHPC_ERR_NOMEM : PHPC_ERR_CUDA;
+    }
     g_noalloc_ptr[dev] = p;
   }
   *out = g_noalloc_ptr[dev];

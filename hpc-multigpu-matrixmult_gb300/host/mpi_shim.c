@@ -212,7 +212,7 @@ int MPI_Waitall(int count, MPI_Request requests[], MPI_Status statuses[]) {
 int MPI_Reduce(const void *sendbuf, void *recvbuf, int count, MPI_Datatype type, MPI_Op op, int root, MPI_Comm comm) {
   if (!comm_ok(comm)) return MPI_ERR_COMM;
   const int bs = base_size(type);
-  if (root != 0 || op != MPI_SUM || count < 0 || bs <= 0) return MPI_ERR_ARG;
+  if (root != 0 || (op != MPI_SUM && op != MPI_MAX) || count < 0 || bs <= 0) return MPI_ERR_ARG;
   if (sendbuf != MPI_IN_PLACE && sendbuf != recvbuf) memcpy(recvbuf, sendbuf, (size_t)count * bs);
   return MPI_SUCCESS;
 }

@@ -21,8 +21,10 @@
  *  - on one rank (the `mpirun -np 1` drop-in) L = 1: one local GEMM call of
  *    the whole matrices, whose copies and compute overlap inside the call;
  *  - a local error skips the remaining products but not the broadcasts and
- *    the gather, so the other ranks are not left waiting; the first error is
- *    kept for phpc_summa_last_error().
+ *    the gather, so the other ranks are not left waiting; a rank that cannot
+ *    allocate its receive buffers makes every rank skip the step loop (they
+ *    agree on it before the first broadcast); the first error is kept for
+ *    phpc_summa_last_error().
  */
 #include "phpc_summa.h"
 
@@ -134,11 +136,21 @@ static void summa(int method, MPI_Comm grid, const double *A, const double *B, d
   const int keep_cols[2] = {0, 1}, keep_rows[2] = {1, 0};
   mpi_check(MPI_Cart_sub(grid, keep_cols, &g.row_comm)); /* the processes of my grid row    */
   mpi_check(MPI_Cart_sub(grid, keep_rows, &g.col_comm)); /* the processes of my grid column */
+  int no_buffers = 0;
   for (int i = 0; i < 2; ++i) {
     g.abuf[i] = g.dims[1] > 1 ? (double *)malloc(sizeof(double) * (size_t)g.mr * g.kp) : NULL;
     g.bbuf[i] = g.dims[0] > 1 ? (double *)malloc(sizeof(double) * (size_t)g.kp * g.nc) : NULL;
-    if ((g.dims[1] > 1 && !g.abuf[i]) || (g.dims[0] > 1 && !g.bbuf[i])) keep_error(PHPC_ERR_NOMEM);
+    if ((g.dims[1] > 1 && !g.abuf[i]) || (g.dims[0] > 1 && !g.bbuf[i])) no_buffers = 1;
   }
+  /* A rank without its receive buffers cannot take part in the broadcasts,
+   * and the others would wait for it: every rank learns whether any rank
+   * lacks them before the first broadcast, and then all skip the step loop
+   * together (each reporting PHPC_ERR_NOMEM) and go on to the gather. */
+  int any_without = 0;
+  mpi_check(MPI_Reduce(&no_buffers, &any_without, 1, MPI_INT, MPI_MAX, 0, grid));
+  mpi_check(MPI_Bcast(&any_without, 1, MPI_INT, 0, grid));
+  if (any_without) keep_error(PHPC_ERR_NOMEM);
+  const int run_steps = !any_without; /* the same on every rank */
   MPI_Datatype c_block;
   mpi_check(MPI_Type_vector(g.mr, g.kp, N, MPI_DOUBLE, &g.a_panel));
   mpi_check(MPI_Type_vector(g.kp, g.nc, N, MPI_DOUBLE, &g.b_panel));
@@ -148,14 +160,15 @@ static void summa(int method, MPI_Comm grid, const double *A, const double *B, d
   mpi_check(MPI_Type_commit(&c_block));
 
   phpc_panels *acc = NULL;
-  if (!t_summa_error)
+  if (run_steps && !t_summa_error)
     keep_error(phpc_panels_begin(&acc, method, my_c, N, g.mr, g.nc, g.kp, gpu_count, grid_width, grid_height,
                                  block_width));
 
   /* step t: wait for panel t, post panel t+1, multiply panel t */
   MPI_Request req[2][2];
-  step_panels cur = post_step(&g, 0, req[0]);
-  for (int t = 0; t < steps; ++t) {
+  step_panels cur = {0};
+  if (run_steps) cur = post_step(&g, 0, req[0]);
+  for (int t = 0; run_steps && t < steps; ++t) {
     mpi_check(MPI_Waitall(2, req[t & 1], MPI_STATUSES_IGNORE));
     step_panels next = cur;
     if (t + 1 < steps) next = post_step(&g, t + 1, req[(t + 1) & 1]);

@@ -37,6 +37,7 @@ typedef struct {
 #define MPI_DOUBLE 2
 #define MPI_INT 3
 #define MPI_SUM 1
+#define MPI_MAX 2
 #define MPI_IN_PLACE ((void *)1)
 #define MPI_STATUS_IGNORE ((MPI_Status *)0)
 #define MPI_STATUSES_IGNORE ((MPI_Status *)0)

@@ -170,8 +170,12 @@ int phpc_ozaki_multiply_dev(int m, int k, int n, double *dC, int64_t ldc, int sl
  * Returns PHPC_ERR_WORKSPACE when phpc_ozaki_workspace_bytes(m, k, n, slices)
  * exceeds that size (e.g. m = n = k = 1024 needs 28 MiB at 7 slices).
  * The first call on each device looks up the array's device address; make
- * that first call before any stream capture. All calls share the array:
- * calls whose GPU work overlaps race and must be ordered by the caller.
+ * that first call before any stream capture. Under lazy module loading (the
+ * CUDA default) that first lookup can also be the moment the library's module
+ * and its 64 MiB array are loaded onto the device: make one call (a small
+ * problem will do) before fixing a memory plan; if the device has no room
+ * for the array then, the call returns PHPC_ERR_NOMEM. All calls share the
+ * array: calls whose GPU work overlaps race and must be ordered by the caller.
  */
 #define PHPC_NOALLOC_SCRATCH_BYTES (64u << 20)
 int phpc_dgemm_ozaki_noalloc_dev(int m, int k, int n, const double *dA, int64_t lda, const double *dB, int64_t ldb,

@@ -19,8 +19,9 @@
  * 0.125 s per call (or per panel added), so that the SUMMA's time sum is
  * checkable; the panel-accumulator entry points (phpc_panels_*) add each
  * panel into the caller's C block directly. A job can name one rank whose
- * local GEMM fails (PHPC_ERR_NOMEM, as a device allocation failure would), to
- * check that the other ranks still finish.
+ * local GEMM fails (PHPC_ERR_NOMEM, as a device allocation failure would), and
+ * one rank whose host allocations inside the SUMMA layer fail, to check that
+ * the other ranks still finish.
  */
 #include <stdint.h>
 #include <stdlib.h>
@@ -33,7 +34,11 @@
 #define STUB_STEP_SECONDS 0.125f
 
 static __thread int t_error;
-static __thread int t_calls, t_adds, t_fail;
+static __thread int t_calls, t_adds, t_fail, t_fail_alloc;
+
+/* The SUMMA layer's allocations (build_oracle.py compiles host/phpc_summa.c
+ * with -Dmalloc=summa_harness_malloc): they fail on the rank the job names. */
+void *summa_harness_malloc(size_t bytes) { return t_fail_alloc ? NULL : malloc(bytes); }
 
 int phpc_last_error(void) { return t_error; }
 
@@ -135,6 +140,7 @@ typedef struct {
   int *summa_error;         /* per rank: phpc_summa_last_error() (0 where absent) */
   int *calls, *adds;        /* per rank: local GEMM calls, panels added */
   int fail_rank;            /* rank whose local GEMM fails, or -1 */
+  int fail_alloc_rank;      /* rank whose SUMMA-layer allocations fail, or -1 */
 } summa_job;
 
 static int rank_body(void *arg, int rank) {
@@ -153,6 +159,7 @@ static int rank_body(void *arg, int rank) {
   memcpy(c, job->c0, sizeof(double) * nn);
   t_calls = t_adds = 0;
   t_fail = rank == job->fail_rank;
+  t_fail_alloc = rank == job->fail_alloc_rank;
   float secs = -1.f;
   if (job->method == 0)
     phpc_gemm_summa_cuda(grid, a, b, c, job->n, job->gpu_count, job->grid_width, job->grid_height, job->block_width,

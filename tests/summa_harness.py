@@ -29,7 +29,7 @@ class _Job(ct.Structure):
     _fields_ = [(n, ct.c_int) for n in ("method", "rows", "cols", "n", "gpu_count", "grid_width", "grid_height",
                                         "block_width")] + [
         ("a", _dp), ("b", _dp), ("c0", _dp), ("c_out", _dp), ("seconds", _fp), ("summa_error", _ip),
-        ("calls", _ip), ("adds", _ip), ("fail_rank", ct.c_int)]
+        ("calls", _ip), ("adds", _ip), ("fail_rank", ct.c_int), ("fail_alloc_rank", ct.c_int)]
 
 
 @dataclass
@@ -51,7 +51,7 @@ def load(path: Path) -> ct.CDLL:
 
 def run(lib: ct.CDLL, method: int, rows: int, cols: int, a: np.ndarray, b: np.ndarray, c0: np.ndarray, *,
         gpu_count: int = 1, grid_width: int = 2, grid_height: int = 2, block_width: int = 16,
-        fail_rank: int = -1) -> Result:
+        fail_rank: int = -1, fail_alloc_rank: int = -1) -> Result:
     n = a.shape[0]
     a, b, c0 = (np.ascontiguousarray(x, dtype=np.float64) for x in (a, b, c0))
     p = rows * cols
@@ -62,7 +62,8 @@ def run(lib: ct.CDLL, method: int, rows: int, cols: int, a: np.ndarray, b: np.nd
     adds = np.zeros(p, np.int32)
     job = _Job(method, rows, cols, n, gpu_count, grid_width, grid_height, block_width, a.ctypes.data_as(_dp),
                b.ctypes.data_as(_dp), c0.ctypes.data_as(_dp), out.ctypes.data_as(_dp), secs.ctypes.data_as(_fp),
-               err.ctypes.data_as(_ip), calls.ctypes.data_as(_ip), adds.ctypes.data_as(_ip), fail_rank)
+               err.ctypes.data_as(_ip), calls.ctypes.data_as(_ip), adds.ctypes.data_as(_ip), fail_rank,
+               fail_alloc_rank)
     status = lib.summa_threads_run(ct.byref(job))
     return Result(status, out, secs, err, calls, adds)
 

@@ -212,3 +212,18 @@ def test_main_out_multi_rank_divisibility_and_usage(built, tmp_path):
     r = _run_cli(tmp_path, 6, 24, 16, 2, 2)  # missing test name
     assert r.returncode == 1 and "Usage:" in r.stderr
     assert not (tmp_path / "csv").exists() or not any((tmp_path / "csv").iterdir())
+
+
+@pytest.mark.parametrize("method", [0, 1], ids=["cuda", "cublas"])
+def test_receive_buffer_failure_on_one_rank_stops_every_rank(ours, method):
+    """Rank 2 of a 2 x 3 grid cannot allocate its panel receive buffers (host
+    allocation failure made in the harness). No rank may broadcast into a
+    buffer that does not exist, nor wait for a rank that will not take part:
+    the ranks agree before the first broadcast, all skip the step loop, every
+    rank reports PHPC_ERR_NOMEM, and the gather still runs (C keeps C0)."""
+    a, b, c0 = H.inputs(24, 5, "uniform")
+    res = H.run(ours, method, 2, 3, a, b, c0, fail_alloc_rank=2)
+    assert res.status == 0  # every rank finished; no broadcast or message left over
+    assert res.summa_error.tolist() == [PHPC_ERR_NOMEM] * 6
+    assert res.adds.tolist() == [0] * 6
+    assert np.array_equal(res.c, c0)
