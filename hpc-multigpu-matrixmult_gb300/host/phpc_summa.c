@@ -20,6 +20,9 @@
  *    of the local GEMM, so the result is bit-identical;
  *  - on one rank (the `mpirun -np 1` drop-in) L = 1: one local GEMM call of
  *    the whole matrices, whose copies and compute overlap inside the call;
+ *  - PHPC_SUMMA_SCHEDULE=blocking runs the reference's schedule instead (each
+ *    step's broadcasts complete, then one local GEMM call per step), to
+ *    measure what the overlap and the resident C block save;
  *  - a local error skips the remaining products but not the broadcasts and
  *    the gather, so the other ranks are not left waiting; a rank that cannot
  *    allocate its receive buffers makes every rank skip the step loop (they
@@ -29,6 +32,7 @@
 #include "phpc_summa.h"
 
 #include <stdlib.h>
+#include <string.h>
 
 #include "phpc_gemm.h"
 
@@ -159,26 +163,46 @@ static void summa(int method, MPI_Comm grid, const double *A, const double *B, d
   mpi_check(MPI_Type_commit(&g.b_panel));
   mpi_check(MPI_Type_commit(&c_block));
 
-  phpc_panels *acc = NULL;
-  if (run_steps && !t_summa_error)
-    keep_error(phpc_panels_begin(&acc, method, my_c, N, g.mr, g.nc, g.kp, gpu_count, grid_width, grid_height,
-                                 block_width));
+  const char *sched = getenv("PHPC_SUMMA_SCHEDULE");
+  if (sched && strcmp(sched, "blocking") == 0) {
+    /* The reference's schedule, for comparison: each step's broadcasts
+     * complete before its product, and the product is one local GEMM call
+     * that copies the C block to the device and back. Same bits. */
+    MPI_Request req[2];
+    float total = 0.f;
+    for (int t = 0; run_steps && t < steps; ++t) {
+      const step_panels sp = post_step(&g, t, req);
+      mpi_check(MPI_Waitall(2, req, MPI_STATUSES_IGNORE));
+      if (t_summa_error) continue;
+      float s = 0.f;
+      gemm(sp.a, sp.lda, sp.b, sp.ldb, my_c, N, g.mr, g.kp, g.nc, gpu_count, grid_width, grid_height, block_width,
+           &s);
+      keep_error(phpc_last_error());
+      total += s;
+    }
+    if (!t_summa_error) *seconds = total;
+  } else {
+    phpc_panels *acc = NULL;
+    if (run_steps && !t_summa_error)
+      keep_error(phpc_panels_begin(&acc, method, my_c, N, g.mr, g.nc, g.kp, gpu_count, grid_width, grid_height,
+                                   block_width));
 
-  /* step t: wait for panel t, post panel t+1, multiply panel t */
-  MPI_Request req[2][2];
-  step_panels cur = {0};
-  if (run_steps) cur = post_step(&g, 0, req[0]);
-  for (int t = 0; run_steps && t < steps; ++t) {
-    mpi_check(MPI_Waitall(2, req[t & 1], MPI_STATUSES_IGNORE));
-    step_panels next = cur;
-    if (t + 1 < steps) next = post_step(&g, t + 1, req[(t + 1) & 1]);
-    if (acc && !t_summa_error) keep_error(phpc_panels_add(acc, cur.a, cur.lda, cur.b, cur.ldb, g.kp));
-    cur = next;
-  }
-  if (acc) {
-    float s = 0.f;
-    keep_error(phpc_panels_end(acc, &s));
-    if (!t_summa_error) *seconds = s;
+    /* step t: wait for panel t, post panel t+1, multiply panel t */
+    MPI_Request req[2][2];
+    step_panels cur = {0};
+    if (run_steps) cur = post_step(&g, 0, req[0]);
+    for (int t = 0; run_steps && t < steps; ++t) {
+      mpi_check(MPI_Waitall(2, req[t & 1], MPI_STATUSES_IGNORE));
+      step_panels next = cur;
+      if (t + 1 < steps) next = post_step(&g, t + 1, req[(t + 1) & 1]);
+      if (acc && !t_summa_error) keep_error(phpc_panels_add(acc, cur.a, cur.lda, cur.b, cur.ldb, g.kp));
+      cur = next;
+    }
+    if (acc) {
+      float s = 0.f;
+      keep_error(phpc_panels_end(acc, &s));
+      if (!t_summa_error) *seconds = s;
+    }
   }
 
   if (rank == 0) {

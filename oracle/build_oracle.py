@@ -13,6 +13,9 @@
   thread-per-rank MPI (mpi_threads.c), the CPU local GEMM of
   summa_threads.c and the MPI-rule checks of mpi_threads_check.c, for the
   multi-rank SUMMA tests on CPU.
+* ``oracle/libsumma_gpu_threads.so``: the same SUMMA layer and thread-per-rank
+  MPI with the library's real CUDA local GEMM (lib/libphpc_gemm.so), for the
+  multi-rank tests on one GPU (summa_gpu_threads.c).
 * ``oracle/libmain_threads.so``: this library's command-line driver
   (host/main.c as ``phpc_cli_main``, host/utils.c) on the same harness, with
   main_threads.c's stubs for its two outside calls, to run it as a multi-rank
@@ -70,6 +73,14 @@ def build() -> None:
         summa_obj = HERE / "_build" / "phpc_summa_harness.o"
         _run(["gcc", *cflags, "-Dmalloc=summa_harness_malloc", "-c", "-o", str(summa_obj), str(summa_src)])
         _run([*hflags, "-o", str(so), str(summa_obj), *map(str, harness), str(check), "-lpthread"])
+    # the same SUMMA layer with the library's real CUDA local GEMM, for the
+    # multi-rank GPU tests (only once the library has been built)
+    gemm_lib = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "lib"
+    gpu_so = HERE / "libsumma_gpu_threads.so"
+    gpu_srcs = [summa_src, HERE / "mpi_threads.c", HERE / "summa_gpu_threads.c"]
+    if (gemm_lib / "libphpc_gemm.so").exists() and _stale(gpu_so, hdeps + gpu_srcs + [gemm_lib / "libphpc_gemm.so"]):
+        _run([*hflags, "-o", str(gpu_so), *map(str, gpu_srcs), f"-L{gemm_lib}", "-lphpc_gemm",
+              f"-Wl,-rpath,{gemm_lib}", "-lpthread"])
     cuda_inc = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda")) / "include"
     if (cuda_inc / "cuda_runtime_api.h").exists():
         host = HERE.parent / "hpc-multigpu-matrixmult_gb300" / "host"

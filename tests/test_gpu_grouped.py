@@ -165,3 +165,48 @@ def test_grouped_modular_graph_replay_and_validation(phpc, torch_cuda):
     with pytest.raises(phpc.PhpcError) as e:
         phpc.GroupedPlan(probs, 0, W, ws, moduli=17)
     assert e.value.code == 1
+
+
+def test_grouped_512_problems_one_graph(phpc, oracle, torch_cuda):
+    """The batching workload's size: 512 independent problems (m, k, n
+    log-uniform in [64, 256], multiples of 16, seeded shapes), the modular plan
+    with the benchmark's 13 moduli, run as one CUDA graph. Every problem is
+    bit-identical to the single-problem modular call of the same inputs, and
+    16 seeded problems stay within the FP64-accurate bar (1e-14) against the
+    double-double oracle."""
+    torch = torch_cuda
+    shapes = phpc.grouped_shapes(512, seed=5, lo=64, hi=256)
+    q = 13
+    mats = []
+    for i, (m, k, n) in enumerate(shapes):
+        A = torch.empty((m, k), dtype=torch.float64, device="cuda")
+        B = torch.empty((k, n), dtype=torch.float64, device="cuda")
+        C = torch.empty((m, n), dtype=torch.float64, device="cuda")
+        phpc.fill_wide_dev(A, m * k, 7000 + 3 * i, 0, -20, 20)
+        phpc.fill_wide_dev(B, k * n, 7001 + 3 * i, 0, -20, 20)
+        phpc.fill_uniform_dev(C, m * n, 7002 + 3 * i, 0)
+        mats.append((A, B, C, C.clone()))
+    probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B, C, _) in zip(shapes, mats)]
+    ws = phpc.GroupedPlan.workspace_bytes(probs, 0, moduli=q)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    plan = phpc.GroupedPlan(probs, 0, W, ws, moduli=q)
+    plan.graph_launch()
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    ws1 = max(phpc.ozaki2_workspace_bytes(m, k, n, q) for m, k, n in shapes)
+    W1 = torch.empty(ws1, dtype=torch.uint8, device="cuda")
+    for (m, k, n), (A, B, _, C1) in zip(shapes, mats):
+        phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C1, n, q, W1, ws1)
+    torch.cuda.synchronize()
+    assert phpc.device_status() == 0
+    for i, (_, _, C, C1) in enumerate(mats):
+        assert torch.equal(C, C1), f"problem {i} {shapes[i]}"
+    pick = np.random.default_rng(5).choice(512, size=16, replace=False)
+    for i in sorted(int(x) for x in pick):
+        A, B, C, _ = mats[i]
+        c0 = torch.empty_like(C)
+        phpc.fill_uniform_dev(c0, C.numel(), 7002 + 3 * i, 0)
+        ref = oracle.gemm_dd(A.cpu().numpy(), B.cpu().numpy(), c0.cpu().numpy())
+        err = oracle.rel_errors(C.cpu().numpy(), ref)
+        assert err["frob"] <= 1e-14 and err["max"] <= 1e-14, (i, shapes[i], err)
+    plan.close()

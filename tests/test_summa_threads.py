@@ -227,3 +227,18 @@ def test_receive_buffer_failure_on_one_rank_stops_every_rank(ours, method):
     assert res.summa_error.tolist() == [PHPC_ERR_NOMEM] * 6
     assert res.adds.tolist() == [0] * 6
     assert np.array_equal(res.c, c0)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c["rows"] * c["cols"] > 1], ids=lambda c: c["name"])
+def test_blocking_schedule_reproduces_golden(ours, case, monkeypatch):
+    """PHPC_SUMMA_SCHEDULE=blocking runs the reference's own schedule (each
+    step's broadcasts complete, then one local GEMM call per step, C copied by
+    every call): the same bits, calls and per-rank time sums as the
+    reference's SUMMA."""
+    monkeypatch.setenv("PHPC_SUMMA_SCHEDULE", "blocking")
+    a, b, c0 = H.inputs(case["n"], case["seed"], case["dist"])
+    res = H.run(ours, 0, case["rows"], case["cols"], a, b, c0)
+    assert res.status == 0 and not res.summa_error.any()
+    assert sha(res.c) == case["sha_c"]
+    assert res.calls.tolist() == case["calls"] and res.adds.tolist() == [0] * len(case["calls"])
+    assert res.seconds.tolist() == case["seconds"]
