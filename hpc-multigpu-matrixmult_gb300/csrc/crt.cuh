@@ -8,6 +8,18 @@
 namespace phpc {
 
 constexpr int kCrtMaxModuli = 15;  // M < 2^127: weights in four 32-bit limbs, sums in five
+constexpr int kCrtMaxLimbs = 10;   // balanced 13-bit digits of M / m_i (15 moduli: 10)
+
+// Constants of the reconstruction on FP32 limbs (crt_limbs_pair), each value
+// in both lanes of a packed f32x2 operation.
+struct CrtLimbs {
+  int np;                                 // digits of the largest M / m_i (5 .. 10)
+  float2 inv[kCrtMaxModuli];              // (M / m_i)^-1 mod m_i
+  float2 rm[kCrtMaxModuli];               // 1 / m_i rounded to float
+  float2 negm[kCrtMaxModuli];             // -m_i
+  float2 P[kCrtMaxModuli][kCrtMaxLimbs];  // balanced 13-bit digits of M / m_i, least significant first
+  float2 negM[kCrtMaxLimbs + 1];          // balanced 13-bit digits of M, negated
+};
 
 struct CrtTable {
   int n;                          // number of moduli
@@ -18,6 +30,7 @@ struct CrtTable {
   float Minv;                     // 1 / (M >> 32 qlimb) rounded to float
   int fast;                       // 1: every result y has |y| / M <= 1/2 - 1/32 (crt_round's one-step path)
                                   //    for this table's K (grouped problems carry their own flag)
+  CrtLimbs L;                     // the same reconstruction on FP32 limbs (one-step path)
 };
 
 // c + v * 2^x for a double v and an int x, one rounding (the scaling is exact
@@ -28,6 +41,26 @@ __device__ __forceinline__ double crt_add_scaled(double c, double v, int x) {
   if (E >= 1 && E <= 2046)
     return c + __longlong_as_double(static_cast<long long>((bits & ~(0x7FFull << 52)) | (static_cast<uint64_t>(E) << 52)));
   return c + ldexp(v, x);
+}
+
+// A 128-bit magnitude (hi, lo) rounded once to double, sign applied: returns
+// v and sets shift so that the value is v * 2^shift (v an integer-valued
+// double).
+__device__ __forceinline__ double round_magnitude(uint64_t hi, uint64_t lo, bool neg, int& shift) {
+  double v;
+  if (hi == 0) {
+    v = __ull2double_rn(lo);
+    shift = 0;
+  } else {
+    // round the 128-bit magnitude to 53 bits once: its top 64 bits plus a
+    // sticky bit for everything below them, converted with round-to-nearest
+    const int lz = __clzll(static_cast<long long>(hi));
+    const uint64_t topbits = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    const uint64_t rest = lz ? (lo << lz) : lo;
+    v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
+    shift = 64 - lz;
+  }
+  return neg ? -v : v;
 }
 
 // The symmetric representative of acc mod M (acc = sum r_i W_i < 2^13 M, as
@@ -145,22 +178,8 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T,
       }
     }
   }
-  const uint64_t hi = (static_cast<uint64_t>(x[3]) << 32) | x[2];
-  const uint64_t lo = (static_cast<uint64_t>(x[1]) << 32) | x[0];
-  double v;
-  if (hi == 0) {
-    v = __ull2double_rn(lo);
-    shift = 0;
-  } else {
-    // round the 128-bit magnitude to 53 bits once: its top 64 bits plus a
-    // sticky bit for everything below them, converted with round-to-nearest
-    const int lz = __clzll(static_cast<long long>(hi));
-    const uint64_t topbits = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
-    const uint64_t rest = lz ? (lo << lz) : lo;
-    v = __ull2double_rn(topbits | (rest != 0 ? 1ull : 0ull));
-    shift = 64 - lz;
-  }
-  return neg ? -v : v;
+  return round_magnitude((static_cast<uint64_t>(x[3]) << 32) | x[2], (static_cast<uint64_t>(x[1]) << 32) | x[0], neg,
+                         shift);
 }
 
 // The CRT of one element from its residues r[i] mod m_i: acc = sum r_i W_i,
@@ -191,6 +210,79 @@ __device__ __forceinline__ double crt_value(const uint32_t (&rr)[kCrtMaxModuli],
   l[3] = static_cast<uint32_t>(t);
   l[4] = static_cast<uint32_t>(t >> 32);
   return crt_round(l, T, fast, shift);
+}
+
+// The one-step CRT of two adjacent elements on FP32 limbs, the two elements
+// in the two lanes of packed f32x2 operations. w[i] holds their residues mod
+// m_i (element 0 in the low 16 bits, element 1 in the high 16 bits). Valid
+// when every result satisfies |y| / M <= 1/2 - 1/32 (CrtTable::fast); gives
+// the same y, rounded the same way, as crt_value. Steps (every one except the
+// two rounding estimates is exact in FP32: all values are integers below 2^24):
+//  1. t_i = r_i inv_i mod m_i, symmetric: p = r_i inv_i < 2^17, t_i = p -
+//     round(p / m_i) m_i (|t_i| <= m_i / 2); sum_i t_i (M / m_i) = y (mod M);
+//  2. S_j = sum_i t_i P_ij over the balanced 13-bit digits P_ij of M / m_i
+//     (|P_ij| <= 2^12, |S_j| <= 15 181 2^12 < 2^24);
+//  3. q = round(sum_i t_i / m_i) (|q| <= 8; exact under the fast path's margin);
+//  4. Y_j = S_j - q M_j (|Y_j| < 2^24), digits of y = sum_j Y_j 2^(13 j);
+//  5. carries: h_j = round(Y_j 2^-13), d_j = (Y_j - h_j 2^13) + h_(j-1)
+//     (|d_j| < 2^13), read out as integers through the rounding constant
+//     1.5 2^23, and y = sum_j d_j 2^(13 j) mod 2^128 (|y| < 2^127).
+// NP = T.L.np, the number of digits of the largest M / m_i.
+template <int NP>
+__device__ __forceinline__ void crt_limbs_pair(const uint32_t (&w)[kCrtMaxModuli], const CrtTable& T, double& v0,
+                                               int& s0, double& v1, int& s1) {
+  const float2 kRound = make_float2(12582912.0f, 12582912.0f), kUnround = make_float2(-12582912.0f, -12582912.0f);
+  const float2 kUnbias = make_float2(-8388608.0f, -8388608.0f);
+  const float2 kDigit = make_float2(0x1p-13f, 0x1p-13f), kNegBase = make_float2(-8192.0f, -8192.0f);
+  float2 S[NP];
+#pragma unroll
+  for (int j = 0; j < NP; ++j) S[j] = make_float2(0.0f, 0.0f);
+  float2 est = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int i = 0; i < kCrtMaxModuli; ++i) {
+    if (i < T.n) {
+      // r as floats: 2^23 + r has r in its mantissa bits
+      const float2 r = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | (w[i] & 0xFFFFu)),
+                                              __uint_as_float(0x4B000000u | (w[i] >> 16))),
+                                  kUnbias);
+      const float2 p = __fmul2_rn(r, T.L.inv[i]);
+      const float2 qq = __fadd2_rn(__ffma2_rn(p, T.L.rm[i], kRound), kUnround);
+      const float2 t = __ffma2_rn(qq, T.L.negm[i], p);
+      est = __ffma2_rn(t, T.L.rm[i], est);
+#pragma unroll
+      for (int j = 0; j < NP; ++j) S[j] = __ffma2_rn(t, T.L.P[i][j], S[j]);
+    }
+  }
+  const float2 q = __fadd2_rn(__fadd2_rn(est, kRound), kUnround);
+  int d0[NP + 2], d1[NP + 2];
+  float2 hprev = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int j = 0; j <= NP; ++j) {
+    const float2 y = j < NP ? __ffma2_rn(q, T.L.negM[j], S[j]) : __fmul2_rn(q, T.L.negM[NP]);
+    const float2 h = __fadd2_rn(__ffma2_rn(y, kDigit, kRound), kUnround);
+    const float2 d = __fadd2_rn(__fadd2_rn(__ffma2_rn(h, kNegBase, y), hprev), kRound);
+    d0[j] = __float_as_int(d.x) - 0x4B400000;
+    d1[j] = __float_as_int(d.y) - 0x4B400000;
+    hprev = h;
+  }
+  {
+    const float2 d = __fadd2_rn(hprev, kRound);
+    d0[NP + 1] = __float_as_int(d.x) - 0x4B400000;
+    d1[NP + 1] = __float_as_int(d.y) - 0x4B400000;
+  }
+  // y = sum_j d_j 2^(13 j) modulo 2^128, most significant digit first
+  using u128 = unsigned __int128;
+  u128 y0 = 0, y1 = 0;
+#pragma unroll
+  for (int j = NP + 1; j >= 0; --j) {
+    y0 = (y0 << 13) + static_cast<u128>(static_cast<__int128>(d0[j]));
+    y1 = (y1 << 13) + static_cast<u128>(static_cast<__int128>(d1[j]));
+  }
+  const bool n0 = static_cast<uint64_t>(y0 >> 64) >> 63, n1 = static_cast<uint64_t>(y1 >> 64) >> 63;
+  if (n0) y0 = ~y0 + 1;
+  if (n1) y1 = ~y1 + 1;
+  v0 = round_magnitude(static_cast<uint64_t>(y0 >> 64), static_cast<uint64_t>(y0), n0, s0);
+  v1 = round_magnitude(static_cast<uint64_t>(y1 >> 64), static_cast<uint64_t>(y1), n1, s1);
 }
 
 // *c += v * 2^(shift + e): the CRT result of one element applied to C

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
+#include <type_traits>
 
 #include "crt.cuh"
 #include "ozaki_digits.cuh"
@@ -103,6 +104,34 @@ inline ModTable make_table(int nmod, int k) {
   T.crt.Minv = static_cast<float>(1.0 / static_cast<double>(static_cast<uint64_t>(M >> (32 * T.crt.qlimb))));
   T.crt.n = T.n;
   T.crt.fast = mod_crt_fast();
+  // the reconstruction on FP32 limbs: balanced 13-bit digits of M / m_i and M
+  auto digits = [](u128 x, float2* out, int count) {
+    int used = 0;
+    for (int j = 0; j < count; ++j) {
+      int64_t d = static_cast<int64_t>(x & 0x1FFF);
+      if (d >= 4096) d -= 8192;
+      out[j] = make_float2(static_cast<float>(d), static_cast<float>(d));
+      x = (x - static_cast<u128>(static_cast<__int128>(d))) >> 13;
+      if (d != 0 || x != 0) used = j + 1;
+    }
+    return x == 0 ? used : -1;
+  };
+  int np = 0;
+  for (int i = 0; i < nmod; ++i) {
+    const uint32_t m = kModuli[i];
+    const u128 Mi = M / m;
+    uint32_t inv = 0;
+    for (uint32_t v = 1; v < m; ++v)
+      if ((static_cast<uint64_t>(static_cast<uint32_t>(Mi % m)) * v) % m == 1) { inv = v; break; }
+    T.crt.L.inv[i] = make_float2(static_cast<float>(inv), static_cast<float>(inv));
+    T.crt.L.rm[i] = T.invm[i];
+    T.crt.L.negm[i] = T.negm[i];
+    np = std::max(np, digits(Mi, T.crt.L.P[i], kCrtMaxLimbs));
+  }
+  T.crt.L.np = np;
+  float2 Md[kCrtMaxLimbs + 1];
+  digits(M, Md, kCrtMaxLimbs + 1);
+  for (int j = 0; j <= kCrtMaxLimbs; ++j) T.crt.L.negM[j] = make_float2(-Md[j].x, -Md[j].y);
   return T;
 }
 
@@ -318,11 +347,29 @@ constexpr int kColBlockK = 64, kColBlockJ = 32;
 
 constexpr int kCrtCols = 4;  // consecutive columns per thread (one 8-byte load per residue plane)
 
+// Calls f(std::integral_constant<int, np>()) for the CRT's digit count np
+// (5 .. 10: the kernels are instantiated per count).
+template <class F>
+inline void with_crt_digits(int np, F&& f) {
+  switch (np) {
+    case 5: f(std::integral_constant<int, 5>()); break;
+    case 6: f(std::integral_constant<int, 6>()); break;
+    case 7: f(std::integral_constant<int, 7>()); break;
+    case 8: f(std::integral_constant<int, 8>()); break;
+    case 9: f(std::integral_constant<int, 9>()); break;
+    default: f(std::integral_constant<int, 10>()); break;
+  }
+}
+
 // C[row][c0 .. c0 + 3] += the CRT of their residues (rp: plane 0 of the 16-bit
 // residue planes at the row and column c0; c0 a multiple of 4 inside a plane
 // row padded to 16), scaled by 2^(row_shift + eb[c] - bb[c]) (row_shift: the
 // row's exponent less its grid width). Columns at or beyond ncols are left
 // alone.
+// NP = T.L.np (the kernels are instantiated per digit count); with fast set
+// the four elements are reconstructed on FP32 limbs, two at a time
+// (crt_limbs_pair), else by the 32-bit-limb integer path (crt_value).
+template <int NP>
 __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_t rplane, const CrtTable& T, int fast,
                                          int ncols, int row_shift, const int* __restrict__ ebp,
                                          const int* __restrict__ bbp, double* cp) {
@@ -330,6 +377,31 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i)
     rw[i] = i < T.n ? *reinterpret_cast<const uint2*>(rp + i * rplane) : make_uint2(0u, 0u);
+  if (fast) {
+    uint32_t w01[kCrtMaxModuli], w23[kCrtMaxModuli];
+#pragma unroll
+    for (int i = 0; i < kCrtMaxModuli; ++i) {
+      w01[i] = rw[i].x;
+      w23[i] = rw[i].y;
+    }
+    double v[kCrtCols];
+    int sh[kCrtCols];
+    crt_limbs_pair<NP>(w01, T, v[0], sh[0], v[1], sh[1]);
+    crt_limbs_pair<NP>(w23, T, v[2], sh[2], v[3], sh[3]);
+    if (ncols == kCrtCols) {
+      double cv[kCrtCols];
+#pragma unroll
+      for (int c = 0; c < kCrtCols; ++c) cv[c] = cp[c];
+#pragma unroll
+      for (int c = 0; c < kCrtCols; ++c)
+        cp[c] = crt_added(cv[c], v[c], sh[c] + row_shift + max(ebp[c], -20000) - bbp[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < kCrtCols; ++c)
+        if (c < ncols) crt_apply(cp + c, v[c], sh[c] + row_shift + max(ebp[c], -20000) - bbp[c]);
+    }
+    return;
+  }
   if (ncols == kCrtCols) {
     // whole group: C loaded up front and the four reconstructions written
     // without early exits, so that they can overlap (1-4 % faster)

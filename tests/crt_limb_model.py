@@ -1,0 +1,123 @@
+"""Model of the CRT reconstruction on FP32 limbs (the kernel crt_limbs_pair in
+csrc/crt.cuh), used by the CPU tests to check its arithmetic on many residue
+vectors: every step that the kernel does exactly must stay within the range
+in which FP32 represents integers exactly, and the result must be the
+symmetric representative of sum_i r_i W_i mod M.
+
+The reconstruction, for residues r_i in [0, m_i) of the q moduli:
+
+1. t_i = r_i inv_i mod m_i, symmetric (|t_i| <= m_i / 2), inv_i =
+   (M / m_i)^-1 mod m_i: p = r_i inv_i < 2^17 exactly, qq = round(p / m_i)
+   through the 1.5 2^23 rounding constant, t_i = p - qq m_i by one FMA.
+   Then sum_i t_i (M / m_i) = sum_i r_i W_i (mod M) with W_i = (M / m_i) inv_i.
+2. S_j = sum_i t_i P_ij, P_ij the balanced 13-bit digits of P_i = M / m_i
+   (|P_ij| <= 2^12): |S_j| <= 15 * 181 * 2^12 < 2^24, so every partial sum is
+   an integer FP32 holds exactly.
+3. est = sum_i t_i fl(1 / m_i) in FP32, |est| <= 7.5; q = round(est). With the
+   fast path's guarantee |y| / M <= 1/2 - 1/32 the rounding is exact.
+4. Y_j = S_j - q M_j (M_j the balanced 13-bit digits of M): |Y_j| < 2^24.
+5. Carries: h_j = round(Y_j 2^-13), l_j = Y_j - h_j 2^13 (|l_j| <= 2^12),
+   digits d_0 = l_0, d_j = l_j + h_(j-1): |d_j| < 2^22, converted to integers
+   through the rounding constant; y = sum_j d_j 2^(13 j) mod 2^128.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+MODULI = [363, 362, 361, 359, 355, 353, 349, 347, 343, 337, 331, 317, 313, 311, 307]
+MAGIC = np.float32(12582912.0)  # 1.5 * 2^23
+
+
+def balanced_digits(x: int, count: int, bits: int = 13) -> list[int]:
+    out = []
+    for _ in range(count):
+        r = x % (1 << bits)
+        if r >= 1 << (bits - 1):
+            r -= 1 << bits
+        out.append(r)
+        x = (x - r) >> bits
+    assert x == 0
+    return out
+
+
+class Table:
+    def __init__(self, q: int):
+        self.q = q
+        self.m = MODULI[:q]
+        self.M = 1
+        for m in self.m:
+            self.M *= m
+        self.P = [self.M // m for m in self.m]
+        self.inv = [pow(P % m, -1, m) for P, m in zip(self.P, self.m)]
+        self.W = [P * v for P, v in zip(self.P, self.inv)]
+        self.NP = max(len_digits(P) for P in self.P)
+        self.Pd = [balanced_digits(P, self.NP) for P in self.P]
+        self.Md = balanced_digits(self.M, self.NP + 1)
+
+
+def len_digits(x: int) -> int:
+    n = 1
+    while True:
+        try:
+            balanced_digits(x, n)
+            return n
+        except AssertionError:
+            n += 1
+
+
+def f32(x) -> np.float32:
+    return np.float32(x)
+
+
+def fma32(a, b, c) -> np.float32:
+    """FP32 fused multiply-add, exact product and one rounding (through float64:
+    the products here have at most 48 significant bits and the sums are
+    either exact in float64 or rounded once to float32 after an exact
+    float64 sum)."""
+    return np.float32(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+def reconstruct(T: Table, r: list[int], checks: dict | None = None) -> int:
+    """y (the symmetric representative of sum r_i W_i mod M) by the limb
+    algorithm; records the largest magnitudes of its exact steps in checks."""
+    S = [f32(0)] * T.NP
+    est = f32(0)
+    tmax = 0
+    for i, m in enumerate(T.m):
+        p = f32(r[i]) * f32(T.inv[i])
+        assert float(p) == r[i] * T.inv[i]
+        qq = fma32(p, f32(1.0 / m), MAGIC) - MAGIC
+        t = fma32(qq, f32(-m), p)
+        assert float(t) == r[i] * T.inv[i] - float(qq) * m
+        tmax = max(tmax, abs(int(t)))
+        est = fma32(t, f32(1.0 / m), est)
+        for j in range(T.NP):
+            exact = int(S[j]) + int(t) * T.Pd[i][j]
+            S[j] = fma32(t, f32(T.Pd[i][j]), S[j])
+            assert int(S[j]) == exact and abs(exact) < 1 << 24
+    q = (est + MAGIC) - MAGIC
+    Y = [fma32(q, f32(-T.Md[j]), S[j] if j < T.NP else f32(0)) for j in range(T.NP + 1)]
+    Yexact = [(int(S[j]) if j < T.NP else 0) - int(q) * T.Md[j] for j in range(T.NP + 1)]
+    assert [int(y) for y in Y] == Yexact and max(abs(y) for y in Yexact) < 1 << 24
+    h = [fma32(y, f32(2.0 ** -13), MAGIC) - MAGIC for y in Y]
+    low = [fma32(hj, f32(-8192.0), y) for hj, y in zip(h, Y)]
+    d = [low[0]] + [low[j] + h[j - 1] for j in range(1, T.NP + 1)] + [h[T.NP]]
+    ints = []
+    for x in d:
+        assert abs(int(x)) < 1 << 22 and float(x) == int(x)
+        bits = (np.float32(x) + MAGIC).view(np.int32)
+        ints.append(int(bits) - 0x4B400000)
+    y = sum(v << (13 * j) for j, v in enumerate(ints))
+    y = ((y + (1 << 127)) % (1 << 128)) - (1 << 127)  # 128-bit two's complement
+    if checks is not None:
+        checks["t"] = max(checks.get("t", 0), tmax)
+        checks["q"] = max(checks.get("q", 0), abs(int(q)))
+        checks["S"] = max(checks.get("S", 0), max(abs(int(s)) for s in S))
+        checks["Y"] = max(checks.get("Y", 0), max(abs(v) for v in Yexact))
+        checks["d"] = max(checks.get("d", 0), max(abs(v) for v in ints))
+    return y
+
+
+def symmetric_crt(T: Table, r: list[int]) -> int:
+    acc = sum(ri * Wi for ri, Wi in zip(r, T.W)) % T.M
+    return acc - T.M if 2 * acc > T.M else acc

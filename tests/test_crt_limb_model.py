@@ -1,0 +1,46 @@
+"""The CRT on FP32 limbs (csrc/crt.cuh, crt_limbs_pair) checked on the CPU
+through its model (tests/crt_limb_model.py): for every modulus count the
+library supports, on seeded and extreme values, every step the kernel does
+exactly stays exact, and the result is the integer the residues stand for.
+"""
+import numpy as np
+import pytest
+
+import crt_limb_model as CL
+
+
+@pytest.mark.parametrize("q", list(range(8, 16)))
+def test_limb_crt_recovers_every_value_within_the_margin(q):
+    T = CL.Table(q)
+    rng = np.random.default_rng(q)
+    bound = T.M * 15 // 32  # |y| / M <= 1/2 - 1/32, the fast path's guarantee
+    values = [0, 1, -1, bound, -bound, bound - 1, -(bound - 1), T.M // 4, -(T.M // 3)]
+    values += [int(x) for x in rng.integers(-(1 << 62), 1 << 62, 200)]
+    values += [(int(rng.integers(0, 1 << 62)) * (1 << 62) + int(rng.integers(0, 1 << 62))) % (2 * bound) - bound
+               for _ in range(300)]
+    checks = {}
+    for y in values:
+        r = [y % m for m in T.m]
+        assert CL.symmetric_crt(T, r) == y
+        assert CL.reconstruct(T, r, checks) == y, (q, y)
+    assert checks["S"] < 1 << 24 and checks["Y"] < 1 << 24 and checks["d"] < 1 << 22
+    assert checks["t"] <= 181 and checks["q"] <= 8
+
+
+@pytest.mark.parametrize("q", [8, 13, 15])
+def test_limb_crt_extreme_residues(q):
+    """Residue vectors that drive the limb sums to their extremes (every t_i
+    at +-181 or +-m_i/2, with the signs of the largest digits), kept to those
+    whose value lies within the fast path's margin."""
+    T = CL.Table(q)
+    bound = T.M * 15 // 32
+    rng = np.random.default_rng(100 + q)
+    tried = 0
+    for _ in range(4000):
+        r = [int(rng.choice([0, m // 2, (m + 1) // 2, m - 1, 1])) for m in T.m]
+        y = CL.symmetric_crt(T, r)
+        if abs(y) > bound:
+            continue
+        tried += 1
+        assert CL.reconstruct(T, r) == y
+    assert tried > 200
