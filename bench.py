@@ -46,7 +46,8 @@ Multi-GPU (torchrun): every rank runs an independent replica (the GEMM path
 has no exchange on a one-GPU-per-process node); value = total work / max time.
 
 Other modes (one JSON line each): --peaks (throughput of the arithmetic pipes:
-DFMA, the FP64 tensor-core mma.sync shapes, IMMA, FFMA), --case METHOD (one
+DFMA, the FP64 tensor-core mma.sync shapes, IMMA, FFMA), --link (the host
+link: copy engines and kernels over page-locked memory), --case METHOD (one
 method at one size, for profiling one launch), --summa-rank RxC (one SUMMA
 rank's panel steps, per-step calls against the panel accumulator).
 --cpu-scaling (opt-in, a few minutes of CPU) times the reference's sequential
@@ -99,6 +100,7 @@ def parse_args():
     p.add_argument("--configs", type=int, default=1,
                    help="also run the rectangular FP32 and the batched workloads after the timed region (1/0)")
     p.add_argument("--peaks", action="store_true", help="throughput probes of the arithmetic pipes, then exit")
+    p.add_argument("--link", action="store_true", help="host-link probes (copy engines and kernels), then exit")
     p.add_argument("--case", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma"], default=None,
                    help="time one method at one size (--m/--k/--n, --reps) and exit")
     p.add_argument("--m", type=int, default=0)
@@ -669,6 +671,13 @@ def main():
         return
     if args.peaks:
         run_peaks(args)
+        return
+    if args.link:
+        import torch
+        import phpc
+        import workloads
+
+        print(json.dumps({"probe": "host link", **workloads.host_link(torch, phpc)}), flush=True)
         return
     if args.case:
         run_case(args)

@@ -1,18 +1,23 @@
-"""Autotuner for the FP64-accurate Ozaki GEMMs: scheme, tile width, L2 raster.
+"""Autotuner: scheme, tile shapes, L2 raster and pipeline depths of the GEMMs.
 
-For each square size N it sweeps the scheme (the modular scheme with q
-moduli, or the digit scheme with s slices), output tile width BN (128 or 256),
-the raster height of the persistent tile order (group_rows) and the CTA
-grouping (1 = one CTA per 128 x BN tile, 2 = CTA pairs computing 256 x BN
-tiles with M = 256 tcgen05 MMAs), times the
+For each square size N it sweeps, for the FP64-accurate Ozaki GEMM, the
+scheme (the modular scheme with q moduli, or the digit scheme with s slices),
+output tile width BN (128 or 256), the raster height of the persistent tile
+order (group_rows) and the CTA grouping (1 = one CTA per 128 x BN tile, 2 =
+CTA pairs computing 256 x BN tiles with M = 256 tcgen05 MMAs), times the
 full call (scans + splits + slice GEMM; CUDA events, median of --reps) on
 seeded inputs resident in HBM, and measures the Frobenius relative error of
 the result against the double-double reference (phpc_dgemm_dd_rows_dev) on
 sampled rows, for two input classes: uniform [-1, 1) and wide exponents
 (u * 2^e, e uniform in [-20, 20]). A configuration qualifies when both errors
-are below target / margin; the fastest qualifying configuration wins. For the
-grouped call it picks BN on the batching workload (512 problems, modular
-plan with --grouped-moduli moduli).
+are below target / margin; the fastest qualifying configuration wins, and
+then the pipeline depth (K-stages of the tcgen05 shared-memory ring, 2 up to
+the deepest that fits) is swept for it. For the grouped call it picks BN and
+the stages on the batching workload (512 problems, modular plan with
+--grouped-moduli moduli); for the 3xBF16 FP32 GEMM the tile width, raster and
+stages on the rectangular workload (M = 32768, N = 8192, K = 4096, FP32
+normal(0, 1), error against the FP64 product on sampled rows); for the plain
+FP64 GEMM the ring depth (2-6 stages) per size up to --plain-max-n.
 
 Writes tune_table.txt next to this file (copied into lib/ by the build, where
 the library reads it):
@@ -47,6 +52,8 @@ def main() -> int:
     p.add_argument("--grouped-count", type=int, default=512)
     p.add_argument("--grouped-moduli", type=int, default=13)
     p.add_argument("--clusters", default="1,2")
+    p.add_argument("--plain-max-n", type=int, default=8192)
+    p.add_argument("--f32-shape", default="32768,4096,8192", help="m,k,n of the 3xBF16 entry")
     p.add_argument("--out", default=str(HERE / "tune_table.txt"))
     a = p.parse_args()
 
@@ -62,10 +69,31 @@ def main() -> int:
 
     clusters = [int(x) for x in a.clusters.split(",")]
 
-    def set_cfg(bn, gr, cl=1):
+    def set_cfg(bn, gr, cl=1, stages=0):
         os.environ["PHPC_OZAKI_BN"] = str(bn)
         os.environ["PHPC_GROUP_ROWS"] = str(gr)
         os.environ["PHPC_CLUSTER"] = str(cl)
+        if stages:
+            os.environ["PHPC_STAGES"] = str(stages)
+        else:
+            os.environ.pop("PHPC_STAGES", None)
+
+    def median_ms(fn, reps):
+        fn()  # warm
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    def max_stages(bn, cl):
+        """The deepest tcgen05 ring that fits (TcCfg::kStages: 192 KB of 64-deep
+        bf16 stages of a 128-row A tile and a BN / cluster-row B tile)."""
+        return (192 * 1024) // (128 * 64 * 2 + (bn // cl) * 64 * 2)
 
     for n in sizes:
         classes = {}
@@ -111,35 +139,39 @@ def main() -> int:
                 for gr in grs:
                     for cl in clusters:
                         set_cfg(bn, gr, cl)
-                        run(A, B, C, W)  # warm
-                        ts = []
-                        for _ in range(a.reps):
-                            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                            e0.record(st)
-                            run(A, B, C, W)
-                            e1.record(st)
-                            e1.synchronize()
-                            ts.append(e0.elapsed_time(e1))
-                        ms = statistics.median(ts)
+                        ms = median_ms(lambda: run(A, B, C, W), a.reps)
                         rec = {"n": n, "moduli": cnt if kind == "moduli" else 0,
                                "slices": cnt if kind == "slices" else 7, "bn": bn, "group_rows": gr,
-                               "cluster": cl, "ms": round(ms, 3), "tflops": round(2.0 * n ** 3 / ms / 1e9, 3),
-                               "err": errs, "qualifies": ok}
+                               "cluster": cl, "stages": 0, "ms": round(ms, 3),
+                               "tflops": round(2.0 * n ** 3 / ms / 1e9, 3), "err": errs, "qualifies": ok}
                         report.append(rec)
                         print(json.dumps(rec), flush=True)
                         if ok:
-                            cands.append(rec)
+                            cands.append((rec, run, W))
             del W
             torch.cuda.empty_cache()
         if not cands:
             raise SystemExit(f"no configuration meets {a.target} / {a.margin} at N={n}")
-        best = min(cands, key=lambda r: r["ms"])
+        best, run, W = min(cands, key=lambda c: c[0]["ms"])
+        # pipeline depth of the winner: 2 .. the deepest ring that fits (0 = deepest)
+        A, B, _, _ = classes["wide"]
+        deepest = max_stages(best["bn"], best["cluster"])
+        for stages in range(2, deepest):
+            set_cfg(best["bn"], best["group_rows"], best["cluster"], stages)
+            ms = median_ms(lambda: run(A, B, C, W), a.reps)
+            rec = dict(best, stages=stages, ms=round(ms, 3), tflops=round(2.0 * n ** 3 / ms / 1e9, 3))
+            report.append(rec)
+            print(json.dumps(rec), flush=True)
+            if ms < best["ms"]:
+                best = rec
+        os.environ.pop("PHPC_STAGES", None)
+        del cands, W
         table.append(best)
         del classes, C
         torch.cuda.empty_cache()
 
     # grouped call: tile width on the batching workload
-    grouped_bn, grouped_rep = 128, []
+    grouped_bn, grouped_stages, grouped_rep, best_ms = 128, 0, [], None
     if a.grouped_count > 0:
         shapes = phpc.grouped_shapes(a.grouped_count, seed=5)
         mats = []
@@ -153,40 +185,113 @@ def main() -> int:
         probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B, C) in zip(shapes, mats)]
         best_ms = None
         for bn in (128, 256):
-            os.environ["PHPC_GROUPED_BN"] = str(bn)
-            ws = phpc.GroupedPlan.workspace_bytes(probs, s, moduli=q)
-            W = torch.empty(ws, dtype=torch.uint8, device="cuda")
-            plan = phpc.GroupedPlan(probs, s, W, ws, st, moduli=q)
-            plan.graph_launch(st)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            for _ in range(a.reps):
-                plan.graph_launch(st)
-            e1.record(st)
-            e1.synchronize()
-            ms = e0.elapsed_time(e1) / a.reps
-            plan.close()
-            del W
-            rec = {"grouped_count": a.grouped_count, "moduli": q, "bn": bn, "ms": round(ms, 3)}
-            grouped_rep.append(rec)
-            print(json.dumps(rec), flush=True)
-            if best_ms is None or ms < best_ms:
-                best_ms, grouped_bn = ms, bn
+            for stages in [0] + list(range(2, max_stages(bn, 1))):
+                os.environ["PHPC_GROUPED_BN"] = str(bn)
+                set_cfg(256, 8, 1, stages)
+                ws = phpc.GroupedPlan.workspace_bytes(probs, s, moduli=q)
+                W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+                plan = phpc.GroupedPlan(probs, s, W, ws, st, moduli=q)
+                ms = median_ms(lambda: plan.graph_launch(st), a.reps)
+                plan.close()
+                del W
+                rec = {"grouped_count": a.grouped_count, "moduli": q, "bn": bn, "stages": stages,
+                       "ms": round(ms, 3)}
+                grouped_rep.append(rec)
+                print(json.dumps(rec), flush=True)
+                if best_ms is None or ms < best_ms:
+                    best_ms, grouped_bn, grouped_stages = ms, bn, stages
         os.environ.pop("PHPC_GROUPED_BN", None)
-    for key in ("PHPC_OZAKI_BN", "PHPC_GROUP_ROWS", "PHPC_CLUSTER"):
+        del mats
+        torch.cuda.empty_cache()
+    for key in ("PHPC_OZAKI_BN", "PHPC_GROUP_ROWS", "PHPC_CLUSTER", "PHPC_STAGES"):
         os.environ.pop(key, None)
+
+    # 3xBF16 FP32 GEMM on the rectangular workload: tile width, raster, stages
+    fm, fk, fn = (int(x) for x in a.f32_shape.split(","))
+    g = torch.Generator(device="cuda").manual_seed(1)
+    A32 = torch.randn((fm, fk), dtype=torch.float32, device="cuda", generator=g)
+    B32 = torch.randn((fk, fn), dtype=torch.float32, device="cuda", generator=g)
+    C32 = torch.zeros((fm, fn), dtype=torch.float32, device="cuda")
+    rows = np.linspace(0, fm - 1, min(a.rows, fm)).astype(np.int32)
+    d_rows = torch.from_numpy(rows).cuda()
+    A64 = A32.index_select(0, d_rows.long()).double().contiguous()
+    R32 = torch.empty((len(rows), fn), dtype=torch.float64, device="cuda")
+    idx = torch.arange(len(rows), dtype=torch.int32, device="cuda")
+    phpc.dgemm_dd_rows_dev(len(rows), fk, fn, A64, fk, B32.double(), fn, None, fn, idx, len(rows), R32, fn, st)
+    ws32 = phpc.bf16x3_workspace_bytes(fm, fk, fn)
+    W32 = torch.empty(ws32, dtype=torch.uint8, device="cuda")
+    f32_best = None
+    for bn in (128, 256):
+        for gr in (4, 8, 16):
+            for stages in [0] + list(range(2, max_stages(bn, 1))):
+                os.environ["PHPC_F32_BN"] = str(bn)
+                os.environ["PHPC_GROUP_ROWS"] = str(gr)
+                set_cfg(256, gr, 1, stages)
+
+                def run32():
+                    phpc.sgemm_bf16x3_dev(fm, fk, fn, A32, fk, B32, fn, C32, fn, W32, ws32, st)
+
+                ms = median_ms(run32, a.reps)
+                C32.zero_()
+                run32()
+                got = C32.index_select(0, d_rows.long()).double()
+                err = float((got - R32).norm() / R32.norm())
+                rec = {"f32": [fm, fk, fn], "bn": bn, "group_rows": gr, "stages": stages, "ms": round(ms, 3),
+                       "tflops": round(2.0 * fm * fk * fn / ms / 1e9, 2), "err": err}
+                report.append(rec)
+                print(json.dumps(rec), flush=True)
+                if err <= 1e-6 and (f32_best is None or ms < f32_best["ms"]):
+                    f32_best = rec
+    for key in ("PHPC_F32_BN", "PHPC_GROUP_ROWS", "PHPC_STAGES"):
+        os.environ.pop(key, None)
+    del A32, B32, C32, W32, A64
+    torch.cuda.empty_cache()
+    if f32_best is None:
+        raise SystemExit("no 3xBF16 configuration meets 1e-6")
+
+    # plain FP64 GEMM: ring depth per size (DFMA pipe, phpc_gemm_cuda's default)
+    plain = []
+    for n in [x for x in sizes if x <= a.plain_max_n]:
+        A = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        B = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        C = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        phpc.fill_uniform_dev(A, n * n, 11, 0, st)
+        phpc.fill_uniform_dev(B, n * n, 12, 0, st)
+        best_p = None
+        for stages in (2, 3, 4, 5, 6):
+            os.environ["PHPC_DMMA_STAGES"] = str(stages)
+            ms = median_ms(lambda: phpc.dgemm_dmma_dev(n, n, n, A, n, B, n, C, n, 1, 1, 256, st), a.reps)
+            rec = {"plain_n": n, "stages": stages, "ms": round(ms, 3), "tflops": round(2.0 * n ** 3 / ms / 1e9, 4)}
+            report.append(rec)
+            print(json.dumps(rec), flush=True)
+            if best_p is None or ms < best_p["ms"]:
+                best_p = rec
+        plain.append(best_p)
+        del A, B, C
+        torch.cuda.empty_cache()
+    os.environ.pop("PHPC_DMMA_STAGES", None)
 
     assert phpc.device_status() == 0
     lines = [f"# written by autotune.py on {torch.cuda.get_device_name()} ({time.strftime('%Y-%m-%d %H:%M UTC', time.gmtime())})",
              f"# target Frobenius error {a.target} / margin {a.margin}, uniform and wide-exponent inputs",
-             "# max_mnk slices bn group_rows cluster moduli   (moduli 0 = digit scheme with `slices`)"]
+             "# max_mnk slices bn group_rows cluster moduli stages   (moduli 0 = digit scheme with `slices`;"
+             " stages 0 = the deepest ring)"]
     for i, b in enumerate(table):
         nxt = table[i + 1]["n"] if i + 1 < len(table) else None
         bound = int((b["n"] ** 3 * nxt ** 3) ** 0.5) if nxt else 2 ** 62
         lines.append(f"# N={b['n']}: {b['ms']} ms, {b['tflops']} TFLOP/s, err {b['err']}")
-        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']} {b['cluster']} {b['moduli']}")
-    lines.append(f"grouped {2 ** 62} 7 {grouped_bn}")
+        lines.append(f"{bound} {b['slices']} {b['bn']} {b['group_rows']} {b['cluster']} {b['moduli']} {b['stages']}")
+    lines.append(f"# grouped ({a.grouped_count} problems, {a.grouped_moduli} moduli): bn {grouped_bn}, stages "
+                 f"{grouped_stages}, {round(best_ms, 3) if best_ms else None} ms")
+    lines.append(f"grouped {2 ** 62} 7 {grouped_bn} {grouped_stages}")
+    fb = f32_best
+    lines.append(f"# f32 {fb['f32']}: {fb['ms']} ms, {fb['tflops']} TFLOP/s, err {fb['err']:.3e}")
+    lines.append(f"f32 {2 ** 62} {fb['bn']} {fb['group_rows']} {fb['stages']}")
+    for i, b in enumerate(plain):
+        nxt = plain[i + 1]["plain_n"] if i + 1 < len(plain) else None
+        bound = int((b["plain_n"] ** 3 * nxt ** 3) ** 0.5) if nxt else 2 ** 62
+        lines.append(f"# plain N={b['plain_n']}: {b['ms']} ms, {b['tflops']} TFLOP/s")
+        lines.append(f"plain {bound} {b['stages']}")
     Path(a.out).write_text("\n".join(lines) + "\n")
     print(f"wrote {a.out}")
     return 0

@@ -233,7 +233,7 @@ extern "C" int phpc_sgemm_bf16x3_dev(int m, int k, int n, const float* dA, int64
         rc = PHPC_ERR_CUDA;
       } else {
         const PairList pl = bf16x3_pairs();
-        rc = default_bn(m, k, n) == 128
+        rc = default_f32(m, k, n).bn == 128
                  ? launch_tc_slice_gemm<128, kF32>(pa, pb, 3, 3, L.ldp, m, n, k, pl, dC, ldc, nullptr, nullptr, st,
                                                    nullptr, 0, 0)
                  : launch_tc_slice_gemm<256, kF32>(pa, pb, 3, 3, L.ldp, m, n, k, pl, dC, ldc, nullptr, nullptr, st,

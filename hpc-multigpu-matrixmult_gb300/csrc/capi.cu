@@ -29,6 +29,10 @@ namespace {
 
 enum Method { kDmma, kOzakiMethod };
 
+// Device time of the last host call's phases on this thread (milliseconds):
+// scans and splits, tensor-core (or plain FP64) GEMM, CRT reconstruction.
+thread_local float t_phase_ms[3] = {0.f, 0.f, 0.f};
+
 struct Pinned {
   const void* ptr = nullptr;
   bool registered = false;
@@ -100,6 +104,7 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
 int host_gemm(Method method, const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k,
               int n, int gw, int gh, float* seconds) {
   if (seconds) *seconds = 0.f;
+  t_phase_ms[0] = t_phase_ms[1] = t_phase_ms[2] = 0.f;
   if (m < 0 || k < 0 || n < 0) return PHPC_ERR_ARG;
   if (m == 0 || n == 0) return PHPC_OK;
   if (!a || !b || !c || lda < k || ldb < n || ldc < n) return PHPC_ERR_ARG;
@@ -189,7 +194,11 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
     float kernel_ms = 0.f;
     if (rc == PHPC_OK && end_ev) {
       kernel_ms = elapsed_ms(r.ev[7], end_ev);
-      if (method == kOzakiMethod) kernel_ms += elapsed_ms(r.ev[3], r.ev[4]) + elapsed_ms(r.ev[5], r.ev[6]);
+      t_phase_ms[1] = kernel_ms;
+      if (method == kOzakiMethod) {
+        t_phase_ms[0] = elapsed_ms(r.ev[3], r.ev[4]) + elapsed_ms(r.ev[5], r.ev[6]);
+        kernel_ms += t_phase_ms[0];
+      }
     }
     if (rc == PHPC_OK && method == kOzakiMethod && (dstatus & 0xFF) == PHPC_ERR_NONFINITE) {
       // inf/NaN cannot be carried by integers: redo this call in IEEE
@@ -208,6 +217,8 @@ int host_gemm(Method method, const double* a, int lda, const double* b, int ldb,
       if (rc == PHPC_OK && cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
         rc = PHPC_ERR_CUDA;
       kernel_ms = elapsed_ms(r.ev[7], end_ev);
+      t_phase_ms[0] = 0.f;
+      t_phase_ms[1] = kernel_ms;
     }
     if (end_ev) cudaEventDestroy(end_ev);
     if (rc == PHPC_OK && dstatus != 0) rc = dstatus;
@@ -267,6 +278,7 @@ int b_panels(int rows, int n, int bn, int cl, int sms) {
 // the original C.
 int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k, int n,
                       int nmod, float* seconds) {
+  t_phase_ms[0] = t_phase_ms[1] = t_phase_ms[2] = 0.f;
   const DeviceInfo* dev = current_device();
   cudaMemPool_t pool = host_api_pool();
   int* status = device_status_ptr();
@@ -299,16 +311,14 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
     cudaStream_t sB = r.st[0], sA = r.st[1], sG = r.st[2], sC = sx[0], sO = sx[1], sS = sx[2];
     cudaEvent_t ev_alloc{}, ev_bcopy{}, ev_b1{}, ev_g0{}, ev_g1{}, ev_crt0{};
-    std::vector<cudaEvent_t> ev_a0(np), ev_a1(np), ev_c(np), ev_g(np);
+    // per row panel: A copied, A split; C copied; GEMM started (panels > 0) and
+    // done; CRT started and done
+    std::vector<cudaEvent_t> ev_a0(np), ev_a1(np), ev_c(np), ev_gs(np), ev_m(np), ev_cs(np), ev_g(np);
     // per B column panel: copied; split started, done; first row panel's block GEMM started, done
     std::vector<cudaEvent_t> ev_bc(nbpanels), ev_bs0(nbpanels), ev_bs1(nbpanels), ev_gb0(nbpanels), ev_gb1(nbpanels);
     for (cudaEvent_t* e : {&ev_alloc, &ev_bcopy, &ev_b1, &ev_g0, &ev_g1, &ev_crt0}) new_event(*e);
-    for (int p = 0; p < np; ++p) {
-      new_event(ev_a0[p]);
-      new_event(ev_a1[p]);
-      new_event(ev_c[p]);
-      new_event(ev_g[p]);
-    }
+    for (int p = 0; p < np; ++p)
+      for (auto* v : {&ev_a0, &ev_a1, &ev_c, &ev_gs, &ev_m, &ev_cs, &ev_g}) new_event((*v)[p]);
     for (int j = 0; j < nbpanels; ++j)
       for (auto* v : {&ev_bc, &ev_bs0, &ev_bs1, &ev_gb0, &ev_gb1}) new_event((*v)[j]);
     if (rc == PHPC_OK &&
@@ -382,10 +392,13 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
             cudaEventRecord(ev_gb1[j], sG);
           }
         } else {
+          cudaEventRecord(ev_gs[p], sG);
           rc = ozaki2_multiply_rows(m, r0, rows, k, n, nmod, r.ws, ws_bytes, sG, bn);
         }
+        cudaEventRecord(ev_m[p], sG);
         cudaStreamWaitEvent(sG, ev_c[p], 0);
         if (p == 0) cudaEventRecord(ev_crt0, sG);
+        cudaEventRecord(ev_cs[p], sG);
         if (rc == PHPC_OK) rc = ozaki2_reconstruct_rows(m, r0, rows, k, n, r.dC, dldc, nmod, r.ws, ws_bytes, sG);
         cudaEventRecord(ev_g[p], sG);
       }
@@ -442,6 +455,21 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       kernel_ms = elapsed_ms(ev_a0[0], ev_a1[0]) + elapsed_ms(ev_crt0, ev_g1);
       for (int j = 0; j < nbpanels; ++j)
         kernel_ms += elapsed_ms(ev_bs0[j], ev_bs1[j]) + elapsed_ms(ev_gb0[j], ev_gb1[j]);
+      // per phase: the spans of its kernels (later A splits run while GEMMs
+      // of earlier panels do, so the three can add up to more than kernel_ms)
+      float prep = 0.f, gemm = 0.f, crt = 0.f;
+      for (int j = 0; j < nbpanels; ++j) {
+        prep += elapsed_ms(ev_bs0[j], ev_bs1[j]);
+        gemm += elapsed_ms(ev_gb0[j], ev_gb1[j]);
+      }
+      for (int p = 0; p < np; ++p) {
+        prep += elapsed_ms(ev_a0[p], ev_a1[p]);
+        if (p > 0) gemm += elapsed_ms(ev_gs[p], ev_m[p]);
+        crt += elapsed_ms(ev_cs[p], ev_g[p]);
+      }
+      t_phase_ms[0] = prep;
+      t_phase_ms[1] = gemm;
+      t_phase_ms[2] = crt;
     }
     if (rc == PHPC_OK && nonfinite) {
       // inf/NaN cannot be carried by integers: redo the call in IEEE FP64
@@ -460,7 +488,11 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
            cudaStreamSynchronize(sB) != cudaSuccess ||
            cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
         rc = PHPC_ERR_CUDA;
-      if (rc == PHPC_OK) kernel_ms = elapsed_ms(ev_g0, ev_g1);
+      if (rc == PHPC_OK) {
+        kernel_ms = elapsed_ms(ev_g0, ev_g1);
+        t_phase_ms[0] = t_phase_ms[2] = 0.f;
+        t_phase_ms[1] = kernel_ms;
+      }
     }
     if (rc == PHPC_OK && dstatus != 0) rc = dstatus;
     if (rc == PHPC_OK && seconds) *seconds = kernel_ms / 1000.f;
@@ -503,4 +535,10 @@ extern "C" void phpc_gemm_cublas(const double* a, int lda, const double* b, int 
   else
     rc = phpc::host_gemm(phpc::kOzakiMethod, a, lda, b, ldb, c, ldc, m, k, n, 1, 1, gpu_time);
   phpc::set_last_error(rc);
+}
+
+extern "C" int phpc_last_phase_times(float* ms) {
+  if (!ms) return PHPC_ERR_ARG;
+  for (int i = 0; i < 3; ++i) ms[i] = phpc::t_phase_ms[i];
+  return PHPC_OK;
 }

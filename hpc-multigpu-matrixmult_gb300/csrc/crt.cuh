@@ -15,6 +15,8 @@ constexpr int kCrtMaxLimbs = 10;   // balanced 13-bit digits of M / m_i (15 modu
 struct CrtLimbs {
   int np;                                 // digits of the largest M / m_i (5 .. 10)
   float2 inv[kCrtMaxModuli];              // (M / m_i)^-1 mod m_i
+  float2 ninvb[kCrtMaxModuli];            // -2^23 (M / m_i)^-1 mod m_i
+  float2 cw[3];                           // 2^(13 j) / M rounded to float, j = np - 1, np - 2, np - 3
   float2 rm[kCrtMaxModuli];               // 1 / m_i rounded to float
   float2 negm[kCrtMaxModuli];             // -m_i
   float2 P[kCrtMaxModuli][kCrtMaxLimbs];  // balanced 13-bit digits of M / m_i, least significant first
@@ -212,49 +214,95 @@ __device__ __forceinline__ double crt_value(const uint32_t (&rr)[kCrtMaxModuli],
   return crt_round(l, T, fast, shift);
 }
 
+// c + y 2^x for a 128-bit two's complement integer y = (hi, lo), |y| < 2^127:
+// y is rounded once to double (to nearest even; the same rounding as
+// crt_round's) and the sum rounded once. The double y 2^x is assembled from
+// integer bits (sign, leading-one position, 53-bit mantissa), so the FP64
+// pipe, which is slow on this GPU, does one add per element.
+__device__ __forceinline__ double crt_add_i128(double c, uint64_t lo, uint64_t hi, int x) {
+  const uint64_t sign = hi & (1ull << 63);
+  if (sign) {  // magnitude
+    lo = ~lo + 1;
+    hi = ~hi + (lo == 0 ? 1 : 0);
+  }
+  if ((hi | lo) == 0) return c + 0.0;
+  uint64_t top, rest;
+  int e;  // position of the leading one
+  if (hi != 0) {
+    const int lz = __clzll(static_cast<long long>(hi));
+    top = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    rest = lz ? lo << lz : lo;
+    e = 127 - lz;
+  } else {
+    const int lz = __clzll(static_cast<long long>(lo));
+    top = lo << lz;
+    rest = 0;
+    e = 63 - lz;
+  }
+  uint64_t mant = top >> 11;  // 53 bits, leading one at bit 52
+  const uint64_t round_bit = (top >> 10) & 1, sticky = ((top & 0x3FF) | rest) != 0 ? 1 : 0;
+  mant += round_bit & (sticky | (mant & 1));
+  if (mant >> 53) {
+    mant >>= 1;
+    ++e;
+  }
+  const int E = e + 1023 + x;  // biased exponent of y 2^x
+  if (E >= 1 && E <= 2046)
+    return c + __longlong_as_double(static_cast<long long>(sign | (static_cast<uint64_t>(E) << 52) |
+                                                           (mant & ((1ull << 52) - 1))));
+  const double m = static_cast<double>(mant);  // outside the normal range: scale in double (rare)
+  return c + ldexp(sign ? -m : m, e - 52 + x);
+}
+
 // The one-step CRT of two adjacent elements on FP32 limbs, the two elements
 // in the two lanes of packed f32x2 operations. w[i] holds their residues mod
 // m_i (element 0 in the low 16 bits, element 1 in the high 16 bits). Valid
 // when every result satisfies |y| / M <= 1/2 - 1/32 (CrtTable::fast); gives
-// the same y, rounded the same way, as crt_value. Steps (every one except the
-// two rounding estimates is exact in FP32: all values are integers below 2^24):
-//  1. t_i = r_i inv_i mod m_i, symmetric: p = r_i inv_i < 2^17, t_i = p -
-//     round(p / m_i) m_i (|t_i| <= m_i / 2); sum_i t_i (M / m_i) = y (mod M);
+// the y of crt_value as a 128-bit two's complement integer (y0, y1). Every
+// step except the quotient estimate is exact in FP32 (all values are
+// integers below 2^24):
+//  1. t_i = r_i inv_i mod m_i, symmetric: with r_i read as the float
+//     2^23 + r_i, p = (2^23 + r_i) inv_i - 2^23 inv_i = r_i inv_i < 2^17 in one
+//     FMA, t_i = p - round(p / m_i) m_i (|t_i| <= m_i / 2), and
+//     sum_i t_i (M / m_i) = y (mod M);
 //  2. S_j = sum_i t_i P_ij over the balanced 13-bit digits P_ij of M / m_i
 //     (|P_ij| <= 2^12, |S_j| <= 15 181 2^12 < 2^24);
-//  3. q = round(sum_i t_i / m_i) (|q| <= 8; exact under the fast path's margin);
-//  4. Y_j = S_j - q M_j (|Y_j| < 2^24), digits of y = sum_j Y_j 2^(13 j);
-//  5. carries: h_j = round(Y_j 2^-13), d_j = (Y_j - h_j 2^13) + h_(j-1)
+//  3. q = round(sum_i t_i / m_i) from the top three limb sums,
+//     est = sum_j S_j fl(2^(13 j) / M) (|est| <= 7.5, error below 2^-19; the
+//     lower limbs weigh below 2^-27); exact under the fast path's margin;
+//  4. Y_j = S_j - q M_j (|Y_j| < 2^24), the limbs of y = sum_j Y_j 2^(13 j);
+//  5. carries: h_j = round(Y_j 2^-13), digits d_j = (Y_j - h_j 2^13) + h_(j-1)
 //     (|d_j| < 2^13), read out as integers through the rounding constant
-//     1.5 2^23, and y = sum_j d_j 2^(13 j) mod 2^128 (|y| < 2^127).
+//     1.5 2^23; four digits make a 52-bit chunk (int64), and
+//     y = A + B 2^52 + C 2^104 for the chunks A, B, C.
 // NP = T.L.np, the number of digits of the largest M / m_i.
 template <int NP>
-__device__ __forceinline__ void crt_limbs_pair(const uint32_t (&w)[kCrtMaxModuli], const CrtTable& T, double& v0,
-                                               int& s0, double& v1, int& s1) {
+__device__ __forceinline__ void crt_limbs_pair(const uint32_t (&w)[kCrtMaxModuli], const CrtTable& T,
+                                               uint64_t (&lo)[2], uint64_t (&hi)[2]) {
   const float2 kRound = make_float2(12582912.0f, 12582912.0f), kUnround = make_float2(-12582912.0f, -12582912.0f);
-  const float2 kUnbias = make_float2(-8388608.0f, -8388608.0f);
   const float2 kDigit = make_float2(0x1p-13f, 0x1p-13f), kNegBase = make_float2(-8192.0f, -8192.0f);
   float2 S[NP];
 #pragma unroll
   for (int j = 0; j < NP; ++j) S[j] = make_float2(0.0f, 0.0f);
-  float2 est = make_float2(0.0f, 0.0f);
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i) {
     if (i < T.n) {
-      // r as floats: 2^23 + r has r in its mantissa bits
-      const float2 r = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | (w[i] & 0xFFFFu)),
-                                              __uint_as_float(0x4B000000u | (w[i] >> 16))),
-                                  kUnbias);
-      const float2 p = __fmul2_rn(r, T.L.inv[i]);
+      const float2 rb = make_float2(__uint_as_float(0x4B000000u | (w[i] & 0xFFFFu)),
+                                    __uint_as_float(0x4B000000u | (w[i] >> 16)));
+      const float2 p = __ffma2_rn(rb, T.L.inv[i], T.L.ninvb[i]);
       const float2 qq = __fadd2_rn(__ffma2_rn(p, T.L.rm[i], kRound), kUnround);
       const float2 t = __ffma2_rn(qq, T.L.negm[i], p);
-      est = __ffma2_rn(t, T.L.rm[i], est);
 #pragma unroll
       for (int j = 0; j < NP; ++j) S[j] = __ffma2_rn(t, T.L.P[i][j], S[j]);
     }
   }
+  float2 est = __fmul2_rn(S[NP - 1], T.L.cw[0]);
+  est = __ffma2_rn(S[NP - 2], T.L.cw[1], est);
+  est = __ffma2_rn(S[NP - 3], T.L.cw[2], est);
   const float2 q = __fadd2_rn(__fadd2_rn(est, kRound), kUnround);
-  int d0[NP + 2], d1[NP + 2];
+  int d0[12], d1[12];  // digits; those above NP + 1 are zero
+#pragma unroll
+  for (int j = 0; j < 12; ++j) d0[j] = d1[j] = 0;
   float2 hprev = make_float2(0.0f, 0.0f);
 #pragma unroll
   for (int j = 0; j <= NP; ++j) {
@@ -270,19 +318,21 @@ __device__ __forceinline__ void crt_limbs_pair(const uint32_t (&w)[kCrtMaxModuli
     d0[NP + 1] = __float_as_int(d.x) - 0x4B400000;
     d1[NP + 1] = __float_as_int(d.y) - 0x4B400000;
   }
-  // y = sum_j d_j 2^(13 j) modulo 2^128, most significant digit first
-  using u128 = unsigned __int128;
-  u128 y0 = 0, y1 = 0;
+  // 52-bit chunks of four digits: |chunk| < 2^52 (int64 exact)
+  auto chunk = [](const int (&d)[12], int j0) -> int64_t {
+    const int32_t a = d[j0] + d[j0 + 1] * 8192, b = d[j0 + 2] + d[j0 + 3] * 8192;
+    return static_cast<int64_t>(a) + static_cast<int64_t>(b) * 67108864;
+  };
 #pragma unroll
-  for (int j = NP + 1; j >= 0; --j) {
-    y0 = (y0 << 13) + static_cast<u128>(static_cast<__int128>(d0[j]));
-    y1 = (y1 << 13) + static_cast<u128>(static_cast<__int128>(d1[j]));
+  for (int e = 0; e < 2; ++e) {
+    const int(&d)[12] = e ? d1 : d0;
+    const int64_t A = chunk(d, 0), B = chunk(d, 4), C = chunk(d, 8);
+    // y = A + B 2^52 + C 2^104 modulo 2^128
+    const uint64_t b_lo = static_cast<uint64_t>(B) << 52;
+    lo[e] = static_cast<uint64_t>(A) + b_lo;
+    hi[e] = static_cast<uint64_t>(A >> 63) + static_cast<uint64_t>(B >> 12) + (static_cast<uint64_t>(C) << 40) +
+            (lo[e] < b_lo ? 1 : 0);
   }
-  const bool n0 = static_cast<uint64_t>(y0 >> 64) >> 63, n1 = static_cast<uint64_t>(y1 >> 64) >> 63;
-  if (n0) y0 = ~y0 + 1;
-  if (n1) y1 = ~y1 + 1;
-  v0 = round_magnitude(static_cast<uint64_t>(y0 >> 64), static_cast<uint64_t>(y0), n0, s0);
-  v1 = round_magnitude(static_cast<uint64_t>(y1 >> 64), static_cast<uint64_t>(y1), n1, s1);
 }
 
 // *c += v * 2^(shift + e): the CRT result of one element applied to C

@@ -6,8 +6,9 @@
 //    grid (grid_width x grid_height blocks of C, src/phpc_summa.c:36-44),
 //    block by block, so the CTAs working at one time share A row panels and
 //    B column panels in L2;
-//  - a producer warp that streams the k-panels of A and B into a 4-stage
-//    shared-memory ring with TMA (the on-device form of the reference's
+//  - a producer warp that streams the k-panels of A and B into a shared-memory
+//    ring of 2-6 stages (4 unless PHPC_DMMA_STAGES or the tuning table's
+//    "plain" entry says otherwise) with TMA (the on-device form of the reference's
 //    per-panel row/column broadcasts, src/phpc_summa.c:63-89);
 //  - consumer warps computing 32 x 32 outputs each with FP64 accumulation in
 //    registers over the whole K range, on the scalar FP64 pipe (DFMA, the
@@ -27,8 +28,9 @@
 namespace phpc {
 namespace {
 
-constexpr int kBK = 16;      // doubles of K per stage (one 128-byte row of A)
-constexpr int kStages = 4;
+constexpr int kBK = 16;         // doubles of K per stage (one 128-byte row of A)
+constexpr int kDefaultStages = 4;
+constexpr int kMaxStages = 6;   // ring depth bounds (PHPC_DMMA_STAGES, tuning table)
 
 struct SummaGrid {
   int tm, tn;   // tiles along M and N
@@ -65,7 +67,7 @@ struct DmmaCfg {
   static constexpr int kStageA = BM * kBK * 8;
   static constexpr int kStageB = kBK * BN * 8;
   static constexpr int kStageBytes = kStageA + kStageB;
-  static constexpr size_t kSmem = (size_t)kStages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/;
+  static constexpr size_t smem(int stages) { return (size_t)stages * kStageBytes + 1024 /*align*/ + 256 /*barriers*/; }
 };
 
 // DFMA = false: mma.sync.m16n8k4.f64 (FP64 tensor cores); true: the same
@@ -75,12 +77,13 @@ struct DmmaCfg {
 template <int BM, int BN, bool DFMA>
 __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
     dmma_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, double* C,
-                     int64_t ldc, int M, int N, int K, int kpanel, SummaGrid grid, int* status) {
+                     int64_t ldc, int M, int N, int K, int kpanel, SummaGrid grid, int stages, int* status) {
   using Cfg = DmmaCfg<BM, BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * Cfg::kStageBytes);
-  uint64_t* empty = full + kStages;
+  const int S = stages;  // ring depth, 2 .. kMaxStages (checked by the launcher)
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * Cfg::kStageBytes);
+  uint64_t* empty = full + S;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = grid.tm * grid.tn;
@@ -88,7 +91,7 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
   const int kp_steps = max(1, kpanel / kBK);  // BK steps per SUMMA k-panel
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], Cfg::kConsumers);
     }
@@ -118,7 +121,7 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
             tma_load_2d(sa, &tmA, ks * kBK, rm * BM, &full[stage]);
             tma_load_2d(sa + Cfg::kStageA, &tmB, rn * BN, ks * kBK, &full[stage]);
             ++issued;
-            if (++stage == kStages) { stage = 0; phase ^= 1; }
+            if (++stage == S) { stage = 0; phase ^= 1; }
           }
         }
       }
@@ -126,8 +129,8 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
         // Let the copies already in flight land before the CTA exits.
         int s = stage;
         uint32_t ph = phase;
-        for (int i = 0; i < min(issued, kStages); ++i) {
-          if (--s < 0) { s = kStages - 1; ph ^= 1; }
+        for (int i = 0; i < min(issued, S); ++i) {
+          if (--s < 0) { s = S - 1; ph ^= 1; }
           const uint32_t addr = smem_u32(&full[s]);
           const uint64_t t0 = globaltimer_ns();
           while (!mbar_try_wait(addr, ph) && globaltimer_ns() - t0 < PHPC_WAIT_LIMIT_NS) {}
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(DmmaCfg<BM, BN>::kThreads)
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[stage]);
-        if (++stage == kStages) { stage = 0; phase ^= 1; }
+        if (++stage == S) { stage = 0; phase ^= 1; }
       }
       if (!ok) break;
       // Epilogue: C += tile (rows g and g+8 of each m16 block, two adjacent columns).
@@ -249,18 +252,28 @@ int launch_dmma(int m, int k, int n, const double* dA, int64_t lda, const double
   g.gw = std::min(gw, g.tn);
   const int ntiles = g.tm * g.tn;
   auto kern = dmma_gemm_kernel<BM, BN, DFMA>;
-  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::kSmem));
+  const int stages = default_plain_stages(m, k, n);
+  if (stages < 2 || stages > kMaxStages) return PHPC_ERR_ARG;
+  const size_t smem = Cfg::smem(stages);
+  PHPC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 1;
-  PHPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::kThreads, Cfg::kSmem));
+  PHPC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::kThreads, smem));
   per_sm = std::max(1, per_sm);
   const int nblocks = std::min(ntiles, dev->sm_count * per_sm);
-  kern<<<nblocks, Cfg::kThreads, Cfg::kSmem, stream>>>(tmA, tmB, dC, ldc, m, n, k, kpanel, g,
+  kern<<<nblocks, Cfg::kThreads, smem, stream>>>(tmA, tmB, dC, ldc, m, n, k, kpanel, g, stages,
                                                                              device_status_ptr());
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
 }
 
 }  // namespace
+
+// The FP64 pipe of the plain GEMM: the scalar FMA units (DFMA, default) or the
+// FP64 tensor cores (PHPC_FP64_PIPE=dmma); same bits either way.
+bool fp64_pipe_is_dfma() {
+  const char* pipe = getenv("PHPC_FP64_PIPE");
+  return !(pipe && strcmp(pipe, "dmma") == 0);
+}
 
 // Tile shape: 128 x 128 when there are at least two waves of such tiles,
 // else 64 x 64 so that small problems still spread over the SMs.
@@ -272,8 +285,7 @@ int dgemm_dmma(int m, int k, int n, const double* dA, int64_t lda, const double*
   const int64_t tiles128 = (int64_t)ceil_div(m, 128) * ceil_div(n, 128);
   const char* force = getenv("PHPC_DMMA_TILE");
   const bool big = force ? atoi(force) == 128 : tiles128 >= 2 * dev->sm_count;
-  const char* pipe = getenv("PHPC_FP64_PIPE");
-  const bool dfma = !(pipe && strcmp(pipe, "dmma") == 0);
+  const bool dfma = fp64_pipe_is_dfma();
   if (big)
     return dfma ? launch_dmma<128, 128, true>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream)
                 : launch_dmma<128, 128, false>(m, k, n, dA, lda, dB, ldb, dC, ldc, gw, gh, kpanel, stream);
@@ -303,3 +315,5 @@ extern "C" int phpc_dgemm_dmma_dev(int m, int k, int n, const double* dA, int64_
   set_last_error(rc);
   return rc;
 }
+
+extern "C" const char* phpc_fp64_pipe_name(void) { return phpc::fp64_pipe_is_dfma() ? "dfma" : "dmma"; }

@@ -331,6 +331,7 @@ PairList residue_pairs(const ModTable& T) {
 struct phpc_grouped_plan {
   int device;
   int count, s, moduli, bn;  // moduli > 0: modular scheme (s unused)
+  int stages;                // K-stages of the tensor-core GEMM's ring (0 = the deepest)
   int total_rows, total_cols, total_sblocks, total_rblocks, total_tiles, total_pieces, total_cunits,
       total_crt_units;
   phpc::GSplitProb* d_split;
@@ -351,6 +352,7 @@ int launch_grouped_gemm(const phpc_grouped_plan* pl, cudaStream_t stream) {
   if (!dev) return PHPC_ERR_CUDA;
   TcArgs a{};
   a.status = device_status_ptr();
+  a.stages = pl->stages;
   if (MODE == kResidue) {  // (tile, modulus) work units, moduli outer, unless PHPC_SPLIT_MODULI=0
     const char* env = getenv("PHPC_SPLIT_MODULI");
     a.split_pairs = env ? (atoi(env) != 0 ? 1 : 0) : 1;
@@ -450,6 +452,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->s = modular ? 0 : planes;
   pl->moduli = modular ? planes : 0;
   pl->bn = default_grouped_bn(problems, count);
+  pl->stages = default_grouped_stages(problems, count);
   if (modular) {
     int kmax = 1;
     for (int i = 0; i < count; ++i) kmax = std::max(kmax, problems[i].k);

@@ -111,7 +111,9 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   const uint64_t sB[2] = {(uint64_t)ldp * 2, (uint64_t)ldp * 2 * b_plane_rows};
   const int cm = opt.cfg_m > 0 ? opt.cfg_m : m, cn = opt.cfg_n > 0 ? opt.cfg_n : n,
             ck = opt.cfg_k > 0 ? opt.cfg_k : k;
-  const int cluster = default_cluster(cm, ck, cn);
+  // the 3xBF16 GEMM has its own table entries ("f32") and runs on single CTAs
+  const F32Tune f32 = MODE == kF32 ? default_f32(cm, ck, cn) : F32Tune{};
+  const int cluster = MODE == kF32 ? 1 : default_cluster(cm, ck, cn);
   const uint32_t bB[3] = {kTcBK, (uint32_t)(BN / cluster), 1};  // with a 2-CTA cluster each CTA loads half of B
   if (!encode_tiled(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesA, dA, sA, bA, CU_TENSOR_MAP_SWIZZLE_128B) ||
       !encode_tiled(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, planesB, dB, sB, bB, CU_TENSOR_MAP_SWIZZLE_128B))
@@ -122,7 +124,8 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.K = k;
   a.tm = ceil_div(m, kTcBM);
   a.tn = ceil_div(n, BN);
-  a.group_rows = default_group_rows(cm, ck, cn);
+  a.group_rows = MODE == kF32 ? f32.group_rows : default_group_rows(cm, ck, cn);
+  a.stages = MODE == kF32 ? f32.stages : default_stages(cm, ck, cn);
   a.C = C;
   a.ldc = ldc;
   a.ea = ea;

@@ -15,7 +15,10 @@
 //                           kind 2 (iters iterations): shows whether the two
 //                           FP64 pipes add up or share one datapath
 // Work is counted as 2 flops per multiply-add (2*M*N*K per mma instruction).
+// phpc_link_probe times SM loads and stores over the host link: a kernel that
+// copies between page-locked host memory and HBM.
 #include <cstdint>
+#include <cstring>
 
 #include "phpc_host.hpp"
 
@@ -198,8 +201,61 @@ int run_probe(int kind, int blocks, int threads, int64_t iters, int64_t iters2, 
   return rc;
 }
 
+// Host-link probe: one grid-stride copy of n 16-byte words between
+// page-locked host memory (through its device address) and device memory.
+__global__ void link_copy_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+int run_link_probe(int to_host, size_t bytes, int blocks, float* ms) {
+  void *host = nullptr, *dev = nullptr, *host_dev = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = PHPC_OK;
+  if (cudaHostAlloc(&host, bytes, cudaHostAllocMapped) != cudaSuccess || cudaMalloc(&dev, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    rc = PHPC_ERR_NOMEM;
+  } else if (cudaHostGetDevicePointer(&host_dev, host, 0) != cudaSuccess ||
+             cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+             cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = PHPC_ERR_CUDA;
+  } else {
+    memset(host, 0, bytes);
+    const uint4* src = static_cast<const uint4*>(to_host ? dev : host_dev);
+    uint4* dst = static_cast<uint4*>(to_host ? host_dev : dev);
+    const size_t n = bytes / 16;
+    link_copy_kernel<<<blocks, 1024, 0, st>>>(src, dst, n / 8);  // warm-up
+    cudaEventRecord(e0, st);
+    link_copy_kernel<<<blocks, 1024, 0, st>>>(src, dst, n);
+    cudaEventRecord(e1, st);
+    if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)
+      rc = PHPC_ERR_CUDA;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (dev) cudaFree(dev);
+  if (host) cudaFreeHost(host);
+  return rc;
+}
+
 }  // namespace
 }  // namespace phpc
+
+extern "C" int phpc_link_probe(int to_host, size_t bytes, int blocks, float* ms) {
+  using namespace phpc;
+  int rc;
+  if ((to_host != 0 && to_host != 1) || bytes < (1u << 20) || (bytes % 16) || blocks < 1 || blocks > 65535 || !ms)
+    rc = PHPC_ERR_ARG;
+  else if (!current_device())
+    rc = PHPC_ERR_CUDA;
+  else
+    rc = run_link_probe(to_host, bytes, blocks, ms);
+  set_last_error(rc);
+  return rc;
+}
 
 extern "C" int phpc_pipe_probe(int kind, int blocks, int threads, int64_t iters, int64_t iters2, float* ms,
                                double* flops) {

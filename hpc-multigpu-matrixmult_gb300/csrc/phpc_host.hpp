@@ -45,6 +45,7 @@ bool encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const v
   } while (0)
 
 // Library-internal launchers (device pointers, asynchronous on `stream`).
+bool fp64_pipe_is_dfma();
 int dgemm_dmma(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
                int64_t ldc, int gw, int gh, int kpanel, cudaStream_t stream);
 int dgemm_ozaki(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
@@ -92,6 +93,19 @@ int default_bn(int m, int k, int n);
 int default_grouped_bn(const phpc_gemm_problem* problems, int count);
 int default_group_rows(int m, int k, int n);
 int default_cluster(int m, int k, int n);
+// Pipeline depths: K-stages of the tcgen05 engine's shared-memory ring for
+// the FP64-accurate GEMMs (0 = the deepest ring that fits), of the 3xBF16
+// FP32 GEMM, and of the plain FP64 GEMM (2 .. 6).
+int default_stages(int m, int k, int n);
+int default_plain_stages(int m, int k, int n);
+// 3xBF16 FP32 GEMM: tile width, raster height and stages from the table's
+// "f32" entries (PHPC_F32_BN / PHPC_GROUP_ROWS / PHPC_STAGES override).
+struct F32Tune {
+  int bn, group_rows, stages;
+};
+F32Tune default_f32(int m, int k, int n);
+// Stages of the grouped GEMM (the "grouped" entry's fifth field; 0 = deepest).
+int default_grouped_stages(const phpc_gemm_problem* problems, int count);
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 

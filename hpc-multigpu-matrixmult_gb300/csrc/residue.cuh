@@ -124,11 +124,17 @@ inline ModTable make_table(int nmod, int k) {
     for (uint32_t v = 1; v < m; ++v)
       if ((static_cast<uint64_t>(static_cast<uint32_t>(Mi % m)) * v) % m == 1) { inv = v; break; }
     T.crt.L.inv[i] = make_float2(static_cast<float>(inv), static_cast<float>(inv));
+    const float nb = -8388608.0f * static_cast<float>(inv);  // exact: inv < 2^9
+    T.crt.L.ninvb[i] = make_float2(nb, nb);
     T.crt.L.rm[i] = T.invm[i];
     T.crt.L.negm[i] = T.negm[i];
     np = std::max(np, digits(Mi, T.crt.L.P[i], kCrtMaxLimbs));
   }
   T.crt.L.np = np;
+  for (int j = 0; j < 3; ++j) {
+    const float c = static_cast<float>(std::ldexp(1.0, 13 * (np - 1 - j)) / static_cast<double>(M));
+    T.crt.L.cw[j] = make_float2(c, c);
+  }
   float2 Md[kCrtMaxLimbs + 1];
   digits(M, Md, kCrtMaxLimbs + 1);
   for (int j = 0; j <= kCrtMaxLimbs; ++j) T.crt.L.negM[j] = make_float2(-Md[j].x, -Md[j].y);
@@ -384,21 +390,22 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
       w01[i] = rw[i].x;
       w23[i] = rw[i].y;
     }
-    double v[kCrtCols];
-    int sh[kCrtCols];
-    crt_limbs_pair<NP>(w01, T, v[0], sh[0], v[1], sh[1]);
-    crt_limbs_pair<NP>(w23, T, v[2], sh[2], v[3], sh[3]);
+    uint64_t lo01[2], hi01[2], lo23[2], hi23[2];
+    crt_limbs_pair<NP>(w01, T, lo01, hi01);
+    crt_limbs_pair<NP>(w23, T, lo23, hi23);
+    const uint64_t lo[kCrtCols] = {lo01[0], lo01[1], lo23[0], lo23[1]};
+    const uint64_t hi[kCrtCols] = {hi01[0], hi01[1], hi23[0], hi23[1]};
     if (ncols == kCrtCols) {
       double cv[kCrtCols];
 #pragma unroll
       for (int c = 0; c < kCrtCols; ++c) cv[c] = cp[c];
 #pragma unroll
       for (int c = 0; c < kCrtCols; ++c)
-        cp[c] = crt_added(cv[c], v[c], sh[c] + row_shift + max(ebp[c], -20000) - bbp[c]);
+        cp[c] = crt_add_i128(cv[c], lo[c], hi[c], row_shift + max(ebp[c], -20000) - bbp[c]);
     } else {
 #pragma unroll
       for (int c = 0; c < kCrtCols; ++c)
-        if (c < ncols) crt_apply(cp + c, v[c], sh[c] + row_shift + max(ebp[c], -20000) - bbp[c]);
+        if (c < ncols) cp[c] = crt_add_i128(cp[c], lo[c], hi[c], row_shift + max(ebp[c], -20000) - bbp[c]);
     }
     return;
   }

@@ -115,6 +115,7 @@ struct TcArgs {
   int64_t ldr;                // kResidue: row stride of a residue plane in elements (multiple of 16)
   int64_t rplane;             // kResidue: plane stride in elements
   int split_pairs;            // kResidue, one CTA per tile: a work unit is one (tile, modulus), moduli outer
+  int stages;                 // K-stages of the ring in use, 2 .. TcCfg::kStages (other values: kStages)
 };
 
 // Grouped mode: many independent problems in one persistent launch. The
@@ -258,15 +259,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                          const __grid_constant__ TcGroupTable gt) {
   static_assert(CLUSTER == 1 || (CLUSTER == 2 && !GROUPED), "the CTA pair computes tiles of one problem");
   using Cfg = TcCfg<BN, CLUSTER>;
-  constexpr int S = Cfg::kStages;
+  // The shared-memory layout is that of the deepest ring; the ring in use has
+  // S stages (the tuning table's pipeline depth).
+  constexpr int SMAX = Cfg::kStages;
+  const int S = (args.stages >= 2 && args.stages < SMAX) ? args.stages : SMAX;
   constexpr int HALF = BN / 2;
   constexpr uint16_t kPair = 0x3;  // multicast mask: both CTAs of the pair
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* scratch = smem + S * Cfg::kStageBytes;
+  uint8_t* scratch = smem + SMAX * Cfg::kStageBytes;
   uint64_t* full = reinterpret_cast<uint64_t*>(scratch + kTcEpiWarps * Cfg::kScratchPerWarp);
-  uint64_t* empty = full + S;
-  uint64_t* tfull = empty + S;      // [2] MMA -> epilogue
+  uint64_t* empty = full + SMAX;
+  uint64_t* tfull = empty + SMAX;   // [2] MMA -> epilogue
   uint64_t* tempty = tfull + 2;     // [2] epilogue -> MMA
   uint64_t* drain = tempty + 2;     // MMA issuer waits here for its last MMAs before teardown
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   int* status = args.status;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < S; ++s) {
+    for (int s = 0; s < SMAX; ++s) {
       mbar_init(&full[s], 1);   // pair: the leader's, fed by both CTAs' loads
       mbar_init(&empty[s], 1);  // pair: the leader's commit, multicast to both CTAs
     }

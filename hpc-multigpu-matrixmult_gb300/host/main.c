@@ -9,8 +9,8 @@
  *   N,size,gpu_count,num_blocks,threads_per_block,total_threads,
  *   cuda_time,cuda_gpu_time,cublas_time
  * "cuda" is the plain FP64 SUMMA (phpc_gemm_cuda), "cublas" the FP64-accurate
- * Ozaki SUMMA (phpc_gemm_cublas); the _ext.csv method names are "dmma" and
- * "ozaki_split" for them.
+ * Ozaki SUMMA (phpc_gemm_cublas); the _ext.csv method names are the FP64
+ * pipe that ran ("dfma" or "dmma", phpc_fp64_pipe_name) and "ozaki_split".
  *
  * Differences from the reference, all opt-in or corrective:
  *  - C is zeroed before each method (the reference accumulated the second
@@ -21,7 +21,15 @@
  *  - a second file, <same name>_ext.csv, records per method the wall and
  *    device seconds, FP64-equivalent TFLOP/s (2 N^3 / device time) and, for
  *    the index inputs, the max-abs and Frobenius relative errors against the
- *    exact closed-form product (nan for the other inputs).
+ *    exact closed-form product (nan for the other inputs); then the device
+ *    time of each phase of the last local GEMM call (phpc_last_phase_times:
+ *    scans + splits, GEMM, CRT reconstruction, in ms) with its algorithmic
+ *    rate: the splits' HBM GB/s (read A and B once, write the BF16 planes),
+ *    the GEMM's TFLOP/s (BF16 tensor-core flops of the split GEMMs; FP64 flops
+ *    of the plain GEMM) and the reconstruction's HBM GB/s (read the 16-bit
+ *    residues, read and write C). With one rank the last local call is the
+ *    whole product; with several it is rank 0's last panel (the panel
+ *    accumulator reports no phases: zeros).
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -119,7 +127,9 @@ int main(int argc, char *argv[]) {
              tile_width, grid_width, grid_height);
     ext = fopen(filename, "w");
     CHECK_OR_ABORT(ext, "Error: Could not create CSV file %s\n", filename);
-    fprintf(ext, "method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err\n");
+    fprintf(ext,
+            "method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err,split_ms,gemm_ms,crt_ms,split_gbs,"
+            "gemm_tflops,crt_gbs\n");
   }
 
   const char *dist = getenv("PHPC_DIST");
@@ -150,6 +160,8 @@ int main(int argc, char *argv[]) {
     else
       phpc_gemm_summa_cublas(grid_comm, A, B, C, N, gpu_count, &dev[1]);
     wall[method] = get_cur_time() - t0;
+    float phase[3] = {0.f, 0.f, 0.f};
+    phpc_last_phase_times(phase);
     const int err = phpc_summa_last_error();
     CHECK_OR_ABORT(err == 0, "Error: %s GEMM failed with status %d (%s)\n", method ? "split" : "plain", err,
                    phpc_error_string(err));
@@ -158,8 +170,17 @@ int main(int argc, char *argv[]) {
     if (rank == 0) {
       double max_rel = NAN, frob_rel = NAN;
       if (is_index) index_errors(C, N, &max_rel, &frob_rel);
-      fprintf(ext, "%s,%d,%f,%f,%f,%.3e,%.3e\n", method ? "ozaki_split" : "dmma", N, wall[method], dev[method],
-              dev[method] > 0 ? flops / dev[method] * 1e-12 : 0.0, max_rel, frob_rel);
+      /* algorithmic work of each phase (N x N x N): planes = moduli or slices */
+      const int q = phpc_default_moduli(N, N, N), s = phpc_default_slices(N, N, N);
+      const double planes = method ? (q ? q : s) : 0, gemms = method ? (q ? q : s * (s + 1) / 2.0) : 1;
+      const double nn = (double)N * N;
+      const double split_bytes = (8.0 + 2.0 * planes) * 2.0 * nn, crt_bytes = (2.0 * planes + 16.0) * nn;
+      fprintf(ext, "%s,%d,%f,%f,%f,%.3e,%.3e,%.3f,%.3f,%.3f,%.1f,%.2f,%.1f\n",
+              method ? "ozaki_split" : phpc_fp64_pipe_name(), N, wall[method], dev[method],
+              dev[method] > 0 ? flops / dev[method] * 1e-12 : 0.0, max_rel, frob_rel, phase[0], phase[1], phase[2],
+              phase[0] > 0 ? split_bytes / phase[0] * 1e-6 : 0.0,
+              phase[1] > 0 ? gemms * flops / phase[1] * 1e-9 : 0.0,
+              phase[2] > 0 && method && q ? crt_bytes / phase[2] * 1e-6 : 0.0);
     }
   }
 

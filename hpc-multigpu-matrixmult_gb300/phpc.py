@@ -97,6 +97,8 @@ _lib.phpc_default_moduli.restype = ct.c_int
 _lib.phpc_pipe_probe.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int64, ct.c_int64, ct.POINTER(ct.c_float),
                                  ct.POINTER(ct.c_double)]
 _lib.phpc_pipe_probe.restype = ct.c_int
+_lib.phpc_link_probe.argtypes = [ct.c_int, ct.c_size_t, ct.c_int, ct.POINTER(ct.c_float)]
+_lib.phpc_link_probe.restype = ct.c_int
 
 
 class GemmProblem(ct.Structure):
@@ -405,6 +407,13 @@ def pipe_probe(kind: int, blocks: int, threads: int, iters: int, iters2: int = 0
     _check(_lib.phpc_pipe_probe(kind, blocks, threads, iters, iters2, ct.byref(ms), ct.byref(fl)),
            "phpc_pipe_probe")
     return ms.value, fl.value
+
+
+def link_probe(to_host: bool, nbytes: int, blocks: int) -> float:
+    """phpc_link_probe: device milliseconds of a kernel copying nbytes over the host link."""
+    ms = ct.c_float(0.0)
+    _check(_lib.phpc_link_probe(1 if to_host else 0, nbytes, blocks, ct.byref(ms)), "phpc_link_probe")
+    return ms.value
 
 
 def device_status() -> int:

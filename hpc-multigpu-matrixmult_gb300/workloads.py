@@ -22,6 +22,8 @@ that bench.py prints:
                   and through the device-resident panel accumulator.
 * ``pipe_peaks``  the register-only throughput probes of the arithmetic pipes
                   (DFMA, DMMA shapes, IMMA, FFMA).
+* ``host_link``   the host link: copy-engine copies (each way and both at
+                  once) and kernels that read or write page-locked host memory.
 """
 from __future__ import annotations
 
@@ -306,4 +308,32 @@ def pipe_peaks(phpc, sm_count: int, target_ms: float = 150.0) -> dict:
     ms, fl = phpc.pipe_probe(7, blocks, threads, it_mma, it_fma)
     out[phpc.PIPE_PROBES[7]] = {"tflops": round(fl / ms / 1e9, 4), "ms": round(ms, 2), "iters_dmma": it_mma,
                                 "iters_dfma": it_fma, "sum_of_alone": round(dfma + dmma, 4)}
+    return out
+
+
+def host_link(torch, phpc, nbytes: int = 2 << 30, reps: int = 3) -> dict:
+    st = torch.cuda.current_stream()
+    n = nbytes // 8
+    h_in = torch.ones(n, dtype=torch.float64).pin_memory()
+    h_out = torch.empty(n, dtype=torch.float64).pin_memory()
+    d_in = torch.empty(n, dtype=torch.float64, device="cuda")
+    d_out = torch.ones(n, dtype=torch.float64, device="cuda")
+    side = torch.cuda.Stream()
+
+    def both():
+        side.wait_stream(st)
+        with torch.cuda.stream(side):
+            h_out.copy_(d_out, non_blocking=True)
+        d_in.copy_(h_in, non_blocking=True)
+        st.wait_stream(side)
+
+    gbs = lambda ms: round(nbytes / ms / 1e6, 1)  # noqa: E731
+    out = {"bytes": nbytes,
+           "ce_h2d_gbs": [gbs(x) for x in timed_ms(torch, st, lambda: d_in.copy_(h_in, non_blocking=True), reps)],
+           "ce_d2h_gbs": [gbs(x) for x in timed_ms(torch, st, lambda: h_out.copy_(d_out, non_blocking=True), reps)],
+           "ce_both_gbs_each_way": [gbs(x) for x in timed_ms(torch, st, both, reps)]}
+    sm = torch.cuda.get_device_properties(0).multi_processor_count
+    for blocks in (16, 32, sm, 4 * sm):
+        out[f"kernel_pull_{blocks}ctas_gbs"] = round(nbytes / phpc.link_probe(False, nbytes, blocks) / 1e6, 1)
+        out[f"kernel_push_{blocks}ctas_gbs"] = round(nbytes / phpc.link_probe(True, nbytes, blocks) / 1e6, 1)
     return out

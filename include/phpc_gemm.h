@@ -101,6 +101,19 @@ int phpc_panels_begin(phpc_panels **acc, int method, double *c, int ldc, int m, 
 int phpc_panels_add(phpc_panels *acc, const double *a, int lda, const double *b, int ldb, int k);
 int phpc_panels_end(phpc_panels *acc, float *seconds);
 
+/* Device time of the phases of this thread's last phpc_gemm_cuda or
+ * phpc_gemm_cublas call, in milliseconds (no reference counterpart: the
+ * reference reports one kernel time): ms[0] exponent scans and operand
+ * splits, ms[1] the GEMM (the tensor-core residue or digit GEMM; for
+ * phpc_gemm_cuda the plain FP64 GEMM), ms[2] the CRT reconstruction (modular
+ * scheme). Each is the sum of its kernels' event-timed spans; spans on
+ * concurrent streams may overlap. Zeros after a failed call. */
+int phpc_last_phase_times(float *ms);
+
+/* "dfma" or "dmma": the FP64 pipe phpc_gemm_cuda and phpc_dgemm_dmma_dev run
+ * on (PHPC_FP64_PIPE; no reference counterpart). */
+const char *phpc_fp64_pipe_name(void);
+
 /* ---------------------------------------------- device-pointer entry points */
 
 /* Plain FP64 GEMM (phpc_gemm_cuda's kernel; DFMA pipe, or DMMA with
@@ -244,6 +257,13 @@ int phpc_default_slices(int m, int k, int n);
  * the fewest moduli giving a grid of at least 51 bits). */
 int phpc_default_moduli(int m, int k, int n);
 
+/* The configuration the library uses for an m x k x n problem (tuning table,
+ * environment overrides, built-in defaults; no reference counterpart), in
+ * cfg[10]: FP64-accurate GEMM moduli (0 = digit scheme), slices, tile width,
+ * raster height, CTAs per cluster, ring stages (0 = deepest that fits); 3xBF16
+ * GEMM tile width, raster height, stages; plain FP64 GEMM ring stages. */
+int phpc_tuning(int m, int k, int n, int *cfg);
+
 /* ------------------------------------------------------------------ utils */
 
 /* Higher-precision reference for stating errors: R[r][j] = C0[i][j] +
@@ -268,6 +288,13 @@ int phpc_fill_wide_dev(double *dx, size_t n, uint64_t seed, uint64_t offset, int
  * 7 even warps DFMA for iters2 iterations and odd warps DMMA m16n8k4 for
  * iters. Synchronous; allocates a sink of blocks * threads doubles. */
 int phpc_pipe_probe(int kind, int blocks, int threads, int64_t iters, int64_t iters2, float *ms, double *flops);
+
+/* Host-link probe (no reference counterpart): one kernel of `blocks` CTAs
+ * copies `bytes` (a multiple of 16, >= 1 MiB) from page-locked host memory
+ * into device memory (to_host = 0) or back (to_host = 1) through the host
+ * buffer's device address; *ms = its device time. Synchronous; allocates the
+ * two buffers for the call. */
+int phpc_link_probe(int to_host, size_t bytes, int blocks, float *ms);
 
 /* Last kernel status of the calling thread's device (reads and clears the
  * device status word; synchronises the device). */

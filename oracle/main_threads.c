@@ -7,8 +7,11 @@
  * reduction over ranks, the CSV's process count), as the reference's
  * `mpirun -np P main.out N tw gw gh name` (src/main.c:17-123) would run it.
  *
- * The driver's two outside calls are stubbed: cudaGetDeviceCount reports one
- * device, phpc_error_string names the status.
+ * The driver's outside calls are stubbed: cudaGetDeviceCount reports one
+ * device, phpc_error_string names the status, phpc_fp64_pipe_name answers
+ * "dfma", phpc_default_moduli / _slices 13 / 7, and phpc_last_phase_times
+ * reports the harness's local GEMM as the whole GEMM phase (0.125 s per call
+ * or panel, no split or reconstruction).
  */
 #include <cuda_runtime_api.h>
 #include <stdio.h>
@@ -24,6 +27,24 @@ cudaError_t cudaGetDeviceCount(int *count) {
 }
 
 const char *phpc_error_string(int code) { return code == PHPC_OK ? "success" : "error"; }
+
+const char *phpc_fp64_pipe_name(void) { return "dfma"; }
+
+int phpc_default_moduli(int m, int k, int n) {
+  (void)m, (void)k, (void)n;
+  return 13;
+}
+
+int phpc_default_slices(int m, int k, int n) {
+  (void)m, (void)k, (void)n;
+  return 7;
+}
+
+int phpc_last_phase_times(float *ms) {
+  ms[0] = ms[2] = 0.f;
+  ms[1] = 125.f;
+  return PHPC_OK;
+}
 
 typedef struct {
   int argc;

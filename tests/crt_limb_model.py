@@ -13,8 +13,11 @@ The reconstruction, for residues r_i in [0, m_i) of the q moduli:
 2. S_j = sum_i t_i P_ij, P_ij the balanced 13-bit digits of P_i = M / m_i
    (|P_ij| <= 2^12): |S_j| <= 15 * 181 * 2^12 < 2^24, so every partial sum is
    an integer FP32 holds exactly.
-3. est = sum_i t_i fl(1 / m_i) in FP32, |est| <= 7.5; q = round(est). With the
-   fast path's guarantee |y| / M <= 1/2 - 1/32 the rounding is exact.
+3. est = S_(NP-1) c_(NP-1) + S_(NP-2) c_(NP-2) + S_(NP-3) c_(NP-3) in FP32,
+   c_j = fl(2^(13 j) / M): the top three limb sums give acc / M (|acc / M| =
+   |sum_i t_i / m_i| <= 7.5) to within 2^-19 (the lower limbs weigh below
+   2^-27); q = round(est). With the fast path's guarantee
+   |y| / M <= 1/2 - 1/32 the rounding is exact.
 4. Y_j = S_j - q M_j (M_j the balanced 13-bit digits of M): |Y_j| < 2^24.
 5. Carries: h_j = round(Y_j 2^-13), l_j = Y_j - h_j 2^13 (|l_j| <= 2^12),
    digits d_0 = l_0, d_j = l_j + h_(j-1): |d_j| < 2^22, converted to integers
@@ -53,6 +56,8 @@ class Table:
         self.NP = max(len_digits(P) for P in self.P)
         self.Pd = [balanced_digits(P, self.NP) for P in self.P]
         self.Md = balanced_digits(self.M, self.NP + 1)
+        # weights of the top three limb sums in the quotient estimate
+        self.c = {j: np.float32((2.0 ** (13 * j)) / self.M) for j in range(max(0, self.NP - 3), self.NP)}
 
 
 def len_digits(x: int) -> int:
@@ -81,20 +86,23 @@ def reconstruct(T: Table, r: list[int], checks: dict | None = None) -> int:
     """y (the symmetric representative of sum r_i W_i mod M) by the limb
     algorithm; records the largest magnitudes of its exact steps in checks."""
     S = [f32(0)] * T.NP
-    est = f32(0)
     tmax = 0
     for i, m in enumerate(T.m):
-        p = f32(r[i]) * f32(T.inv[i])
+        # r as the float 2^23 + r; p = (2^23 + r) inv - 2^23 inv = r inv, exact in one FMA
+        rb = f32(8388608 + r[i])
+        p = fma32(rb, f32(T.inv[i]), f32(-8388608.0 * T.inv[i]))
         assert float(p) == r[i] * T.inv[i]
         qq = fma32(p, f32(1.0 / m), MAGIC) - MAGIC
         t = fma32(qq, f32(-m), p)
         assert float(t) == r[i] * T.inv[i] - float(qq) * m
         tmax = max(tmax, abs(int(t)))
-        est = fma32(t, f32(1.0 / m), est)
         for j in range(T.NP):
             exact = int(S[j]) + int(t) * T.Pd[i][j]
             S[j] = fma32(t, f32(T.Pd[i][j]), S[j])
             assert int(S[j]) == exact and abs(exact) < 1 << 24
+    est = f32(0)
+    for j in sorted(T.c, reverse=True):
+        est = fma32(S[j], T.c[j], est)
     q = (est + MAGIC) - MAGIC
     Y = [fma32(q, f32(-T.Md[j]), S[j] if j < T.NP else f32(0)) for j in range(T.NP + 1)]
     Yexact = [(int(S[j]) if j < T.NP else 0) - int(q) * T.Md[j] for j in range(T.NP + 1)]

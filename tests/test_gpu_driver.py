@@ -65,12 +65,18 @@ def test_main_out_csv(tmp_path, built, dist):
     assert row[:6] == ["512", "1", "1", "4", "1024", "4096"]
     assert all(float(x) > 0 for x in row[6:])
     ext = (tmp_path / "csv" / "t0_N512_T1_G1_TW32_GW2_GH2_ext.csv").read_text().strip().splitlines()
-    assert ext[0].startswith("method,")
+    assert ext[0] == ("method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err,split_ms,gemm_ms,crt_ms,"
+                      "split_gbs,gemm_tflops,crt_gbs")
     recs = [line.split(",") for line in ext[1:]]
-    assert [r_[0] for r_ in recs] == ["dmma", "ozaki_split"]
+    assert [r_[0] for r_ in recs] == ["dfma", "ozaki_split"]  # the plain GEMM's pipe, then the split GEMM
     if dist == "index":
         for r_ in recs:  # exact integer products: both methods reproduce the closed form
             assert float(r_[5]) == 0.0 and float(r_[6]) == 0.0
+    plain, split = ([float(x) for x in r_[7:]] for r_ in recs)
+    # plain FP64: one GEMM phase, its FP64 rate; split: every phase timed, with its algorithmic rate
+    assert plain[0] == 0.0 and plain[1] > 0 and plain[2] == 0.0 and plain[4] > 0
+    assert all(x > 0 for x in split), split
+    assert split[1] <= float(recs[1][3]) * 1e3 * 1.5  # GEMM phase within the call's device time
 
 
 @pytest.mark.parametrize("moduli", ["15", "0"])

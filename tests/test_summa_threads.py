@@ -197,8 +197,9 @@ def test_main_out_multi_rank(built, tmp_path, procs, grid):
     steps = H.steps(*grid)
     assert float(row[7]) == pytest.approx(steps * H.STEP_SECONDS)
     ext = (tmp_path / "csv" / f"{stem}_ext.csv").read_text().strip().splitlines()
-    assert ext[0] == "method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err"
-    for line, method in zip(ext[1:], ("dmma", "ozaki_split")):
+    assert ext[0] == ("method,matrix_size,wall_s,device_s,tflops,max_rel_err,frob_rel_err,split_ms,gemm_ms,crt_ms,"
+                      "split_gbs,gemm_tflops,crt_gbs")
+    for line, method in zip(ext[1:], ("dfma", "ozaki_split")):
         f = line.split(",")
         assert f[0] == method and int(f[1]) == n
         assert float(f[3]) == pytest.approx(steps * H.STEP_SECONDS)
