@@ -10,7 +10,7 @@ namespace phpc {
 constexpr int kCrtMaxModuli = 15;  // M < 2^127: weights in four 32-bit limbs, sums in five
 constexpr int kCrtMaxLimbs = 10;   // balanced 13-bit digits of M / m_i (15 moduli: 10)
 
-// Constants of the reconstruction on FP32 limbs (crt_limbs_pair), each value
+// Constants of the reconstruction on FP32 limbs (crt_limbs_quad), each value
 // in both lanes of a packed f32x2 operation.
 struct CrtLimbs {
   int np;                                 // digits of the largest M / m_i (5 .. 10)
@@ -254,13 +254,15 @@ __device__ __forceinline__ double crt_add_i128(double c, uint64_t lo, uint64_t h
   return c + ldexp(sign ? -m : m, e - 52 + x);
 }
 
-// The one-step CRT of two adjacent elements on FP32 limbs, the two elements
-// in the two lanes of packed f32x2 operations. w[i] holds their residues mod
-// m_i (element 0 in the low 16 bits, element 1 in the high 16 bits). Valid
-// when every result satisfies |y| / M <= 1/2 - 1/32 (CrtTable::fast); gives
-// the y of crt_value as a 128-bit two's complement integer (y0, y1). Every
-// step except the quotient estimate is exact in FP32 (all values are
-// integers below 2^24):
+// The one-step CRT of four adjacent elements on FP32 limbs: two pairs, each
+// pair in the two lanes of packed f32x2 operations, both pairs computed in
+// one pass over the moduli so that each modulus's constants are read once
+// for the four elements. w[p][i] holds the residues mod m_i of pair p
+// (its first element in the low 16 bits, the second in the high 16 bits).
+// Valid when every result satisfies |y| / M <= 1/2 - 1/32 (CrtTable::fast);
+// gives the y of crt_value as 128-bit two's complement integers
+// (lo[e], hi[e]), e = 2 p + lane. Every step except the quotient estimate is
+// exact in FP32 (all values are integers below 2^24):
 //  1. t_i = r_i inv_i mod m_i, symmetric: with r_i read as the float
 //     2^23 + r_i, p = (2^23 + r_i) inv_i - 2^23 inv_i = r_i inv_i < 2^17 in one
 //     FMA, t_i = p - round(p / m_i) m_i (|t_i| <= m_i / 2), and
@@ -277,61 +279,76 @@ __device__ __forceinline__ double crt_add_i128(double c, uint64_t lo, uint64_t h
 //     y = A + B 2^52 + C 2^104 for the chunks A, B, C.
 // NP = T.L.np, the number of digits of the largest M / m_i.
 template <int NP>
-__device__ __forceinline__ void crt_limbs_pair(const uint32_t (&w)[kCrtMaxModuli], const CrtTable& T,
-                                               uint64_t (&lo)[2], uint64_t (&hi)[2]) {
+__device__ __forceinline__ void crt_limbs_quad(const uint32_t (&w)[2][kCrtMaxModuli], const CrtTable& T,
+                                               uint64_t (&lo)[4], uint64_t (&hi)[4]) {
   const float2 kRound = make_float2(12582912.0f, 12582912.0f), kUnround = make_float2(-12582912.0f, -12582912.0f);
   const float2 kDigit = make_float2(0x1p-13f, 0x1p-13f), kNegBase = make_float2(-8192.0f, -8192.0f);
-  float2 S[NP];
+  float2 S[2][NP];
 #pragma unroll
-  for (int j = 0; j < NP; ++j) S[j] = make_float2(0.0f, 0.0f);
+  for (int p = 0; p < 2; ++p)
+#pragma unroll
+    for (int j = 0; j < NP; ++j) S[p][j] = make_float2(0.0f, 0.0f);
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i) {
     if (i < T.n) {
-      const float2 rb = make_float2(__uint_as_float(0x4B000000u | (w[i] & 0xFFFFu)),
-                                    __uint_as_float(0x4B000000u | (w[i] >> 16)));
-      const float2 p = __ffma2_rn(rb, T.L.inv[i], T.L.ninvb[i]);
-      const float2 qq = __fadd2_rn(__ffma2_rn(p, T.L.rm[i], kRound), kUnround);
-      const float2 t = __ffma2_rn(qq, T.L.negm[i], p);
+      const float2 inv = T.L.inv[i], ninvb = T.L.ninvb[i], rm = T.L.rm[i], negm = T.L.negm[i];
+      float2 t[2];
 #pragma unroll
-      for (int j = 0; j < NP; ++j) S[j] = __ffma2_rn(t, T.L.P[i][j], S[j]);
+      for (int p = 0; p < 2; ++p) {
+        const float2 rb = make_float2(__uint_as_float(0x4B000000u | (w[p][i] & 0xFFFFu)),
+                                      __uint_as_float(0x4B000000u | (w[p][i] >> 16)));
+        const float2 pr = __ffma2_rn(rb, inv, ninvb);
+        const float2 qq = __fadd2_rn(__ffma2_rn(pr, rm, kRound), kUnround);
+        t[p] = __ffma2_rn(qq, negm, pr);
+      }
+#pragma unroll
+      for (int j = 0; j < NP; ++j) {
+        const float2 pij = T.L.P[i][j];
+        S[0][j] = __ffma2_rn(t[0], pij, S[0][j]);
+        S[1][j] = __ffma2_rn(t[1], pij, S[1][j]);
+      }
     }
   }
-  float2 est = __fmul2_rn(S[NP - 1], T.L.cw[0]);
-  est = __ffma2_rn(S[NP - 2], T.L.cw[1], est);
-  est = __ffma2_rn(S[NP - 3], T.L.cw[2], est);
-  const float2 q = __fadd2_rn(__fadd2_rn(est, kRound), kUnround);
-  int d0[12], d1[12];  // digits; those above NP + 1 are zero
 #pragma unroll
-  for (int j = 0; j < 12; ++j) d0[j] = d1[j] = 0;
-  float2 hprev = make_float2(0.0f, 0.0f);
+  for (int p = 0; p < 2; ++p) {
+    float2 est = __fmul2_rn(S[p][NP - 1], T.L.cw[0]);
+    est = __ffma2_rn(S[p][NP - 2], T.L.cw[1], est);
+    est = __ffma2_rn(S[p][NP - 3], T.L.cw[2], est);
+    const float2 q = __fadd2_rn(__fadd2_rn(est, kRound), kUnround);
+    int d0[12], d1[12];  // digits; those above NP + 1 are zero
 #pragma unroll
-  for (int j = 0; j <= NP; ++j) {
-    const float2 y = j < NP ? __ffma2_rn(q, T.L.negM[j], S[j]) : __fmul2_rn(q, T.L.negM[NP]);
-    const float2 h = __fadd2_rn(__ffma2_rn(y, kDigit, kRound), kUnround);
-    const float2 d = __fadd2_rn(__fadd2_rn(__ffma2_rn(h, kNegBase, y), hprev), kRound);
-    d0[j] = __float_as_int(d.x) - 0x4B400000;
-    d1[j] = __float_as_int(d.y) - 0x4B400000;
-    hprev = h;
-  }
-  {
-    const float2 d = __fadd2_rn(hprev, kRound);
-    d0[NP + 1] = __float_as_int(d.x) - 0x4B400000;
-    d1[NP + 1] = __float_as_int(d.y) - 0x4B400000;
-  }
-  // 52-bit chunks of four digits: |chunk| < 2^52 (int64 exact)
-  auto chunk = [](const int (&d)[12], int j0) -> int64_t {
-    const int32_t a = d[j0] + d[j0 + 1] * 8192, b = d[j0 + 2] + d[j0 + 3] * 8192;
-    return static_cast<int64_t>(a) + static_cast<int64_t>(b) * 67108864;
-  };
+    for (int j = 0; j < 12; ++j) d0[j] = d1[j] = 0;
+    float2 hprev = make_float2(0.0f, 0.0f);
 #pragma unroll
-  for (int e = 0; e < 2; ++e) {
-    const int(&d)[12] = e ? d1 : d0;
-    const int64_t A = chunk(d, 0), B = chunk(d, 4), C = chunk(d, 8);
-    // y = A + B 2^52 + C 2^104 modulo 2^128
-    const uint64_t b_lo = static_cast<uint64_t>(B) << 52;
-    lo[e] = static_cast<uint64_t>(A) + b_lo;
-    hi[e] = static_cast<uint64_t>(A >> 63) + static_cast<uint64_t>(B >> 12) + (static_cast<uint64_t>(C) << 40) +
-            (lo[e] < b_lo ? 1 : 0);
+    for (int j = 0; j <= NP; ++j) {
+      const float2 y = j < NP ? __ffma2_rn(q, T.L.negM[j], S[p][j]) : __fmul2_rn(q, T.L.negM[NP]);
+      const float2 h = __fadd2_rn(__ffma2_rn(y, kDigit, kRound), kUnround);
+      const float2 d = __fadd2_rn(__fadd2_rn(__ffma2_rn(h, kNegBase, y), hprev), kRound);
+      d0[j] = __float_as_int(d.x) - 0x4B400000;
+      d1[j] = __float_as_int(d.y) - 0x4B400000;
+      hprev = h;
+    }
+    {
+      const float2 d = __fadd2_rn(hprev, kRound);
+      d0[NP + 1] = __float_as_int(d.x) - 0x4B400000;
+      d1[NP + 1] = __float_as_int(d.y) - 0x4B400000;
+    }
+    // 52-bit chunks of four digits: |chunk| < 2^52 (int64 exact)
+    auto chunk = [](const int (&d)[12], int j0) -> int64_t {
+      const int32_t a = d[j0] + d[j0 + 1] * 8192, b = d[j0 + 2] + d[j0 + 3] * 8192;
+      return static_cast<int64_t>(a) + static_cast<int64_t>(b) * 67108864;
+    };
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const int(&d)[12] = l ? d1 : d0;
+      const int64_t A = chunk(d, 0), B = chunk(d, 4), C = chunk(d, 8);
+      // y = A + B 2^52 + C 2^104 modulo 2^128
+      const uint64_t b_lo = static_cast<uint64_t>(B) << 52;
+      const int e = 2 * p + l;
+      lo[e] = static_cast<uint64_t>(A) + b_lo;
+      hi[e] = static_cast<uint64_t>(A >> 63) + static_cast<uint64_t>(B >> 12) + (static_cast<uint64_t>(C) << 40) +
+              (lo[e] < b_lo ? 1 : 0);
+    }
   }
 }
 

@@ -373,8 +373,8 @@ inline void with_crt_digits(int np, F&& f) {
 // row's exponent less its grid width). Columns at or beyond ncols are left
 // alone.
 // NP = T.L.np (the kernels are instantiated per digit count); with fast set
-// the four elements are reconstructed on FP32 limbs, two at a time
-// (crt_limbs_pair), else by the 32-bit-limb integer path (crt_value).
+// the four elements are reconstructed on FP32 limbs (crt_limbs_quad), else by
+// the 32-bit-limb integer path (crt_value).
 template <int NP>
 __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_t rplane, const CrtTable& T, int fast,
                                          int ncols, int row_shift, const int* __restrict__ ebp,
@@ -384,17 +384,14 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
   for (int i = 0; i < kCrtMaxModuli; ++i)
     rw[i] = i < T.n ? *reinterpret_cast<const uint2*>(rp + i * rplane) : make_uint2(0u, 0u);
   if (fast) {
-    uint32_t w01[kCrtMaxModuli], w23[kCrtMaxModuli];
+    uint32_t w[2][kCrtMaxModuli];
 #pragma unroll
     for (int i = 0; i < kCrtMaxModuli; ++i) {
-      w01[i] = rw[i].x;
-      w23[i] = rw[i].y;
+      w[0][i] = rw[i].x;
+      w[1][i] = rw[i].y;
     }
-    uint64_t lo01[2], hi01[2], lo23[2], hi23[2];
-    crt_limbs_pair<NP>(w01, T, lo01, hi01);
-    crt_limbs_pair<NP>(w23, T, lo23, hi23);
-    const uint64_t lo[kCrtCols] = {lo01[0], lo01[1], lo23[0], lo23[1]};
-    const uint64_t hi[kCrtCols] = {hi01[0], hi01[1], hi23[0], hi23[1]};
+    uint64_t lo[kCrtCols], hi[kCrtCols];
+    crt_limbs_quad<NP>(w, T, lo, hi);
     if (ncols == kCrtCols) {
       double cv[kCrtCols];
 #pragma unroll

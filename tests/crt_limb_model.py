@@ -1,4 +1,4 @@
-"""Model of the CRT reconstruction on FP32 limbs (the kernel crt_limbs_pair in
+"""Model of the CRT reconstruction on FP32 limbs (the kernel crt_limbs_quad in
 csrc/crt.cuh), used by the CPU tests to check its arithmetic on many residue
 vectors: every step that the kernel does exactly must stay within the range
 in which FP32 represents integers exactly, and the result must be the

@@ -1,4 +1,4 @@
-"""The CRT on FP32 limbs (csrc/crt.cuh, crt_limbs_pair) checked on the CPU
+"""The CRT on FP32 limbs (csrc/crt.cuh, crt_limbs_quad) checked on the CPU
 through its model (tests/crt_limb_model.py): for every modulus count the
 library supports, on seeded and extreme values, every step the kernel does
 exactly stays exact, and the result is the integer the residues stand for.
