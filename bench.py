@@ -101,8 +101,8 @@ def parse_args():
                    help="also run the rectangular FP32 and the batched workloads after the timed region (1/0)")
     p.add_argument("--peaks", action="store_true", help="throughput probes of the arithmetic pipes, then exit")
     p.add_argument("--link", action="store_true", help="host-link probes (copy engines and kernels), then exit")
-    p.add_argument("--case", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma"], default=None,
-                   help="time one method at one size (--m/--k/--n, --reps) and exit")
+    p.add_argument("--case", choices=["ozaki", "ozaki2", "dmma", "bf16x3", "ffma", "batched"], default=None,
+                   help="time one method at one size (--m/--k/--n, --reps), or the batched workload, and exit")
     p.add_argument("--m", type=int, default=0)
     p.add_argument("--k", type=int, default=0)
     p.add_argument("--reps", type=int, default=2)
@@ -611,6 +611,12 @@ def run_case(args) -> None:
     import phpc
     import workloads
 
+    if args.case == "batched":
+        r = workloads.batched(torch, phpc, moduli=args.moduli if args.moduli > 0 else 13, reps=args.reps)
+        print(json.dumps(r), flush=True)
+        if r["status"] != 0:
+            raise SystemExit(1)
+        return
     n = args.n
     gw, gh = (int(x) for x in args.grid.lower().split("x"))
     r = workloads.single_case(torch, phpc, args.case, args.m or n, args.k or n, n, reps=args.reps,
