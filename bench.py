@@ -76,9 +76,7 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
 # dominant kernel, from a one-pass ncu capture of this workload on a GB300;
 # keyed by (N, "slices" | "moduli", count).
-NCU_TRAFFIC_BYTES = {(16384, "slices", 7): 426.25e9 + 15.28e9,
-                     (16384, "moduli", 14): 153.23e9 + 7.52e9,
-                     (16384, "moduli", 13): 112.23e9 + 7.31e9}
+NCU_TRAFFIC_BYTES = {(16384, "moduli", 13): 112.12e9 + 7.31e9}
 UNIT = "TFLOP/s"
 
 
