@@ -319,7 +319,6 @@ PairList residue_pairs(const ModTable& T) {
   for (int i = 0; i < T.n; ++i) {
     pl.a[i] = pl.b[i] = pl.g[i] = static_cast<uint8_t>(i);
     pl.mod[i] = static_cast<uint16_t>(T.m[i]);
-    pl.magic[i] = T.magic[i];
     pl.invm[i] = T.invm[i].x;
   }
   return pl;

@@ -134,16 +134,19 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
   a.R = R;
   a.ldr = ldr;
   a.rplane = rplane;
-  if (MODE == kResidue && cluster == 1) {
+  if (MODE == kResidue) {
     // split the moduli into separate work units, moduli outer, when the
     // tiles fill at least one wave of SMs: consecutive waves then work on the
     // same modulus and share its planes in L2, and a ragged last wave is
-    // spread over 13x more units (N = 4096: 14 % faster, DRAM traffic 2.1x ->
-    // 1.06x the algorithmic bytes; N = 8192: 3 %; N = 16384: 1-2 %, DRAM reads
-    // 145 -> 112 GB). Below one wave of tiles it measured 2-7 % slower.
+    // spread over 13x more units (single CTAs, N = 4096: 14 % faster, DRAM
+    // traffic 2.1x -> 1.06x the algorithmic bytes; N = 8192: 3 %; N = 16384:
+    // 1-2 %, DRAM reads 145 -> 112 GB). Below one wave of tiles it measured
+    // 2-7 % slower. A CTA pair's tile is 256 rows high and a wave has half as
+    // many of them.
     int split = opt.split_pairs;
     if (const char* env = getenv("PHPC_SPLIT_MODULI")) split = atoi(env) != 0 ? 1 : 0;
-    if (split < 0) split = (int64_t)a.tm * a.tn >= dev->sm_count ? 1 : 0;
+    const int64_t tiles = cluster == 1 ? (int64_t)a.tm * a.tn : (int64_t)((a.tm + 1) / 2) * a.tn;
+    if (split < 0) split = tiles * cluster >= dev->sm_count ? 1 : 0;
     a.split_pairs = split;
   }
   if (cluster == 1) {

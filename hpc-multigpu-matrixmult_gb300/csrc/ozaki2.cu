@@ -267,7 +267,6 @@ int ozaki2_multiply_block(int m, int r0, int rows, int c0, int cols, int k, int 
     pl.b[i] = static_cast<uint8_t>(i);
     pl.g[i] = static_cast<uint8_t>(i);
     pl.mod[i] = static_cast<uint16_t>(T.m[i]);
-    pl.magic[i] = T.magic[i];
     pl.invm[i] = T.invm[i].x;
   }
   const int64_t rplane = (int64_t)m * L.ldr;

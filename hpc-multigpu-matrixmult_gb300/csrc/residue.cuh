@@ -31,7 +31,6 @@ struct ModTable {
   int bits;    // worst-case grid width for this K (2 K 2^(2b) < M); the kernels use per-row/column widths
   float logT;  // log2 of the norm bound T (T^2 = M (1/2 - 1/32)), less a 2^-8 safety margin
   uint32_t m[kMaxModuli];
-  uint32_t magic[kMaxModuli];  // floor(2^32 / m)
   // Per modulus, each value twice (both lanes of a packed f32x2 FMA):
   float2 cf[kMaxModuli][4];  // symmetric residues of 2^13, 2^26, 2^39, 2^52 mod m (|c| <= 181)
   float2 invm[kMaxModuli];   // 1 / m rounded to float
@@ -75,7 +74,6 @@ inline ModTable make_table(int nmod, int k) {
   for (int i = 0; i < nmod; ++i) {
     const uint32_t m = kModuli[i];
     T.m[i] = m;
-    T.magic[i] = static_cast<uint32_t>((1ull << 32) / m);
     for (int j = 0; j < 4; ++j) {
       const int64_t c = static_cast<int64_t>((1ull << (13 * (j + 1))) % m);
       const float cs = static_cast<float>(2 * c > static_cast<int64_t>(m) ? c - m : c);

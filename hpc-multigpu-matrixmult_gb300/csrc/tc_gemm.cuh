@@ -53,7 +53,7 @@ constexpr int kTcMaxPairs = 64;
 constexpr int kTcChunkSteps = 16;      // kOzaki: 16 x 64 = 1024 products (|d| <= 128) per exact f32 chunk
 constexpr int kTcResidueChunkSteps = 8;  // kResidue: 8 x 64 = 512 products (|r| <= 181) per exact f32 chunk
 constexpr int kTcF32ChunkSteps = 8;    // kF32: flush to round-to-nearest registers every 512 products
-constexpr int kTcFoldChunks = 127;     // 127 chunks of |v| <= 2^24 keep |int32 sum| < 2^31
+constexpr int kTcFoldChunks = 127;     // kOzaki: 127 chunks of |v| <= 2^24 keep |int32 sum| < 2^31
 constexpr int kTcEpiWarps = 8;
 constexpr int kTcFirstEpiWarp = 4;
 constexpr int kTcThreads = (kTcFirstEpiWarp + kTcEpiWarps) * 32;
@@ -68,38 +68,28 @@ struct PairList {
   uint8_t b[kTcMaxPairs];     // B plane index (0-based)
   uint8_t g[kTcMaxPairs];     // group id (Ozaki: diagonal p + q, 1-based digits); pairs of a group are contiguous
   uint16_t mod[kTcMaxPairs];  // kResidue: modulus of the group
-  uint32_t magic[kTcMaxPairs];  // kResidue: floor(2^32 / modulus)
   float invm[kTcMaxPairs];      // kResidue: 1 / modulus rounded to float
 };
 
-// x mod m for 0 <= x < 2^32, 2 <= m < 2^16, magic = floor(2^32 / m) (Barrett: the
-// quotient estimate is low by at most one).
-__device__ __forceinline__ uint32_t mod_small(uint32_t x, uint32_t m, uint32_t magic) {
-  const uint32_t q = __umulhi(x, magic);
-  uint32_t r = x - q * m;
-  if (r >= m) r -= m;
-  return r;
-}
-// Residues in [0, m) of two integer-valued floats |x| < 2^24 (one exact f32
-// chunk), m <= 363: x - m round(x / m) by the 1.5 * 2^23 rounding constant
-// and one exact FMA (|.| <= 0.51 m), moved into [0, m), packed as two 16-bit
-// values read from the mantissas of r + 2^23 (lo in the low half).
-__device__ __forceinline__ uint32_t residue_pair_u16(float x0, float x1, float m, float invm) {
-  const float2 x = make_float2(x0, x1);
+// x - m round(x / m) for two integer-valued floats |x| < 2^24, m <= 363: the
+// quotient through the 1.5 * 2^23 rounding constant is within 0.51 of x / m
+// (fl(1 / m) is off by at most 2^-24 relative), and the remainder, an integer
+// with |.| <= 0.51 m, comes out of one FMA exactly.
+__device__ __forceinline__ float2 reduce_pair_f32(float2 x, float m, float invm) {
   const float2 q = __fadd2_rn(__ffma2_rn(x, make_float2(invm, invm), make_float2(12582912.0f, 12582912.0f)),
                               make_float2(-12582912.0f, -12582912.0f));
-  float2 r = __ffma2_rn(q, make_float2(-m, -m), x);
+  return __ffma2_rn(q, make_float2(-m, -m), x);
+}
+
+// Residues in [0, m) of two integer-valued floats |x| < 2^24: the symmetric
+// remainders moved into [0, m), packed as two 16-bit values read from the
+// mantissas of r + 2^23 (lo in the low half).
+__device__ __forceinline__ uint32_t residue_pair_u16(float x0, float x1, float m, float invm) {
+  float2 r = reduce_pair_f32(make_float2(x0, x1), m, invm);
   r.x = r.x < 0.0f ? r.x + m : r.x;
   r.y = r.y < 0.0f ? r.y + m : r.y;
   const float2 b = __fadd2_rn(r, make_float2(8388608.0f, 8388608.0f));
   return __byte_perm(__float_as_uint(b.x), __float_as_uint(b.y), 0x5410);
-}
-
-// Residue in [0, m) of a signed 32-bit integer.
-__device__ __forceinline__ uint32_t mod_signed(int32_t x, uint32_t m, uint32_t magic) {
-  const uint32_t mag = x < 0 ? 0u - static_cast<uint32_t>(x) : static_cast<uint32_t>(x);
-  const uint32_t r = mod_small(mag, m, magic);
-  return (x < 0 && r) ? m - r : r;
 }
 
 struct TcArgs {
@@ -114,7 +104,7 @@ struct TcArgs {
   uint16_t* R;                // kResidue: residue planes [pairs][M][ldr] (one 16-bit residue per element)
   int64_t ldr;                // kResidue: row stride of a residue plane in elements (multiple of 16)
   int64_t rplane;             // kResidue: plane stride in elements
-  int split_pairs;            // kResidue, one CTA per tile: a work unit is one (tile, modulus), moduli outer
+  int split_pairs;            // kResidue: a work unit is one (tile, modulus), moduli outer
   int stages;                 // K-stages of the ring in use, 2 .. TcCfg::kStages (other values: kStages)
 };
 
@@ -316,9 +306,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (!pair_ok && threadIdx.x == 0) record_error(status, PHPC_ERR_UNSUPPORTED | (15 << 8));
   }
   // kResidue: the moduli are independent, so with split_pairs a work unit is
-  // one (tile, modulus): pairs.n times as many units, for problems with too
-  // few tiles to fill the SMs evenly
-  const bool split = MODE == kResidue && CLUSTER == 1 && args.split_pairs != 0;
+  // one (tile, modulus), moduli outer: pairs.n times as many units, and the
+  // CTAs (or CTA pairs) of a wave share one modulus's planes in L2
+  const bool split = MODE == kResidue && args.split_pairs != 0;
   const int nunits = pair_ok ? ntiles * (split ? pairs.n : 1) : 0;
   // Each role's code is dominated by its own setmaxnreg, so the compiler can
   // allocate up to kTcRegsHigh registers in the epilogue branch.
@@ -497,6 +487,27 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
               for (int j = 0; j < 32; ++j) acc[cb + j] = static_cast<int32_t>(r[j]);
             }
+          } else if (MODE == kResidue) {
+            // Several chunks: each chunk (an exact f32 integer below 2^24) is
+            // reduced mod m in FP32 and added to the running sum in FP32, two
+            // elements per instruction; the sum stays an exact integer (at
+            // most 0.51 m per chunk, folded every kTcFoldChunks chunks). This
+            // keeps the drain off the float-to-integer conversion unit.
+            const float mf = static_cast<float>(pairs.mod[gstart]), invm = pairs.invm[gstart];
+#pragma unroll
+            for (int cb = 0; cb < HALF; cb += 32) {
+              uint32_t r[32];
+              tmem_ld_32x32b_x32(taddr + cb, r);
+              tc_wait_ld();
+#pragma unroll
+              for (int j = 0; j < 32; j += 2) {
+                const float2 red =
+                    reduce_pair_f32(make_float2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])), mf, invm);
+                const float2 sum = __fadd2_rn(make_float2(__int_as_float(acc[cb + j]), __int_as_float(acc[cb + j + 1])), red);
+                acc[cb + j] = __float_as_int(sum.x);
+                acc[cb + j + 1] = __float_as_int(sum.y);
+              }
+            }
           } else if (MODE != kF32) {
 #pragma unroll
             for (int cb = 0; cb < HALF; cb += 32) {
@@ -532,31 +543,30 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           const bool fold = MODE != kF32 ? (group_end || ((c + 1) % kTcFoldChunks) == 0) : group_end;
           if (!fold) continue;
           if (MODE == kResidue) {
-            const uint32_t m = pairs.mod[gstart], magic = pairs.magic[gstart];
+            const float mf = static_cast<float>(pairs.mod[gstart]), invm = pairs.invm[gstart];
             if (!group_end) {  // keep the partial residue; more chunks of this modulus follow
 #pragma unroll
-              for (int u = 0; u < HALF; ++u) acc[u] = static_cast<int32_t>(mod_signed(acc[u], m, magic));
+              for (int u = 0; u < HALF; u += 2) {
+                const float2 red =
+                    reduce_pair_f32(make_float2(__int_as_float(acc[u]), __int_as_float(acc[u + 1])), mf, invm);
+                acc[u] = __float_as_int(red.x);
+                acc[u + 1] = __float_as_int(red.y);
+              }
               continue;
             }
             // One 16-bit residue per element, 64 columns at a time: each lane
             // reduces its row's 64 residues into the warp's scratch (32 words
             // per row), then the warp stores 4 rows x 128 bytes per
             // instruction (lane: row 4 i + lane / 8, 16-byte segment lane % 8).
+            // (acc holds exact f32 integers: the chunk itself, or the sum of
+            // the reduced chunks)
             uint16_t* rplane = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane;
-            const float mf = static_cast<float>(m), invm = pairs.invm[gstart];
 #pragma unroll
             for (int h = 0; h < HALF; h += 64) {
-              if (single) {
 #pragma unroll
-                for (int q = 0; q < 32; ++q)
-                  tr[lane * 33 + q] =
-                      residue_pair_u16(__int_as_float(acc[h + 2 * q]), __int_as_float(acc[h + 2 * q + 1]), mf, invm);
-              } else {
-#pragma unroll
-                for (int q = 0; q < 32; ++q)
-                  tr[lane * 33 + q] =
-                      mod_signed(acc[h + 2 * q], m, magic) | (mod_signed(acc[h + 2 * q + 1], m, magic) << 16);
-              }
+              for (int q = 0; q < 32; ++q)
+                tr[lane * 33 + q] =
+                    residue_pair_u16(__int_as_float(acc[h + 2 * q]), __int_as_float(acc[h + 2 * q + 1]), mf, invm);
               __syncwarp();
               const int seg = lane & 7;
               const int col = col0 + h + seg * 8;

@@ -113,15 +113,47 @@ def test_grids_bound_and_rule(phpc, torch_cuda, kind):
     np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 14, grid))
 
 
-@pytest.mark.parametrize("cluster,bn", [("1", "128"), ("2", "256")])
-def test_bitexact_tile_variants(phpc, torch_cuda, monkeypatch, cluster, bn):
+@pytest.mark.parametrize("cluster,bn,split", [("1", "128", "0"), ("2", "256", "0"), ("2", "256", "1"),
+                                               ("2", "128", "1")])
+def test_bitexact_tile_variants(phpc, torch_cuda, monkeypatch, cluster, bn, split):
+    """Single CTAs and CTA pairs (256-row tiles, M = 256 MMAs), with the
+    moduli in one work unit per tile or as (tile, modulus) units: the bits of
+    the model. 300 rows make the last pair tile half empty."""
     monkeypatch.setenv("PHPC_CLUSTER", cluster)
     monkeypatch.setenv("PHPC_OZAKI_BN", bn)
+    monkeypatch.setenv("PHPC_SPLIT_MODULI", split)
     rng = np.random.default_rng(77)
     a = rng.uniform(-1, 1, (300, 400))
     b = rng.uniform(-1, 1, (400, 520))
     got, grid = run_dev_grid(phpc, torch_cuda, a, b, np.zeros((300, 520)), 15)
     np.testing.assert_array_equal(got, ozaki2_model.gemm(a, b, None, 15, grid))
+
+
+@pytest.mark.parametrize("bn", ["128", "256"])
+def test_pairs_split_many_waves_bitexact(phpc, torch_cuda, monkeypatch, bn):
+    """CTA pairs with (tile, modulus) units over several waves of units and
+    K above one exact chunk (partial residues folded between chunks), odd
+    tile rows: the bits of single CTAs on the same inputs."""
+    torch = torch_cuda
+    m, k, n = 1400, 1700, 2100
+    A = torch.empty((m, k), dtype=torch.float64, device="cuda")
+    B = torch.empty((k, n), dtype=torch.float64, device="cuda")
+    phpc.fill_wide_dev(A, m * k, 71, 0, -20, 20)
+    phpc.fill_wide_dev(B, k * n, 72, 0, -20, 20)
+    ws = phpc.ozaki2_workspace_bytes(m, k, n, 13)
+    W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+    monkeypatch.setenv("PHPC_OZAKI_BN", bn)
+    outs = []
+    for cluster, split in (("1", "1"), ("2", "1"), ("2", "0")):
+        monkeypatch.setenv("PHPC_CLUSTER", cluster)
+        monkeypatch.setenv("PHPC_SPLIT_MODULI", split)
+        C = torch.zeros((m, n), dtype=torch.float64, device="cuda")
+        phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, 13, W, ws)
+        torch.cuda.synchronize()
+        assert phpc.device_status() == 0
+        outs.append(C)
+    assert torch.equal(outs[1], outs[0])
+    assert torch.equal(outs[2], outs[0])
 
 
 @pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] == "index"], ids=lambda c: c["name"])
