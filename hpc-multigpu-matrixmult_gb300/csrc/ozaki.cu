@@ -148,6 +148,9 @@ int launch_tc_slice_gemm(const void* planesA, const void* planesB, int nplanesA,
     const int64_t tiles = cluster == 1 ? (int64_t)a.tm * a.tn : (int64_t)((a.tm + 1) / 2) * a.tn;
     if (split < 0) split = tiles * cluster >= dev->sm_count ? 1 : 0;
     a.split_pairs = split;
+    // odd rounds of units walk K backwards (PHPC_K_SERPENTINE = 0 turns it off)
+    const char* serp = getenv("PHPC_K_SERPENTINE");
+    a.k_serpentine = serp ? (atoi(serp) != 0 ? 1 : 0) : 1;
   }
   if (cluster == 1) {
     auto kern = tc_slice_gemm_kernel<BN, MODE>;

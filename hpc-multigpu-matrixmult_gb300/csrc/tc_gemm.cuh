@@ -106,6 +106,7 @@ struct TcArgs {
   int64_t rplane;             // kResidue: plane stride in elements
   int split_pairs;            // kResidue: a work unit is one (tile, modulus), moduli outer
   int stages;                 // K-stages of the ring in use, 2 .. TcCfg::kStages (other values: kStages)
+  int k_serpentine;           // kResidue: every other round of units walks K from the end (see the producer)
 };
 
 // Grouped mode: many independent problems in one persistent launch. The
@@ -325,27 +326,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t phase = 0;
       int issued = 0;
       bool ok = true;
-      for (int u = unit0; u < nunits && ok; u += ustride) {
+      // kResidue: the units of one round run at about the same time on all
+      // SMs and stream their planes through K together; with k_serpentine
+      // odd rounds walk K from the end, so a round starts on the K-steps the
+      // previous round loaded last (still in L2 for the panels both rounds
+      // share) instead of the ones it loaded first. The residue sums are
+      // exact integers, so the order of the K-steps does not change a bit.
+      const bool serp = MODE == kResidue && !GROUPED && args.k_serpentine != 0;
+      int round = 0;
+      for (int u = unit0; u < nunits && ok; u += ustride, ++round) {
         const int t = split ? u % ntiles : u;
         const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
         TcJob job;
         tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
+        const bool rev = serp && (round & 1);
         for (int pi = p0; pi < p1 && ok; ++pi) {
           const int pa = pairs.a[pi], pb = pairs.b[pi];
           for (int kb = 0; kb < job.nk; ++kb) {
             if (!wait_parity(&empty[stage], phase ^ 1, status, 11)) { ok = false; break; }
             uint8_t* sa = smem + stage * Cfg::kStageBytes;
+            const int kx = (rev ? job.nk - 1 - kb : kb) * kTcBK;
             if (CLUSTER == 1) {
               mbar_arrive_expect_tx(&full[stage], Cfg::kStageBytes);
-              tma_load_3d(sa, job.tmA, kb * kTcBK, job.rm * kTcBM, pa, &full[stage]);
-              tma_load_3d(sa + Cfg::kStageA, job.tmB, kb * kTcBK, job.rn * BN, pb, &full[stage]);
+              tma_load_3d(sa, job.tmA, kx, job.rm * kTcBM, pa, &full[stage]);
+              tma_load_3d(sa + Cfg::kStageA, job.tmB, kx, job.rn * BN, pb, &full[stage]);
             } else {
               // This CTA's 128 rows of A and half of B, into its own shared
               // memory, counted on the leader's full barrier.
               const uint32_t bar = mapa_shared(smem_u32(&full[stage]), 0);
               if (leader) mbar_arrive_expect_tx(&full[stage], 2 * Cfg::kStageBytes);
-              tma_load_3d_pair(sa, job.tmA, kb * kTcBK, job.rm * kTcBM, pa, bar);
-              tma_load_3d_pair(sa + Cfg::kStageA, job.tmB, kb * kTcBK,
+              tma_load_3d_pair(sa, job.tmA, kx, job.rm * kTcBM, pa, bar);
+              tma_load_3d_pair(sa + Cfg::kStageA, job.tmB, kx,
                                job.rn * BN + static_cast<int>(crank) * (BN / 2), pb, bar);
             }
             ++issued;

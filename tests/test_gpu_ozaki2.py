@@ -133,7 +133,9 @@ def test_bitexact_tile_variants(phpc, torch_cuda, monkeypatch, cluster, bn, spli
 def test_pairs_split_many_waves_bitexact(phpc, torch_cuda, monkeypatch, bn):
     """CTA pairs with (tile, modulus) units over several waves of units and
     K above one exact chunk (partial residues folded between chunks), odd
-    tile rows: the bits of single CTAs on the same inputs."""
+    tile rows, K not a multiple of the 64-deep K-step: the bits of single
+    CTAs on the same inputs; and with every other round of units walking K
+    backwards (the default) or all forwards (PHPC_K_SERPENTINE=0)."""
     torch = torch_cuda
     m, k, n = 1400, 1700, 2100
     A = torch.empty((m, k), dtype=torch.float64, device="cuda")
@@ -144,16 +146,18 @@ def test_pairs_split_many_waves_bitexact(phpc, torch_cuda, monkeypatch, bn):
     W = torch.empty(ws, dtype=torch.uint8, device="cuda")
     monkeypatch.setenv("PHPC_OZAKI_BN", bn)
     outs = []
-    for cluster, split in (("1", "1"), ("2", "1"), ("2", "0")):
+    for cluster, split, serp in (("1", "1", "1"), ("2", "1", "1"), ("2", "0", "1"), ("1", "1", "0"),
+                                 ("2", "1", "0")):
         monkeypatch.setenv("PHPC_CLUSTER", cluster)
         monkeypatch.setenv("PHPC_SPLIT_MODULI", split)
+        monkeypatch.setenv("PHPC_K_SERPENTINE", serp)
         C = torch.zeros((m, n), dtype=torch.float64, device="cuda")
         phpc.dgemm_ozaki2_dev(m, k, n, A, k, B, n, C, n, 13, W, ws)
         torch.cuda.synchronize()
         assert phpc.device_status() == 0
         outs.append(C)
-    assert torch.equal(outs[1], outs[0])
-    assert torch.equal(outs[2], outs[0])
+    for i in range(1, len(outs)):
+        assert torch.equal(outs[i], outs[0]), i
 
 
 @pytest.mark.parametrize("case", [c for c in golden_cases() if c["dist"] == "index"], ids=lambda c: c["name"])
