@@ -60,6 +60,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import select
 import statistics
 import subprocess
 import sys
@@ -130,7 +131,9 @@ def measured_peaks() -> dict:
 
 
 class ClockSampler:
-    """nvidia-smi samples every 200 ms while the timed region runs."""
+    """nvidia-smi samples every 50 ms while the timed region runs. Entering
+    waits (up to 5 s) for the first sample, so that the timed region, which
+    starts after it, is covered from its beginning."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -143,10 +146,15 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
                  "-i", str(self.device_index)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+        if self.proc is not None:
+            ready, _, _ = select.select([self.proc.stdout], [], [], 5.0)
+            if ready:
+                # the first sample precedes the timed region: keep it out of the summary
+                self.proc.stdout.readline()
         return self
 
     def __exit__(self, *exc):
