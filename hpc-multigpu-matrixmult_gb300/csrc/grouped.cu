@@ -273,7 +273,7 @@ ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
 }
 
 struct TableLayout {
-  size_t split, tprob, maps, tiles, end;
+  size_t split, tprob, maps, tiles, sched, end;
 };
 
 // Output tiles of the batch at the narrowest tile width (an upper bound for
@@ -290,7 +290,8 @@ TableLayout table_layout(int count, int64_t tiles) {
   T.tprob = align_up(sizeof(GSplitProb) * (size_t)count, 256);
   T.maps = align_up(T.tprob + sizeof(TcGroupProblem) * (size_t)count, 256);
   T.tiles = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
-  T.end = align_up(T.tiles + sizeof(int2) * (size_t)tiles, 256);
+  T.sched = align_up(T.tiles + sizeof(int2) * (size_t)tiles, 256);  // the GEMM's unit counter
+  T.end = align_up(T.sched + sizeof(int), 256);
   return T;
 }
 
@@ -358,6 +359,8 @@ int launch_grouped_gemm(const phpc_grouped_plan* pl, cudaStream_t stream) {
   }
   CUtensorMap dummy;
   std::memset(&dummy, 0, sizeof dummy);
+  if (pl->table.next_unit && cudaMemsetAsync(pl->table.next_unit, 0, sizeof(int), stream) != cudaSuccess)
+    return PHPC_ERR_CUDA;
   const int grid = std::min(pl->total_tiles, dev->sm_count);
   tc_slice_gemm_kernel<BN, MODE, true><<<grid, kTcThreads, Cfg::kSmem, stream>>>(dummy, dummy, pl->pairs, a,
                                                                                  pl->table);
@@ -561,6 +564,13 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->table.probs = reinterpret_cast<const TcGroupProblem*>(base + T.tprob);
   pl->table.maps = reinterpret_cast<const CUtensorMap*>(base + T.maps);
   pl->table.tiles = reinterpret_cast<const int2*>(base + T.tiles);
+  // units handed out in order by a counter (PHPC_GROUPED_SCHED=static: CTA c
+  // takes units c, c + grid, ...)
+  {
+    const char* env = getenv("PHPC_GROUPED_SCHED");
+    const bool stat = env && std::strcmp(env, "static") == 0;
+    pl->table.next_unit = stat ? nullptr : reinterpret_cast<int*>(base + T.sched);
+  }
   std::vector<int2> htiles(tiles);
   for (int i = 0; i < count && rc == PHPC_OK; ++i)
     for (int u = 0; u < ht[i].tm * ht[i].tn; ++u) htiles[ht[i].tile_start + u] = make_int2(i, u);

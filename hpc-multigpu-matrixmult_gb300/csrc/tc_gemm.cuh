@@ -133,7 +133,19 @@ struct TcGroupTable {
   const TcGroupProblem* probs;  // [count]
   const CUtensorMap* maps;      // [2 * count], 64-byte aligned
   const int2* tiles;            // [ntiles]: (problem, tile index within the problem), one load per tile
+  int* next_unit;               // non-null: units handed out in order by this counter (zeroed before
+                                // each launch), else CTA c takes units c, c + grid, ...
 };
+
+constexpr int kTcUnitQ = 4;  // units the producer may claim ahead of the MMA issuer and the epilogue
+
+// Work unit u -> (tile t, first pair p0). Without split a unit is a tile with
+// all its pairs; with split (kResidue) a unit is one (tile, modulus), moduli
+// outer.
+__device__ __forceinline__ void tc_unit(int u, int ntiles, bool split, int& t, int& p0) {
+  t = split ? u % ntiles : u;
+  p0 = split ? u / ntiles : 0;
+}
 
 // What one output tile needs: its problem's sizes, operands and position.
 struct TcJob {
@@ -162,7 +174,7 @@ struct TcCfg {
   static constexpr int kScratchPerWarp = 32 * 33 * 4;       // 32x32 transpose tile, padded
   static constexpr int kTmemCols = 2 * BN;                  // two accumulator buffers
   static constexpr size_t kSmem =
-      (size_t)kStages * kStageBytes + kTcEpiWarps * kScratchPerWarp + 256 /*barriers*/ + 1024 /*align*/;
+      (size_t)kStages * kStageBytes + kTcEpiWarps * kScratchPerWarp + 512 /*barriers, unit queue*/ + 1024 /*align*/;
 };
 
 // Tile t of a tm x tn tile grid in L2 raster order: groups of group_rows tile
@@ -264,7 +276,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* tfull = empty + SMAX;   // [2] MMA -> epilogue
   uint64_t* tempty = tfull + 2;     // [2] epilogue -> MMA
   uint64_t* drain = tempty + 2;     // MMA issuer waits here for its last MMAs before teardown
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  uint64_t* uq_full = drain + 1;    // [kTcUnitQ] unit queue (grouped, next_unit): producer -> MMA, epilogue
+  uint64_t* uq_empty = uq_full + kTcUnitQ;  // [kTcUnitQ] MMA issuer and epilogue warps -> producer
+  int* uq_unit = reinterpret_cast<int*>(uq_empty + kTcUnitQ);  // [kTcUnitQ]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(uq_unit + kTcUnitQ);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Work units: 128 x BN tiles (CLUSTER = 1) or 256 x BN pair tiles (CLUSTER = 2).
@@ -285,6 +300,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(&tempty[b], CLUSTER * kTcEpiWarps);  // pair: the leader's, released by both CTAs' epilogues
     }
     mbar_init(drain, 1);
+    for (int q = 0; q < kTcUnitQ; ++q) {
+      mbar_init(&uq_full[q], 1);
+      mbar_init(&uq_empty[q], 1 + kTcEpiWarps);
+    }
     fence_mbar_init();
   }
   if (warp == 1) {
@@ -311,6 +330,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   // CTAs (or CTA pairs) of a wave share one modulus's planes in L2
   const bool split = MODE == kResidue && args.split_pairs != 0;
   const int nunits = pair_ok ? ntiles * (split ? pairs.n : 1) : 0;
+  // Grouped problems have units of very different lengths, so a fixed
+  // assignment (CTA c: units c, c + grid, ...) lets the CTAs drift apart and
+  // the tiles of one problem, which share its planes in L2, run at different
+  // times. With next_unit the producer claims the next unit of the global
+  // order when it starts loading it and passes it to the MMA issuer and the
+  // epilogue through a small queue in shared memory (slot value -1: no more
+  // units), so the units in flight on all SMs stay consecutive.
+  const bool dyn = GROUPED && CLUSTER == 1 && gt.next_unit != nullptr;
   // Each role's code is dominated by its own setmaxnreg, so the compiler can
   // allocate up to kTcRegsHigh registers in the epilogue branch.
   if (warp < kTcFirstEpiWarp) {
@@ -334,9 +361,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       // exact integers, so the order of the K-steps does not change a bit.
       const bool serp = MODE == kResidue && !GROUPED && args.k_serpentine != 0;
       int round = 0;
-      for (int u = unit0; u < nunits && ok; u += ustride, ++round) {
-        const int t = split ? u % ntiles : u;
-        const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
+      uint32_t qphase = 0;
+      for (int i = 0; ok; ++i, ++round) {
+        int u;
+        if (dyn) {
+          const int q = i % kTcUnitQ;
+          if (!wait_parity(&uq_empty[q], qphase ^ 1, status, 16)) { ok = false; break; }
+          u = atomicAdd(gt.next_unit, 1);
+          if (u >= nunits) u = -1;
+          uq_unit[q] = u;
+          mbar_arrive(&uq_full[q]);
+          if (q == kTcUnitQ - 1) qphase ^= 1;
+          if (u < 0) break;
+        } else {
+          u = unit0 + i * ustride;
+          if (u >= nunits) break;
+        }
+        int t, p0;
+        tc_unit(u, ntiles, split, t, p0);
+        const int p1 = split ? p0 + 1 : pairs.n;
         TcJob job;
         tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
         const bool rev = serp && (round & 1);
@@ -384,9 +427,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       uint32_t tphase[2] = {0, 0};
       int buf = 0;
       bool ok = true;
-      for (int u = unit0; u < nunits && ok; u += ustride) {
-        const int t = split ? u % ntiles : u;
-        const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
+      uint32_t qphase = 0;
+      for (int i = 0; ok; ++i) {
+        int u;
+        if (dyn) {
+          const int q = i % kTcUnitQ;
+          if (!wait_parity(&uq_full[q], qphase, status, 17)) { ok = false; break; }
+          u = uq_unit[q];
+          mbar_arrive(&uq_empty[q]);
+          if (q == kTcUnitQ - 1) qphase ^= 1;
+          if (u < 0) break;
+        } else {
+          u = unit0 + i * ustride;
+          if (u >= nunits) break;
+        }
+        int t, p0;
+        tc_unit(u, ntiles, split, t, p0);
+        const int p1 = split ? p0 + 1 : pairs.n;
         TcJob job;
         tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
         int gstart = p0;
@@ -458,9 +515,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
     for (int j = 0; j < HALF; ++j) acc[j] = 0;
 
-    for (int u = unit0; u < nunits && ok; u += ustride) {
-      const int t = split ? u % ntiles : u;
-      const int p0 = split ? u / ntiles : 0, p1 = split ? p0 + 1 : pairs.n;
+    uint32_t qphase = 0;
+    for (int i = 0; ok; ++i) {
+      int u;
+      if (dyn) {
+        const int q = i % kTcUnitQ;
+        // all lanes must agree before the warp-collective code below
+        ok = __all_sync(0xffffffffu, wait_parity(&uq_full[q], qphase, status, 18));
+        if (!ok) break;
+        u = uq_unit[q];
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&uq_empty[q]);
+        if (q == kTcUnitQ - 1) qphase ^= 1;
+        if (u < 0) break;
+      } else {
+        u = unit0 + i * ustride;
+        if (u >= nunits) break;
+      }
+      int t, p0;
+      tc_unit(u, ntiles, split, t, p0);
+      const int p1 = split ? p0 + 1 : pairs.n;
       TcJob job;
       tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
       const int64_t row0 = (int64_t)job.rm * kTcBM + quad * 32;  // first global row of this warp's quadrant
@@ -490,14 +564,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           // whole sum; keep its bits and reduce it in FP32 at the group end
           const bool single = MODE == kResidue && nchunks == 1;
           if (single) {
+            // every 32-column load in flight before the one wait: the chunk
+            // goes straight into the accumulator registers
 #pragma unroll
-            for (int cb = 0; cb < HALF; cb += 32) {
-              uint32_t r[32];
-              tmem_ld_32x32b_x32(taddr + cb, r);
-              tc_wait_ld();
-#pragma unroll
-              for (int j = 0; j < 32; ++j) acc[cb + j] = static_cast<int32_t>(r[j]);
-            }
+            for (int cb = 0; cb < HALF; cb += 32)
+              tmem_ld_32x32b_x32(taddr + cb, *reinterpret_cast<uint32_t(*)[32]>(&acc[cb]));
+            tc_wait_ld();
           } else if (MODE == kResidue) {
             // Several chunks: each chunk (an exact f32 integer below 2^24) is
             // reduced mod m in FP32 and added to the running sum in FP32, two

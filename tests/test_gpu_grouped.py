@@ -210,3 +210,37 @@ def test_grouped_512_problems_one_graph(phpc, oracle, torch_cuda):
         err = oracle.rel_errors(C.cpu().numpy(), ref)
         assert err["frob"] <= 1e-14 and err["max"] <= 1e-14, (i, shapes[i], err)
     plan.close()
+
+
+
+@pytest.mark.parametrize("scheme", ["modular", "digits"])
+def test_grouped_unit_schedules_same_bits(phpc, torch_cuda, monkeypatch, scheme):
+    """The grouped GEMM hands its work units out in order through a counter
+    (the default) or assigns CTA c the units c, c + grid, ...
+    (PHPC_GROUPED_SCHED=static): the same bits either way, over replays of
+    the captured graph (the counter is zeroed before every launch)."""
+    torch = torch_cuda
+    shapes = phpc.grouped_shapes(60, seed=23, lo=16, hi=900)
+    rng = np.random.default_rng(9)
+    mats = [(torch.from_numpy(rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))).cuda(),
+             torch.from_numpy(rng.uniform(-1, 1, (k, n))).cuda()) for m, k, n in shapes]
+    moduli, s = (13, 0) if scheme == "modular" else (0, 7)
+    results = []
+    for sched in ("static", "dynamic"):
+        if sched == "static":
+            monkeypatch.setenv("PHPC_GROUPED_SCHED", "static")
+        else:
+            monkeypatch.delenv("PHPC_GROUPED_SCHED", raising=False)
+        Cs = [torch.zeros((m, n), dtype=torch.float64, device="cuda") for m, k, n in shapes]
+        probs = [(m, k, n, A, k, B, n, C, n) for (m, k, n), (A, B), C in zip(shapes, mats, Cs)]
+        ws = phpc.GroupedPlan.workspace_bytes(probs, s, moduli=moduli)
+        W = torch.empty(ws, dtype=torch.uint8, device="cuda")
+        plan = phpc.GroupedPlan(probs, s, W, ws, moduli=moduli)
+        for _ in range(3):  # graph replays accumulate into C
+            plan.graph_launch()
+        torch.cuda.synchronize()
+        assert phpc.device_status() == 0
+        plan.close()
+        results.append(Cs)
+    for i, (C, C0) in enumerate(zip(results[1], results[0])):
+        assert torch.equal(C, C0), i
