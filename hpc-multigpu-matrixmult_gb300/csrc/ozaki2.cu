@@ -11,11 +11,12 @@
 //     coprime moduli m_1..m_n <= 363: integers with |r| <= 181, exact in BF16
 //     (residue.cuh). Planes A_i = [n][M][ldp], B_i = [n][N][ldp] (transposed,
 //     K-major).
-//  3. n residue GEMMs on the tcgen05 engine (tc_gemm.cuh, kResidue): the exact
-//     int32 sum of A_i * B_i^T (exact f32 chunks of 512 products) reduced
-//     mod m_i, one 16-bit residue per element, into plane i of R.
+//  3. n residue GEMMs on the tcgen05 engine (tc_gemm.cuh, kResidue): A_i * B_i^T
+//     mod m_i (exact f32 chunks of 512 products, each reduced mod m_i in FP32
+//     and summed exactly), one 16-bit residue per element, into plane i of R.
 //  4. CRT (this file): C_int = sum_i r_i * W_i mod M, W_i = (M/m_i) *
-//     ((M/m_i)^-1 mod m_i), M = prod m_i, in 160-bit integer arithmetic;
+//     ((M/m_i)^-1 mod m_i), M = prod m_i (crt.cuh: on FP32 limbs when the
+//     grids guarantee |C_int| / M <= 1/2 - 1/32, else in 160-bit integers);
 //     the grids keep |A'_i| |B'_j| <= M (1/2 - 1/32), so the symmetric
 //     representative of C_int is the exact integer product A' * B'^T.
 //     C += round_to_double(C_int) * 2^(ea[i] - ba[i] + eb[j] - bb[j]).

@@ -12,17 +12,18 @@
 //          chunks, before int32 could overflow) it folds the integer sums into
 //          the FP64 output: C[i][j] += S * 2^(ea[i] + eb[j] + 2 - 8g).
 //  kResidue Modular Ozaki GEMM: pair i multiplies the residue planes of
-//          modulus m_i; its exact int32 sum (f32 chunks of 512 products of
-//          |r| <= 181) is reduced mod m_i and stored as one 16-bit residue per
-//          element in residue plane i of R; the CRT pass (ozaki2.cu) combines
-//          them. A modulus whose K fits one chunk skips the integer
-//          conversion: the exact f32 chunk is reduced in FP32 (two elements
-//          per f32x2 instruction). Residues leave through the warp's scratch
-//          so that each store instruction writes four 128-byte row segments.
-//          The moduli are independent: with split_pairs a work unit is one
-//          (tile, modulus), moduli outer, so that consecutive waves of CTAs
-//          share one modulus's planes in L2 and a ragged last wave is spread
-//          over more units.
+//          modulus m_i. Each f32 chunk (512 products of |r| <= 181, an exact
+//          integer) is reduced mod m_i in FP32 as it leaves TMEM (two
+//          elements per f32x2 instruction) and added to an FP32 running sum
+//          that stays an exact integer; at the end of the modulus the sum is
+//          stored as one 16-bit residue per element in residue plane i of R,
+//          and the CRT pass (ozaki2.cu) combines the planes. Residues leave
+//          through the warp's scratch so that each store instruction writes
+//          four 128-byte row segments. The moduli are independent: with
+//          split_pairs a work unit is one (tile, modulus), moduli outer, so
+//          that consecutive waves of CTAs share one modulus's planes in L2
+//          and a ragged last wave is spread over more units; every other
+//          round of units walks K backwards (k_serpentine).
 //  kF32    3xBF16 split GEMM: all pairs accumulate into one f32 result. The
 //          tensor cores' f32 accumulation does not round to nearest, so its
 //          error grows with the number of MMAs summed; the accumulator is
