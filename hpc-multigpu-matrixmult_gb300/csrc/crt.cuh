@@ -10,22 +10,26 @@ namespace phpc {
 constexpr int kCrtMaxModuli = 15;  // M < 2^127: weights in four 32-bit limbs, sums in five
 constexpr int kCrtMaxLimbs = 10;   // balanced 13-bit digits of M / m_i (15 moduli: 10)
 
+// What the residue GEMMs store per element and modulus (a 16-bit value): not
+// the residue r_i of the product but t_i = r_i ((M / m_i)^-1 mod m_i) mod m_i,
+// symmetric (|t_i| <= 181), plus kCrtTBias. Then sum_i t_i (M / m_i) = y
+// (mod M), so the reconstruction needs no per-modulus multiplication.
+constexpr int kCrtTBias = 256;
+
 // Constants of the reconstruction on FP32 limbs (crt_limbs_quad), each value
 // in both lanes of a packed f32x2 operation.
 struct CrtLimbs {
   int np;                                 // digits of the largest M / m_i (5 .. 10)
-  float2 inv[kCrtMaxModuli];              // (M / m_i)^-1 mod m_i
-  float2 ninvb[kCrtMaxModuli];            // -2^23 (M / m_i)^-1 mod m_i
+  float2 unbias;                          // -(2^23 + kCrtTBias)
   float2 cw[3];                           // 2^(13 j) / M rounded to float, j = np - 1, np - 2, np - 3
-  float2 rm[kCrtMaxModuli];               // 1 / m_i rounded to float
-  float2 negm[kCrtMaxModuli];             // -m_i
   float2 P[kCrtMaxModuli][kCrtMaxLimbs];  // balanced 13-bit digits of M / m_i, least significant first
   float2 negM[kCrtMaxLimbs + 1];          // balanced 13-bit digits of M, negated
 };
 
 struct CrtTable {
   int n;                          // number of moduli
-  uint32_t W[kCrtMaxModuli][4];   // CRT weights (M / m_i) ((M / m_i)^-1 mod m_i), little-endian 32-bit limbs
+  uint32_t m[kCrtMaxModuli];      // the moduli
+  uint32_t W[kCrtMaxModuli][4];   // CRT weights M / m_i (for the stored t_i mod m_i), little-endian 32-bit limbs
   uint32_t M[4];                  // product of the moduli
   uint32_t Mhalf[4];              // floor(M / 2)
   int qlimb;                      // quotient estimate from limbs qlimb, qlimb + 1 (M >> 32 qlimb in [2^20, 2^52))
@@ -189,12 +193,14 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T,
 // grid leaves the margin CrtTable::fast states).
 __device__ __forceinline__ double crt_value(const uint32_t (&rr)[kCrtMaxModuli], const CrtTable& T, int fast,
                                             int& shift) {
+  // rr[i] is the stored t_i + kCrtTBias; acc = sum_i (t_i mod m_i) (M / m_i),
   // 32-bit limbs accumulated in 64 bits (no overflow: 15 x 2^9 x 2^32 < 2^45)
   uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i) {
     if (i < T.n) {
-      const uint32_t r = rr[i];
+      const int32_t t = static_cast<int32_t>(rr[i]) - kCrtTBias;
+      const uint32_t r = static_cast<uint32_t>(t < 0 ? t + static_cast<int32_t>(T.m[i]) : t);
       a0 += static_cast<uint64_t>(r) * T.W[i][0];
       a1 += static_cast<uint64_t>(r) * T.W[i][1];
       a2 += static_cast<uint64_t>(r) * T.W[i][2];
@@ -257,15 +263,14 @@ __device__ __forceinline__ double crt_add_i128(double c, uint64_t lo, uint64_t h
 // The one-step CRT of four adjacent elements on FP32 limbs: two pairs, each
 // pair in the two lanes of packed f32x2 operations, both pairs computed in
 // one pass over the moduli so that each modulus's constants are read once
-// for the four elements. w[p][i] holds the residues mod m_i of pair p
-// (its first element in the low 16 bits, the second in the high 16 bits).
-// Valid when every result satisfies |y| / M <= 1/2 - 1/32 (CrtTable::fast);
-// gives the y of crt_value as 128-bit two's complement integers
-// (lo[e], hi[e]), e = 2 p + lane. Every step except the quotient estimate is
-// exact in FP32 (all values are integers below 2^24):
-//  1. t_i = r_i inv_i mod m_i, symmetric: with r_i read as the float
-//     2^23 + r_i, p = (2^23 + r_i) inv_i - 2^23 inv_i = r_i inv_i < 2^17 in one
-//     FMA, t_i = p - round(p / m_i) m_i (|t_i| <= m_i / 2), and
+// for the four elements. w[p][i] holds the stored t_i + kCrtTBias of pair p
+// for modulus i (its first element in the low 16 bits, the second in the
+// high 16 bits). Valid when every result satisfies |y| / M <= 1/2 - 1/32
+// (CrtTable::fast); gives the y of crt_value as 128-bit two's complement
+// integers (lo[e], hi[e]), e = 2 p + lane. Every step except the quotient
+// estimate is exact in FP32 (all values are integers below 2^24):
+//  1. t_i read as the float 2^23 + kCrtTBias + t_i (the stored bits under the
+//     exponent of 2^23), less 2^23 + kCrtTBias: one exact add;
 //     sum_i t_i (M / m_i) = y (mod M);
 //  2. S_j = sum_i t_i P_ij over the balanced 13-bit digits P_ij of M / m_i
 //     (|P_ij| <= 2^12, |S_j| <= 15 181 2^12 < 2^24);
@@ -288,18 +293,16 @@ __device__ __forceinline__ void crt_limbs_quad(const uint32_t (&w)[2][kCrtMaxMod
   for (int p = 0; p < 2; ++p)
 #pragma unroll
     for (int j = 0; j < NP; ++j) S[p][j] = make_float2(0.0f, 0.0f);
+  const float2 unbias = T.L.unbias;
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i) {
     if (i < T.n) {
-      const float2 inv = T.L.inv[i], ninvb = T.L.ninvb[i], rm = T.L.rm[i], negm = T.L.negm[i];
       float2 t[2];
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const float2 rb = make_float2(__uint_as_float(0x4B000000u | (w[p][i] & 0xFFFFu)),
+        const float2 tb = make_float2(__uint_as_float(0x4B000000u | (w[p][i] & 0xFFFFu)),
                                       __uint_as_float(0x4B000000u | (w[p][i] >> 16)));
-        const float2 pr = __ffma2_rn(rb, inv, ninvb);
-        const float2 qq = __fadd2_rn(__ffma2_rn(pr, rm, kRound), kUnround);
-        t[p] = __ffma2_rn(qq, negm, pr);
+        t[p] = __fadd2_rn(tb, unbias);
       }
 #pragma unroll
       for (int j = 0; j < NP; ++j) {

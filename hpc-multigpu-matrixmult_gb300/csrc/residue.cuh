@@ -35,6 +35,7 @@ struct ModTable {
   float2 cf[kMaxModuli][4];  // symmetric residues of 2^13, 2^26, 2^39, 2^52 mod m (|c| <= 181)
   float2 invm[kMaxModuli];   // 1 / m rounded to float
   float2 negm[kMaxModuli];   // -m
+  float winv[kMaxModuli];    // (M / m)^-1 mod m: the residue GEMM stores t = r winv mod m (crt.cuh)
   CrtTable crt;                // the reconstruction's constants
 };
 
@@ -87,8 +88,9 @@ inline ModTable make_table(int nmod, int k) {
     uint32_t inv = 0;
     for (uint32_t v = 1; v < m; ++v)
       if ((static_cast<uint64_t>(mi_mod) * v) % m == 1) { inv = v; break; }
-    const u128 W = Mi * inv;  // < M
-    for (int l = 0; l < 4; ++l) T.crt.W[i][l] = static_cast<uint32_t>(W >> (32 * l));
+    T.winv[i] = static_cast<float>(inv);
+    T.crt.m[i] = m;
+    for (int l = 0; l < 4; ++l) T.crt.W[i][l] = static_cast<uint32_t>(Mi >> (32 * l));
   }
   for (int l = 0; l < 4; ++l) {
     T.crt.M[l] = static_cast<uint32_t>(M >> (32 * l));
@@ -115,20 +117,10 @@ inline ModTable make_table(int nmod, int k) {
     return x == 0 ? used : -1;
   };
   int np = 0;
-  for (int i = 0; i < nmod; ++i) {
-    const uint32_t m = kModuli[i];
-    const u128 Mi = M / m;
-    uint32_t inv = 0;
-    for (uint32_t v = 1; v < m; ++v)
-      if ((static_cast<uint64_t>(static_cast<uint32_t>(Mi % m)) * v) % m == 1) { inv = v; break; }
-    T.crt.L.inv[i] = make_float2(static_cast<float>(inv), static_cast<float>(inv));
-    const float nb = -8388608.0f * static_cast<float>(inv);  // exact: inv < 2^9
-    T.crt.L.ninvb[i] = make_float2(nb, nb);
-    T.crt.L.rm[i] = T.invm[i];
-    T.crt.L.negm[i] = T.negm[i];
-    np = std::max(np, digits(Mi, T.crt.L.P[i], kCrtMaxLimbs));
-  }
+  for (int i = 0; i < nmod; ++i) np = std::max(np, digits(M / kModuli[i], T.crt.L.P[i], kCrtMaxLimbs));
   T.crt.L.np = np;
+  const float ub = -(8388608.0f + static_cast<float>(kCrtTBias));
+  T.crt.L.unbias = make_float2(ub, ub);
   for (int j = 0; j < 3; ++j) {
     const float c = static_cast<float>(std::ldexp(1.0, 13 * (np - 1 - j)) / static_cast<double>(M));
     T.crt.L.cw[j] = make_float2(c, c);

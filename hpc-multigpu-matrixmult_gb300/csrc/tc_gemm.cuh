@@ -42,6 +42,7 @@
 // 128 x 40 + 256 x 232 = 384 x 168. The host launches the kernel only after
 // checking that its compiled register count is 168 (tc_regs_ok).
 #pragma once
+#include "crt.cuh"
 #include "phpc_dev.cuh"
 
 namespace phpc {
@@ -70,6 +71,7 @@ struct PairList {
   uint8_t g[kTcMaxPairs];     // group id (Ozaki: diagonal p + q, 1-based digits); pairs of a group are contiguous
   uint16_t mod[kTcMaxPairs];  // kResidue: modulus of the group
   float invm[kTcMaxPairs];      // kResidue: 1 / modulus rounded to float
+  float winv[kTcMaxPairs];      // kResidue: (M / modulus)^-1 mod modulus (the stored value is r winv mod m)
 };
 
 // x - m round(x / m) for two integer-valued floats |x| < 2^24, m <= 363: the
@@ -82,14 +84,17 @@ __device__ __forceinline__ float2 reduce_pair_f32(float2 x, float m, float invm)
   return __ffma2_rn(q, make_float2(-m, -m), x);
 }
 
-// Residues in [0, m) of two integer-valued floats |x| < 2^24: the symmetric
-// remainders moved into [0, m), packed as two 16-bit values read from the
-// mantissas of r + 2^23 (lo in the low half).
-__device__ __forceinline__ uint32_t residue_pair_u16(float x0, float x1, float m, float invm) {
-  float2 r = reduce_pair_f32(make_float2(x0, x1), m, invm);
-  r.x = r.x < 0.0f ? r.x + m : r.x;
-  r.y = r.y < 0.0f ? r.y + m : r.y;
-  const float2 b = __fadd2_rn(r, make_float2(8388608.0f, 8388608.0f));
+// What the residue GEMM stores for two integer-valued floats |x| < 2^24 (the
+// products' sums mod m): t = (x mod m) winv mod m, symmetric, plus
+// kCrtTBias (crt.cuh), as two 16-bit values (lo in the low half) read from
+// the mantissas of 2^23 + kCrtTBias + t. |x mod m| <= 0.51 m after the
+// first reduction, so (x mod m) winv < 2^17 is exact, and the second
+// reduction leaves |t| <= 181.
+__device__ __forceinline__ uint32_t crt_t_pair_u16(float x0, float x1, float m, float invm, float winv) {
+  const float2 r = reduce_pair_f32(make_float2(x0, x1), m, invm);
+  const float2 t = reduce_pair_f32(__fmul2_rn(r, make_float2(winv, winv)), m, invm);
+  const float bias = 8388608.0f + static_cast<float>(kCrtTBias);
+  const float2 b = __fadd2_rn(t, make_float2(bias, bias));
   return __byte_perm(__float_as_uint(b.x), __float_as_uint(b.y), 0x5410);
 }
 
@@ -279,7 +284,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* drain = tempty + 2;     // MMA issuer waits here for its last MMAs before teardown
   uint64_t* uq_full = drain + 1;    // [kTcUnitQ] unit queue (grouped, next_unit): producer -> MMA, epilogue
   uint64_t* uq_empty = uq_full + kTcUnitQ;  // [kTcUnitQ] MMA issuer and epilogue warps -> producer
-  int* uq_unit = reinterpret_cast<int*>(uq_empty + kTcUnitQ);  // [kTcUnitQ]
+  int2* uq_unit = reinterpret_cast<int2*>(uq_empty + kTcUnitQ);  // [kTcUnitQ] (unit, its K-steps)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(uq_unit + kTcUnitQ);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -363,26 +368,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const bool serp = MODE == kResidue && !GROUPED && args.k_serpentine != 0;
       int round = 0;
       uint32_t qphase = 0;
+      // dyn: units are claimed one ahead, so that the claim's round trip to
+      // L2 overlaps the loads of the unit before
+      int u_ahead = dyn ? atomicAdd(gt.next_unit, 1) : 0;
       for (int i = 0; ok; ++i, ++round) {
-        int u;
+        int u, t = 0, p0 = 0;
+        TcJob job;
         if (dyn) {
           const int q = i % kTcUnitQ;
           if (!wait_parity(&uq_empty[q], qphase ^ 1, status, 16)) { ok = false; break; }
-          u = atomicAdd(gt.next_unit, 1);
-          if (u >= nunits) u = -1;
-          uq_unit[q] = u;
+          u = u_ahead < nunits ? u_ahead : -1;
+          if (u >= 0) {
+            tc_unit(u, ntiles, split, t, p0);
+            tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
+          }
+          // the MMA issuer gets the unit's K-steps with it (no table lookups on its path)
+          uq_unit[q] = make_int2(u, u >= 0 ? job.nk : 0);
           mbar_arrive(&uq_full[q]);
           if (q == kTcUnitQ - 1) qphase ^= 1;
           if (u < 0) break;
+          u_ahead = atomicAdd(gt.next_unit, 1);
         } else {
           u = unit0 + i * ustride;
           if (u >= nunits) break;
+          tc_unit(u, ntiles, split, t, p0);
+          tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
         }
-        int t, p0;
-        tc_unit(u, ntiles, split, t, p0);
         const int p1 = split ? p0 + 1 : pairs.n;
-        TcJob job;
-        tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
         const bool rev = serp && (round & 1);
         for (int pi = p0; pi < p1 && ok; ++pi) {
           const int pa = pairs.a[pi], pb = pairs.b[pi];
@@ -430,13 +442,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       bool ok = true;
       uint32_t qphase = 0;
       for (int i = 0; ok; ++i) {
-        int u;
+        int u, nk;
         if (dyn) {
           const int q = i % kTcUnitQ;
           if (!wait_parity(&uq_full[q], qphase, status, 17)) { ok = false; break; }
-          u = uq_unit[q];
+          const int2 e = uq_unit[q];
           mbar_arrive(&uq_empty[q]);
           if (q == kTcUnitQ - 1) qphase ^= 1;
+          u = e.x;
+          nk = e.y;
           if (u < 0) break;
         } else {
           u = unit0 + i * ustride;
@@ -445,8 +459,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         int t, p0;
         tc_unit(u, ntiles, split, t, p0);
         const int p1 = split ? p0 + 1 : pairs.n;
-        TcJob job;
-        tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
+        if (!dyn) {
+          TcJob job;
+          tc_job<GROUPED, CLUSTER>(t, args, &tmA, &tmB, gt, crank, job);
+          nk = job.nk;
+        }
         int gstart = p0;
         while (gstart < p1 && ok) {
           int gend = gstart + 1;
@@ -454,7 +471,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             while (gend < p1 && pairs.g[gend] == pairs.g[gstart]) ++gend;
           else
             gend = p1;
-          const int total = (gend - gstart) * job.nk;
+          const int total = (gend - gstart) * nk;
           const int chunk = MODE == kOzaki ? kTcChunkSteps : MODE == kResidue ? kTcResidueChunkSteps : kTcF32ChunkSteps;
           for (int done = 0; done < total && ok; done += chunk) {
             const int len = min(chunk, total - done);
@@ -524,7 +541,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // all lanes must agree before the warp-collective code below
         ok = __all_sync(0xffffffffu, wait_parity(&uq_full[q], qphase, status, 18));
         if (!ok) break;
-        u = uq_unit[q];
+        u = uq_unit[q].x;
         __syncwarp();
         if (lane == 0) mbar_arrive(&uq_empty[q]);
         if (q == kTcUnitQ - 1) qphase ^= 1;
@@ -645,12 +662,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             // (acc holds exact f32 integers: the chunk itself, or the sum of
             // the reduced chunks)
             uint16_t* rplane = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane;
+            const float winv = pairs.winv[gstart];
 #pragma unroll
             for (int h = 0; h < HALF; h += 64) {
 #pragma unroll
               for (int q = 0; q < 32; ++q)
-                tr[lane * 33 + q] =
-                    residue_pair_u16(__int_as_float(acc[h + 2 * q]), __int_as_float(acc[h + 2 * q + 1]), mf, invm);
+                tr[lane * 33 + q] = crt_t_pair_u16(__int_as_float(acc[h + 2 * q]), __int_as_float(acc[h + 2 * q + 1]),
+                                                   mf, invm, winv);
               __syncwarp();
               const int seg = lane & 7;
               const int col = col0 + h + seg * 8;

@@ -1,18 +1,22 @@
 """Model of the CRT reconstruction on FP32 limbs (the kernel crt_limbs_quad in
-csrc/crt.cuh), used by the CPU tests to check its arithmetic on many residue
-vectors: every step that the kernel does exactly must stay within the range
-in which FP32 represents integers exactly, and the result must be the
+csrc/crt.cuh, fed by the residue GEMM's epilogue crt_t_pair_u16 in
+csrc/tc_gemm.cuh), used by the CPU tests to check its arithmetic on many
+residue vectors: every step that the kernels do exactly must stay within the
+range in which FP32 represents integers exactly, and the result must be the
 symmetric representative of sum_i r_i W_i mod M.
 
 The reconstruction, for residues r_i in [0, m_i) of the q moduli:
 
-1. t_i = r_i inv_i mod m_i, symmetric (|t_i| <= m_i / 2), inv_i =
-   (M / m_i)^-1 mod m_i: p = r_i inv_i < 2^17 exactly, qq = round(p / m_i)
-   through the 1.5 2^23 rounding constant, t_i = p - qq m_i by one FMA.
-   Then sum_i t_i (M / m_i) = sum_i r_i W_i (mod M) with W_i = (M / m_i) inv_i.
-2. S_j = sum_i t_i P_ij, P_ij the balanced 13-bit digits of P_i = M / m_i
-   (|P_ij| <= 2^12): |S_j| <= 15 * 181 * 2^12 < 2^24, so every partial sum is
-   an integer FP32 holds exactly.
+1. (GEMM epilogue) the product's sum x (|x| < 2^24, x = r_i mod m_i) is
+   reduced mod m_i in FP32: r = x - m_i round(x / m_i) with the quotient
+   through the 1.5 2^23 rounding constant and fl(1 / m_i), |r| <= 0.51 m_i;
+   then t_i = p - m_i round(p / m_i) for p = r inv_i (< 2^17, exact), inv_i =
+   (M / m_i)^-1 mod m_i; |t_i| <= 181. Stored as t_i + 256 in 16 bits, and
+   sum_i t_i (M / m_i) = sum_i r_i W_i (mod M) with W_i = (M / m_i) inv_i.
+2. (CRT) t_i read back as (2^23 + 256 + t_i) - (2^23 + 256), exact;
+   S_j = sum_i t_i P_ij over the balanced 13-bit digits P_ij of
+   P_i = M / m_i (|P_ij| <= 2^12): |S_j| <= 15 * 181 * 2^12 < 2^24, so every
+   partial sum is an integer FP32 holds exactly.
 3. est = S_(NP-1) c_(NP-1) + S_(NP-2) c_(NP-2) + S_(NP-3) c_(NP-3) in FP32,
    c_j = fl(2^(13 j) / M): the top three limb sums give acc / M (|acc / M| =
    |sum_i t_i / m_i| <= 7.5) to within 2^-19 (the lower limbs weigh below
@@ -88,13 +92,11 @@ def reconstruct(T: Table, r: list[int], checks: dict | None = None) -> int:
     S = [f32(0)] * T.NP
     tmax = 0
     for i, m in enumerate(T.m):
-        # r as the float 2^23 + r; p = (2^23 + r) inv - 2^23 inv = r inv, exact in one FMA
-        rb = f32(8388608 + r[i])
-        p = fma32(rb, f32(T.inv[i]), f32(-8388608.0 * T.inv[i]))
-        assert float(p) == r[i] * T.inv[i]
-        qq = fma32(p, f32(1.0 / m), MAGIC) - MAGIC
-        t = fma32(qq, f32(-m), p)
-        assert float(t) == r[i] * T.inv[i] - float(qq) * m
+        stored = gemm_t(r[i], m, T.inv[i]) + 256  # the 16-bit value the residue GEMM writes
+        assert 0 <= stored < 1 << 16
+        tb = (np.uint32(0x4B000000) | np.uint32(stored)).view(np.float32)
+        t = f32(np.float32(tb) + np.float32(-(8388608.0 + 256.0)))
+        assert float(t) == stored - 256
         tmax = max(tmax, abs(int(t)))
         for j in range(T.NP):
             exact = int(S[j]) + int(t) * T.Pd[i][j]
@@ -124,6 +126,29 @@ def reconstruct(T: Table, r: list[int], checks: dict | None = None) -> int:
         checks["Y"] = max(checks.get("Y", 0), max(abs(v) for v in Yexact))
         checks["d"] = max(checks.get("d", 0), max(abs(v) for v in ints))
     return y
+
+
+def reduce_f32(x, m: int) -> np.float32:
+    """x - m round(x / m) as the kernels compute it (reduce_pair_f32): the
+    quotient from fl(1 / m) through the rounding constant, the remainder by
+    one FMA (exact)."""
+    q = fma32(f32(x), f32(1.0 / m), MAGIC) - MAGIC
+    rem = fma32(q, f32(-m), f32(x))
+    assert float(rem) == float(x) - float(q) * m
+    return rem
+
+
+def gemm_t(x: int, m: int, inv: int) -> int:
+    """The residue GEMM epilogue's t for an exact product sum x (|x| < 2^24):
+    (x mod m) inv mod m, symmetric (crt_t_pair_u16)."""
+    assert abs(x) < 1 << 24
+    r = reduce_f32(x, m)
+    assert abs(float(r)) <= 0.51 * m
+    p = np.float32(r) * np.float32(inv)
+    assert float(p) == float(r) * inv and abs(float(p)) < 1 << 17
+    t = reduce_f32(p, m)
+    assert abs(float(t)) <= 181 and (int(t) - int(x) * inv) % m == 0
+    return int(t)
 
 
 def symmetric_crt(T: Table, r: list[int]) -> int:

@@ -44,3 +44,18 @@ def test_limb_crt_extreme_residues(q):
         tried += 1
         assert CL.reconstruct(T, r) == y
     assert tried > 200
+
+
+@pytest.mark.parametrize("q", [8, 13, 15])
+def test_gemm_epilogue_t_on_chunk_sums(q):
+    """The residue GEMM's stored value for product sums across the exact f32
+    range (|x| < 2^24, both signs, the range ends): t = (x mod m) inv mod m,
+    |t| <= 181, exact at every step (crt_limb_model.gemm_t asserts each)."""
+    T = CL.Table(q)
+    rng = np.random.default_rng(300 + q)
+    xs = [0, 1, -1, (1 << 24) - 1, -((1 << 24) - 1), 512 * 181 * 181, -512 * 181 * 181]
+    xs += [int(v) for v in rng.integers(-(1 << 24) + 1, 1 << 24, 3000)]
+    for i, m in enumerate(T.m):
+        for x in xs:
+            t = CL.gemm_t(x, m, T.inv[i])
+            assert abs(t) <= 181 and (t - x * T.inv[i]) % m == 0
