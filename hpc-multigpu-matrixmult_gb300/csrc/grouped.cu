@@ -382,12 +382,21 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   const bool modular = pl->moduli > 0;
   if (pl->total_rows > 0) {
     if (modular) {
+      // B's column scans and split on the side stream beside A's (both
+      // memory-bound); the GEMM waits for both
+      cudaStream_t side = side_stream();
+      if (!side || !stream_fork(stream, side)) side = stream;
       g_scan_rows_grid_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count,
                                                                                pl->total_rows, pl->mods, status);
-      g_scan_cols_part_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
-                                                                                   pl->total_cunits, status);
-      g_scan_cols_merge_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, stream>>>(pl->d_split, pl->count,
-                                                                                  pl->total_cols, pl->mods);
+      g_scan_cols_part_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, side>>>(pl->d_split, pl->count,
+                                                                                 pl->total_cunits, status);
+      g_scan_cols_merge_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, side>>>(pl->d_split, pl->count,
+                                                                                pl->total_cols, pl->mods);
+      g_residue_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
+                                                                                 pl->total_pieces, pl->mods);
+      g_residue_cols_kernel<<<pl->total_rblocks, 256, 0, side>>>(pl->d_split, pl->count, pl->total_rblocks,
+                                                                 pl->mods);
+      if (cudaGetLastError() != cudaSuccess || (side != stream && !stream_fork(side, stream))) return PHPC_ERR_CUDA;
     } else {
       g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,
                                                                           status);
@@ -396,12 +405,7 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
       g_scan_cols_kernel<<<ceil_div(pl->total_cunits, 128), 128, 0, stream>>>(pl->d_split, pl->count,
                                                                               pl->total_cunits, status);
     }
-    if (modular) {
-      g_residue_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
-                                                                                 pl->total_pieces, pl->mods);
-      g_residue_cols_kernel<<<pl->total_rblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rblocks,
-                                                                   pl->mods);
-    } else {
+    if (!modular) {
       g_split_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
                                                                                pl->total_pieces, pl->s);
       g_split_cols_kernel<<<pl->total_sblocks, 256, 0, stream>>>(pl->d_split, pl->count, pl->total_sblocks, pl->s);
@@ -658,6 +662,7 @@ extern "C" int phpc_grouped_graph_launch(phpc_grouped_plan* plan, void* stream) 
   } else {
     if (!plan->exec) {
       cudaStream_t cs = nullptr;
+      side_stream_ready();  // the side stream and its event exist before the capture starts
       if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
       if (rc == PHPC_OK && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         rc = PHPC_ERR_CUDA;

@@ -250,6 +250,18 @@ int ozaki2_prepare2(int m, int k, int n, const double* dA, int64_t lda, const do
   return rc;
 }
 
+// The same on one caller stream: B's scans and split run on this thread's
+// side stream beside A's (both are memory-bound; run together, one's ramp-up
+// and tail overlap the other's), and the caller's stream waits for them.
+int ozaki2_prepare_on(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, int nmod,
+                      void* ws, size_t ws_bytes, cudaStream_t stream) {
+  const cudaStream_t side = side_stream();
+  if (!side || !stream_fork(stream, side)) return ozaki2_prepare2(m, k, n, dA, lda, dB, ldb, nmod, ws, ws_bytes, stream, stream);
+  int rc = ozaki2_prepare2(m, k, n, dA, lda, dB, ldb, nmod, ws, ws_bytes, stream, side);
+  if (!stream_fork(side, stream) && rc == PHPC_OK) rc = PHPC_ERR_CUDA;
+  return rc;
+}
+
 // The residue GEMMs of the block rows [r0, r0 + rows) x columns [c0, c0 +
 // cols): plane i of R = (A_i * B_i^T) mod m_i, one 16-bit residue per element.
 // Tile width, cluster and raster are those of the full m x k x n problem.
@@ -336,7 +348,7 @@ int ozaki2_reconstruct(int m, int k, int n, double* dC, int64_t ldc, int nmod, c
 
 int dgemm_ozaki2(int m, int k, int n, const double* dA, int64_t lda, const double* dB, int64_t ldb, double* dC,
                  int64_t ldc, int nmod, void* ws, size_t ws_bytes, cudaStream_t stream, int bn) {
-  int rc = ozaki2_prepare2(m, k, n, dA, lda, dB, ldb, nmod, ws, ws_bytes, stream, stream);
+  int rc = ozaki2_prepare_on(m, k, n, dA, lda, dB, ldb, nmod, ws, ws_bytes, stream);
   if (rc == PHPC_OK) rc = ozaki2_multiply(m, k, n, nmod, ws, ws_bytes, stream, bn);
   if (rc == PHPC_OK) rc = ozaki2_reconstruct(m, k, n, dC, ldc, nmod, ws, ws_bytes, stream);
   return rc;
@@ -374,7 +386,7 @@ extern "C" int phpc_ozaki2_prepare_dev(int m, int k, int n, const double* dA, in
   int rc = ozaki2_args(m, k, n, moduli, true, dA, lda, true, dB, ldb, false, nullptr, 0);
   if (rc == PHPC_OK && m > 0 && n > 0 && k > 0) {
     const cudaStream_t st = static_cast<cudaStream_t>(stream);
-    rc = phpc::ozaki2_prepare2(m, k, n, dA, lda, dB, ldb, moduli, workspace, workspace_bytes, st, st);
+    rc = phpc::ozaki2_prepare_on(m, k, n, dA, lda, dB, ldb, moduli, workspace, workspace_bytes, st);
   }
   phpc::set_last_error(rc);
   return rc;

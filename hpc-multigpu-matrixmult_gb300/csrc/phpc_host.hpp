@@ -85,6 +85,14 @@ int ozaki_multiply(int m, int k, int n, double* dC, int64_t ldc, int s, const vo
 // Device memory pool of the host entry points (one per device, grow-only
 // unless PHPC_POOL_KEEP=0): buffers of one call are reused by the next.
 cudaMemPool_t host_api_pool();
+// A second stream of this host thread on the current device, for work that
+// can run beside the caller's stream (nullptr if it cannot be created).
+cudaStream_t side_stream();
+// Makes `to` wait for the work submitted to `from` so far (an event; valid
+// under stream capture, where it adds `to` to the captured graph).
+bool stream_fork(cudaStream_t from, cudaStream_t to);
+// Creates this thread's side stream and fork event (call before a capture).
+bool side_stream_ready();
 int default_slices(int m, int k, int n);
 // Number of moduli of the modular scheme for this shape, or 0 for the digit
 // scheme (default_slices slices).

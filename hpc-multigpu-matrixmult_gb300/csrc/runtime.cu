@@ -76,6 +76,42 @@ cudaMemPool_t host_api_pool() {
   return g_pool[dev];
 }
 
+// A second stream of this host thread on the current device (non-blocking,
+// created on first use, kept for the thread's lifetime).
+cudaStream_t side_stream() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  thread_local cudaStream_t t_side[kMaxDevices] = {};
+  if (!t_side[dev] && cudaStreamCreateWithFlags(&t_side[dev], cudaStreamNonBlocking) != cudaSuccess) {
+    t_side[dev] = nullptr;
+    cudaGetLastError();
+  }
+  return t_side[dev];
+}
+
+namespace {
+// One event per thread and device, recorded and waited on at once: a wait
+// binds to the record made just before it, so the event can be recorded
+// again right away (also while a graph is being captured).
+cudaEvent_t fork_event() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+  thread_local cudaEvent_t t_ev[kMaxDevices] = {};
+  if (!t_ev[dev] && cudaEventCreateWithFlags(&t_ev[dev], cudaEventDisableTiming) != cudaSuccess) {
+    t_ev[dev] = nullptr;
+    cudaGetLastError();
+  }
+  return t_ev[dev];
+}
+}  // namespace
+
+bool stream_fork(cudaStream_t from, cudaStream_t to) {
+  const cudaEvent_t e = fork_event();
+  return e && cudaEventRecord(e, from) == cudaSuccess && cudaStreamWaitEvent(to, e, 0) == cudaSuccess;
+}
+
+bool side_stream_ready() { return side_stream() != nullptr && fork_event() != nullptr; }
+
 bool encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
                   const uint64_t* strides_bytes, const uint32_t* box, CUtensorMapSwizzle swz) {
   {
