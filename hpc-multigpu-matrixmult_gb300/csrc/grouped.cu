@@ -74,6 +74,21 @@ __device__ __forceinline__ int locate(const GSplitProb* P, int count, int x, F s
   return lo;
 }
 
+// locate() for consecutive x across the active lanes of a warp (x rising
+// with the lane): the lowest active lane searches once, the others walk on
+// from its problem (a warp's x rarely leave it).
+template <typename F>
+__device__ __forceinline__ int locate_warp(const GSplitProb* P, int count, int x, F start) {
+  const unsigned act = __activemask();
+  const int leader = __ffs(act) - 1;
+  const int x0 = __shfl_sync(act, x, leader);
+  int p = 0;
+  if ((threadIdx.x & 31) == leader) p = locate(P, count, x0, start);
+  p = __shfl_sync(act, p, leader);
+  while (p + 1 < count && start(P[p + 1]) <= x) ++p;
+  return p;
+}
+
 __global__ void g_scan_rows_kernel(const GSplitProb* __restrict__ P, int count, int total_rows, int* status) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= total_rows) return;
@@ -87,7 +102,7 @@ constexpr int kScanKChunk = 256;  // rows of B one column-scan unit covers
 __global__ void g_reset_cols_kernel(const GSplitProb* __restrict__ P, int count, int total_cols) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= total_cols) return;
-  const GSplitProb& p = P[locate(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
+  const GSplitProb& p = P[locate_warp(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
   p.eb[c - p.col_start] = kExpZero;
 }
 
@@ -96,7 +111,7 @@ __global__ void g_reset_cols_kernel(const GSplitProb* __restrict__ P, int count,
 __global__ void g_scan_cols_kernel(const GSplitProb* __restrict__ P, int count, int total_units, int* status) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= total_units) return;
-  const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.cunit_start; })];
+  const GSplitProb& p = P[locate_warp(P, count, u, [](const GSplitProb& q) { return q.cunit_start; })];
   const int w = u - p.cunit_start;
   const int64_t col = w % p.n;
   const int k0 = (w / p.n) * kScanKChunk, k1 = min(p.k, k0 + kScanKChunk);
@@ -131,7 +146,7 @@ __global__ void g_scan_rows_grid_kernel(const GSplitProb* __restrict__ P, int co
 __global__ void g_scan_cols_part_kernel(const GSplitProb* __restrict__ P, int count, int total_units, int* status) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= total_units) return;
-  const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.cunit_start; })];
+  const GSplitProb& p = P[locate_warp(P, count, u, [](const GSplitProb& q) { return q.cunit_start; })];
   const int w = u - p.cunit_start;
   const int64_t col = w % p.n;
   const int chunk = w / p.n;
@@ -149,7 +164,7 @@ __global__ void g_scan_cols_merge_kernel(const GSplitProb* __restrict__ P, int c
                                          const __grid_constant__ ModTable T) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= total_cols) return;
-  const GSplitProb& p = P[locate(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
+  const GSplitProb& p = P[locate_warp(P, count, c, [](const GSplitProb& q) { return q.col_start; })];
   const int64_t col = c - p.col_start;
   const int chunks = (p.k + kScanKChunk - 1) / kScanKChunk;
   NormAcc acc;
@@ -172,7 +187,7 @@ struct RowPiece {
 };
 
 __device__ __forceinline__ RowPiece row_piece(const GSplitProb* __restrict__ P, int count, int t) {
-  const GSplitProb& p = P[locate(P, count, t, [](const GSplitProb& q) { return q.piece_start; })];
+  const GSplitProb& p = P[locate_warp(P, count, t, [](const GSplitProb& q) { return q.piece_start; })];
   const int per_row = static_cast<int>(p.ldp >> 3);
   const int local = t - p.piece_start;
   return RowPiece{&p, local / per_row, static_cast<int64_t>(local % per_row) * 8};
