@@ -655,20 +655,28 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               }
               continue;
             }
-            // One 16-bit residue per element, 64 columns at a time: each lane
-            // reduces its row's 64 residues into the warp's scratch (32 words
-            // per row), then the warp stores 4 rows x 128 bytes per
-            // instruction (lane: row 4 i + lane / 8, 16-byte segment lane % 8).
-            // (acc holds exact f32 integers: the chunk itself, or the sum of
-            // the reduced chunks)
+            // One 16-bit value per element, 64 columns at a time: each lane
+            // writes its row's 64 values into the warp's scratch as eight
+            // 16-byte chunks (row r's chunk c at position c ^ (r % 8), so
+            // that the 8 lanes of a quarter-warp hit distinct banks), then
+            // the warp stores 4 rows x 128 bytes per instruction (lane: row
+            // 4 i + lane / 8, 16-byte segment lane % 8), reading its chunk
+            // with one 16-byte load. (acc holds exact f32 integers: the chunk
+            // itself, or the sum of the reduced chunks.)
             uint16_t* rplane = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane;
             const float winv = pairs.winv[gstart];
+            uint4* tq = reinterpret_cast<uint4*>(tr);  // [32 rows][8 chunks], 4 KB of the warp's scratch
 #pragma unroll
             for (int h = 0; h < HALF; h += 64) {
 #pragma unroll
-              for (int q = 0; q < 32; ++q)
-                tr[lane * 33 + q] = crt_t_pair_u16(__int_as_float(acc[h + 2 * q]), __int_as_float(acc[h + 2 * q + 1]),
-                                                   mf, invm, winv);
+              for (int c = 0; c < 8; ++c) {
+                uint32_t w[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                  w[e] = crt_t_pair_u16(__int_as_float(acc[h + 8 * c + 2 * e]), __int_as_float(acc[h + 8 * c + 2 * e + 1]),
+                                        mf, invm, winv);
+                tq[lane * 8 + (c ^ (lane & 7))] = make_uint4(w[0], w[1], w[2], w[3]);
+              }
               __syncwarp();
               const int seg = lane & 7;
               const int col = col0 + h + seg * 8;
@@ -676,12 +684,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
               for (int i = 0; i < 8; ++i) {
                 const int r = 4 * i + (lane >> 3);
                 const int64_t grow = row0 + r;
-                const uint32_t* src = tr + r * 33 + seg * 4;
+                const uint4 v = tq[r * 8 + (seg ^ (r & 7))];
                 if (grow < job.M) {
                   uint16_t* dst = rplane + grow * job.ldr + col;
                   if (col + 8 <= job.N) {
-                    *reinterpret_cast<uint4*>(dst) = make_uint4(src[0], src[1], src[2], src[3]);
+                    *reinterpret_cast<uint4*>(dst) = v;
                   } else {
+                    const uint32_t src[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
                     for (int e = 0; e < 8; ++e)
                       if (col + e < job.N) dst[e] = static_cast<uint16_t>(src[e >> 1] >> (16 * (e & 1)));
