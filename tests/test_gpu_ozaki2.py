@@ -290,9 +290,9 @@ def test_crt_multi_step_path_same_bits(phpc, torch_cuda, monkeypatch, nmod):
 
 
 def test_long_k_intermediate_reduction(phpc, torch_cuda):
-    """K = 70000 > 127 chunks of 512 products: the int32 sums are reduced mod
-    m_i in the middle of a modulus (before they could overflow) and the
-    result stays bit-identical to the exact model."""
+    """K = 70000 > 127 chunks of 512 products: the running sums of the
+    reduced chunks are reduced mod m_i again in the middle of a modulus (every
+    127 chunks) and the result stays bit-identical to the exact model."""
     rng = np.random.default_rng(70000)
     m, k, n = 12, 70000, 20
     a = rng.uniform(-1, 1, (m, k))
