@@ -9,6 +9,15 @@ namespace phpc {
 
 constexpr int kCrtMaxModuli = 15;  // M < 2^127: weights in four 32-bit limbs, sums in five
 constexpr int kCrtMaxLimbs = 10;   // balanced 13-bit digits of M / m_i (15 moduli: 10)
+constexpr int kCrtMinModuli = 8;
+
+// Balanced 13-bit digits of the largest M / m_i for the first n moduli
+// (residue.cuh's kModuli); make_table computes the same count from the
+// moduli and the launchers check that the two agree.
+__host__ __device__ constexpr int crt_digits(int n) {
+  constexpr int kDigits[kCrtMaxModuli + 1] = {0, 0, 0, 0, 0, 0, 0, 0, 5, 6, 6, 7, 8, 8, 9, 10};
+  return kDigits[n];
+}
 
 // What the residue GEMMs store per element and modulus (a 16-bit value): not
 // the residue r_i of the product but t_i = r_i ((M / m_i)^-1 mod m_i) mod m_i,
@@ -191,21 +200,20 @@ __device__ __forceinline__ double crt_round(uint32_t (&l)[5], const CrtTable& T,
 // The CRT of one element from its residues r[i] mod m_i: acc = sum r_i W_i,
 // rounded as crt_round (fast: the one-step path, allowed when the product's
 // grid leaves the margin CrtTable::fast states).
+template <int NMOD>
 __device__ __forceinline__ double crt_value(const uint32_t (&rr)[kCrtMaxModuli], const CrtTable& T, int fast,
                                             int& shift) {
   // rr[i] is the stored t_i + kCrtTBias; acc = sum_i (t_i mod m_i) (M / m_i),
   // 32-bit limbs accumulated in 64 bits (no overflow: 15 x 2^9 x 2^32 < 2^45)
   uint64_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
-  for (int i = 0; i < kCrtMaxModuli; ++i) {
-    if (i < T.n) {
-      const int32_t t = static_cast<int32_t>(rr[i]) - kCrtTBias;
-      const uint32_t r = static_cast<uint32_t>(t < 0 ? t + static_cast<int32_t>(T.m[i]) : t);
-      a0 += static_cast<uint64_t>(r) * T.W[i][0];
-      a1 += static_cast<uint64_t>(r) * T.W[i][1];
-      a2 += static_cast<uint64_t>(r) * T.W[i][2];
-      a3 += static_cast<uint64_t>(r) * T.W[i][3];
-    }
+  for (int i = 0; i < NMOD; ++i) {
+    const int32_t t = static_cast<int32_t>(rr[i]) - kCrtTBias;
+    const uint32_t r = static_cast<uint32_t>(t < 0 ? t + static_cast<int32_t>(T.m[i]) : t);
+    a0 += static_cast<uint64_t>(r) * T.W[i][0];
+    a1 += static_cast<uint64_t>(r) * T.W[i][1];
+    a2 += static_cast<uint64_t>(r) * T.W[i][2];
+    a3 += static_cast<uint64_t>(r) * T.W[i][3];
   }
   uint32_t l[5];
   uint64_t t = a0;
@@ -282,10 +290,12 @@ __device__ __forceinline__ double crt_add_i128(double c, uint64_t lo, uint64_t h
 //     (|d_j| < 2^13), read out as integers through the rounding constant
 //     1.5 2^23; four digits make a 52-bit chunk (int64), and
 //     y = A + B 2^52 + C 2^104 for the chunks A, B, C.
-// NP = T.L.np, the number of digits of the largest M / m_i.
-template <int NP>
+// NMOD = T.n, the number of moduli; NP = T.L.np = crt_digits(NMOD), the
+// number of digits of the largest M / m_i.
+template <int NMOD>
 __device__ __forceinline__ void crt_limbs_quad(const uint32_t (&w)[2][kCrtMaxModuli], const CrtTable& T,
                                                uint64_t (&lo)[4], uint64_t (&hi)[4]) {
+  constexpr int NP = crt_digits(NMOD);
   const float2 kRound = make_float2(12582912.0f, 12582912.0f), kUnround = make_float2(-12582912.0f, -12582912.0f);
   const float2 kDigit = make_float2(0x1p-13f, 0x1p-13f), kNegBase = make_float2(-8192.0f, -8192.0f);
   float2 S[2][NP];
@@ -295,8 +305,8 @@ __device__ __forceinline__ void crt_limbs_quad(const uint32_t (&w)[2][kCrtMaxMod
     for (int j = 0; j < NP; ++j) S[p][j] = make_float2(0.0f, 0.0f);
   const float2 unbias = T.L.unbias;
 #pragma unroll
-  for (int i = 0; i < kCrtMaxModuli; ++i) {
-    if (i < T.n) {
+  for (int i = 0; i < NMOD; ++i) {
+    {
       float2 t[2];
 #pragma unroll
       for (int p = 0; p < 2; ++p) {

@@ -244,7 +244,7 @@ constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one war
 // Modular scheme: C += the CRT of the residues. One warp per unit of one row
 // and 128 columns, units numbered across the problems (no idle blocks for
 // narrow problems), four columns per thread.
-template <int NP>
+template <int NMOD>
 __global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict__ P, int count, int total_units,
                                                     const __grid_constant__ ModTable T) {
   const int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict
   const int64_t row = w / chunks;
   const int64_t c0 = (int64_t)(w % chunks) * kCrtUnitCols + (threadIdx.x & 31) * kCrtCols;
   if (c0 >= p.n) return;
-  crt_cols<NP>(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
+  crt_cols<NMOD>(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
            static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - p.ba[row],
            p.eb + c0, p.bb + c0, p.C + row * p.ldc + c0);
 }
@@ -434,8 +434,9 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   else
     rc = pl->bn == 128 ? launch_grouped_gemm<128, kOzaki>(pl, stream) : launch_grouped_gemm<256, kOzaki>(pl, stream);
   if (rc == PHPC_OK && modular) {
-    with_crt_digits(pl->mods.crt.L.np, [&](auto np) {
-      g_crt_kernel<decltype(np)::value><<<ceil_div(pl->total_crt_units, 4), 128, 0, stream>>>(
+    if (pl->mods.crt.L.np != crt_digits(pl->mods.n)) return PHPC_ERR_UNSUPPORTED;
+    with_crt_moduli(pl->mods.n, [&](auto nm) {
+      g_crt_kernel<decltype(nm)::value><<<ceil_div(pl->total_crt_units, 4), 128, 0, stream>>>(
           pl->d_split, pl->count, pl->total_crt_units, pl->mods);
     });
     if (cudaGetLastError() != cudaSuccess) rc = PHPC_ERR_CUDA;

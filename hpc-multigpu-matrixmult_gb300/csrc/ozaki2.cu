@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
 }
 
 // C[i][j] += C_int * 2^(ea[i] - ba[i] + eb[j] - bb[j]), C_int recovered from the residues.
-template <int NP>
+template <int NMOD>
 __global__ void __launch_bounds__(128) crt_kernel(const uint16_t* __restrict__ R, int64_t ldr, int64_t rplane, int M,
                                                   int N, const int* __restrict__ ea, const int* __restrict__ ba,
                                                   const int* __restrict__ eb, const int* __restrict__ bb,
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(128) crt_kernel(const uint16_t* __restrict__ R
   const int64_t row = blockIdx.x;
   const int64_t c0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * kCrtCols;
   if (row >= M || c0 >= N) return;
-  crt_cols<NP>(R + row * ldr + c0, rplane, T.crt, T.crt.fast, static_cast<int>(min(static_cast<int64_t>(kCrtCols), N - c0)),
+  crt_cols<NMOD>(R + row * ldr + c0, rplane, T.crt, T.crt.fast, static_cast<int>(min(static_cast<int64_t>(kCrtCols), N - c0)),
            max(ea[row], -20000) - ba[row], eb + c0, bb + c0, C + row * ldc + c0);
 }
 
@@ -318,8 +318,9 @@ int ozaki2_reconstruct_rows(int m, int r0, int rows, int k, int n, double* dC, i
   if (rc != PHPC_OK) return rc;
   if (r0 < 0 || rows <= 0 || r0 + rows > m) return PHPC_ERR_ARG;
   const ModTable T = make_table(nmod, k);
-  with_crt_digits(T.crt.L.np, [&](auto np) {
-    crt_kernel<decltype(np)::value><<<dim3(rows, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(
+  if (T.crt.L.np != crt_digits(T.n)) return PHPC_ERR_UNSUPPORTED;  // the kernels' digit count per modulus count
+  with_crt_moduli(T.n, [&](auto nm) {
+    crt_kernel<decltype(nm)::value><<<dim3(rows, ceil_div(n, 128 * kCrtCols)), 128, 0, stream>>>(
         V.R + (int64_t)r0 * L.ldr, L.ldr, (int64_t)m * L.ldr, rows, n, V.ea + r0, V.ba + r0, V.eb, V.bb, T,
         dC + (int64_t)r0 * ldc, ldc);
   });

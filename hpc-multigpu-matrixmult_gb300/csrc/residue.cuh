@@ -343,17 +343,20 @@ constexpr int kColBlockK = 64, kColBlockJ = 32;
 
 constexpr int kCrtCols = 4;  // consecutive columns per thread (one 8-byte load per residue plane)
 
-// Calls f(std::integral_constant<int, np>()) for the CRT's digit count np
-// (5 .. 10: the kernels are instantiated per count).
+// Calls f(std::integral_constant<int, n>()) for the number of moduli n
+// (kMinModuli .. kMaxModuli: the CRT kernels are instantiated per count, so
+// that their loops over the moduli have no inactive iterations).
 template <class F>
-inline void with_crt_digits(int np, F&& f) {
-  switch (np) {
-    case 5: f(std::integral_constant<int, 5>()); break;
-    case 6: f(std::integral_constant<int, 6>()); break;
-    case 7: f(std::integral_constant<int, 7>()); break;
+inline void with_crt_moduli(int n, F&& f) {
+  switch (n) {
     case 8: f(std::integral_constant<int, 8>()); break;
     case 9: f(std::integral_constant<int, 9>()); break;
-    default: f(std::integral_constant<int, 10>()); break;
+    case 10: f(std::integral_constant<int, 10>()); break;
+    case 11: f(std::integral_constant<int, 11>()); break;
+    case 12: f(std::integral_constant<int, 12>()); break;
+    case 13: f(std::integral_constant<int, 13>()); break;
+    case 14: f(std::integral_constant<int, 14>()); break;
+    default: f(std::integral_constant<int, 15>()); break;
   }
 }
 
@@ -362,17 +365,17 @@ inline void with_crt_digits(int np, F&& f) {
 // row padded to 16), scaled by 2^(row_shift + eb[c] - bb[c]) (row_shift: the
 // row's exponent less its grid width). Columns at or beyond ncols are left
 // alone.
-// NP = T.L.np (the kernels are instantiated per digit count); with fast set
-// the four elements are reconstructed on FP32 limbs (crt_limbs_quad), else by
-// the 32-bit-limb integer path (crt_value).
-template <int NP>
+// NMOD = T.n (the kernels are instantiated per modulus count); with fast
+// set the four elements are reconstructed on FP32 limbs (crt_limbs_quad),
+// else by the 32-bit-limb integer path (crt_value).
+template <int NMOD>
 __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_t rplane, const CrtTable& T, int fast,
                                          int ncols, int row_shift, const int* __restrict__ ebp,
                                          const int* __restrict__ bbp, double* cp) {
   uint2 rw[kCrtMaxModuli];
 #pragma unroll
   for (int i = 0; i < kCrtMaxModuli; ++i)
-    rw[i] = i < T.n ? *reinterpret_cast<const uint2*>(rp + i * rplane) : make_uint2(0u, 0u);
+    rw[i] = i < NMOD ? *reinterpret_cast<const uint2*>(rp + i * rplane) : make_uint2(0u, 0u);
   if (fast) {
     uint32_t w[2][kCrtMaxModuli];
 #pragma unroll
@@ -381,7 +384,7 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
       w[1][i] = rw[i].y;
     }
     uint64_t lo[kCrtCols], hi[kCrtCols];
-    crt_limbs_quad<NP>(w, T, lo, hi);
+    crt_limbs_quad<NMOD>(w, T, lo, hi);
     if (ncols == kCrtCols) {
       double cv[kCrtCols];
 #pragma unroll
@@ -408,7 +411,7 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
 #pragma unroll
       for (int i = 0; i < kCrtMaxModuli; ++i) r[i] = ((c < 2 ? rw[i].x : rw[i].y) >> (16 * (c & 1))) & 0xFFFFu;
       int shift;
-      const double v = crt_value(r, T, fast, shift);
+      const double v = crt_value<NMOD>(r, T, fast, shift);
       cv[c] = crt_added(cv[c], v, shift + row_shift + max(ebp[c], -20000) - bbp[c]);
     }
 #pragma unroll
@@ -422,7 +425,7 @@ __device__ __forceinline__ void crt_cols(const uint16_t* __restrict__ rp, int64_
 #pragma unroll
     for (int i = 0; i < kCrtMaxModuli; ++i) r[i] = ((c < 2 ? rw[i].x : rw[i].y) >> (16 * (c & 1))) & 0xFFFFu;
     int shift;
-    const double v = crt_value(r, T, fast, shift);
+    const double v = crt_value<NMOD>(r, T, fast, shift);
     crt_apply(cp + c, v, shift + row_shift + max(ebp[c], -20000) - bbp[c]);
   }
 }

@@ -59,3 +59,16 @@ def test_gemm_epilogue_t_on_chunk_sums(q):
         for x in xs:
             t = CL.gemm_t(x, m, T.inv[i])
             assert abs(t) <= 181 and (t - x * T.inv[i]) % m == 0
+
+
+def test_kernel_digit_table_matches_the_moduli():
+    """The CRT kernels are instantiated per modulus count with the digit count
+    of crt.cuh's crt_digits table; it must equal the count the moduli give
+    (the host also refuses a mismatch before launching)."""
+    import re
+    from pathlib import Path
+
+    src = (Path(__file__).resolve().parent.parent / "hpc-multigpu-matrixmult_gb300" / "csrc" / "crt.cuh").read_text()
+    table = [int(x) for x in re.search(r"kDigits\[kCrtMaxModuli \+ 1\] = \{([^}]*)\}", src).group(1).split(",")]
+    for q in range(8, 16):
+        assert table[q] == CL.Table(q).NP, q

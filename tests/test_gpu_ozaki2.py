@@ -59,7 +59,7 @@ def run_dev(phpc, torch, a, b, c0, nmod):
     return run_dev_grid(phpc, torch, a, b, c0, nmod)[0]
 
 
-@pytest.mark.parametrize("nmod", [8, 12, 14, 15])
+@pytest.mark.parametrize("nmod", [8, 9, 10, 11, 12, 13, 14, 15])
 @pytest.mark.parametrize("m,k,n", [(128, 64, 256), (70, 300, 130), (7, 13, 5), (200, 1100, 96), (40, 2048, 72)])
 def test_bitexact_vs_model(phpc, torch_cuda, nmod, m, k, n):
     rng = np.random.default_rng(nmod * 1009 + m + k + n)
