@@ -214,18 +214,21 @@ __global__ void __launch_bounds__(256) g_split_cols_kernel(const GSplitProb* __r
 }
 
 // Modular scheme: residue planes of one row piece per thread. (Both residue
-// splits are held to 64 registers, four CTAs per SM: a few bytes of spill,
-// 4 % faster than at 79 registers and three CTAs.)
+// splits are held to 64 registers, four CTAs per SM: 4 % faster than at 79
+// registers and three CTAs; instantiated per modulus count, they fit without
+// spills.)
+template <int NMOD>
 __global__ void __launch_bounds__(256, 4) g_residue_rows_kernel(const GSplitProb* __restrict__ P, int count,
                                                              int total_pieces, const __grid_constant__ ModTable T) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total_pieces) return;
   const RowPiece rp = row_piece(P, count, t);
   const GSplitProb& p = *rp.p;
-  residue_row_piece(p.A + rp.row * p.lda, p.k, p.ea[rp.row], p.ba[rp.row], T, p.pa + rp.row * p.ldp,
+  residue_row_piece<NMOD>(p.A + rp.row * p.lda, p.k, p.ea[rp.row], p.ba[rp.row], T, p.pa + rp.row * p.ldp,
                     (int64_t)p.m * p.ldp, rp.k0);
 }
 
+template <int NMOD>
 __global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
                                                              int total_blocks, const __grid_constant__ ModTable T) {
   const int b = blockIdx.x;
@@ -236,7 +239,8 @@ __global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb
   const int64_t col = (int64_t)(lb % nblk_j) * kColBlockJ + (threadIdx.x >> 3);
   const int64_t k0 = (int64_t)(lb / nblk_j) * kColBlockK + (threadIdx.x & 7) * 8;
   if (col >= p.n || k0 >= p.ldp) return;
-  residue_col_piece(p.B, p.ldb, p.k, col, p.eb[col], p.bb[col], T, p.pb + col * p.ldp, (int64_t)p.n * p.ldp, k0);
+  residue_col_piece<NMOD>(p.B, p.ldb, p.k, col, p.eb[col], p.bb[col], T, p.pb + col * p.ldp, (int64_t)p.n * p.ldp,
+                          k0);
 }
 
 constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one warp)
@@ -407,10 +411,12 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
                                                                                  pl->total_cunits, status);
       g_scan_cols_merge_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, side>>>(pl->d_split, pl->count,
                                                                                 pl->total_cols, pl->mods);
-      g_residue_rows_kernel<<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(pl->d_split, pl->count,
-                                                                                 pl->total_pieces, pl->mods);
-      g_residue_cols_kernel<<<pl->total_rblocks, 256, 0, side>>>(pl->d_split, pl->count, pl->total_rblocks,
-                                                                 pl->mods);
+      with_crt_moduli(pl->mods.n, [&](auto nm) {
+        g_residue_rows_kernel<decltype(nm)::value><<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(
+            pl->d_split, pl->count, pl->total_pieces, pl->mods);
+        g_residue_cols_kernel<decltype(nm)::value><<<pl->total_rblocks, 256, 0, side>>>(
+            pl->d_split, pl->count, pl->total_rblocks, pl->mods);
+      });
       if (cudaGetLastError() != cudaSuccess || (side != stream && !stream_fork(side, stream))) return PHPC_ERR_CUDA;
     } else {
       g_scan_rows_kernel<<<ceil_div(pl->total_rows, 8), 256, 0, stream>>>(pl->d_split, pl->count, pl->total_rows,

@@ -92,6 +92,7 @@ __global__ void scan_cols_merge_kernel(int K, int N, int64_t ldpart, const int* 
 }
 
 // A residue planes [n][M][ldp]: blockIdx.x = row, each thread 8 consecutive k.
+template <int NMOD>
 __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, int M, int K,
                                     const int* __restrict__ ea, const int* __restrict__ ba,
                                     const __grid_constant__ ModTable T, uint16_t* __restrict__ planes, int64_t ldp,
@@ -99,11 +100,12 @@ __global__ void residue_rows_kernel(const double* __restrict__ A, int64_t lda, i
   const int64_t row = blockIdx.x;
   const int64_t k0 = ((int64_t)blockIdx.y * blockDim.x + threadIdx.x) * 8;
   if (row >= M || k0 >= ldp) return;
-  residue_row_piece(A + row * lda, K, ea[row], ba[row], T, planes + row * ldp, plane_stride, k0);
+  residue_row_piece<NMOD>(A + row * lda, K, ea[row], ba[row], T, planes + row * ldp, plane_stride, k0);
 }
 
 // B residue planes, transposed ([n][N][ldp]): one kColBlockK x kColBlockJ
 // block per 256-thread CTA (residue.cuh).
+template <int NMOD>
 __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restrict__ B, int64_t ldb, int K, int N,
                                                            const int* __restrict__ eb, const int* __restrict__ bb,
                                                            const __grid_constant__ ModTable T,
@@ -112,7 +114,7 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
   const int64_t col = (int64_t)blockIdx.x * kColBlockJ + (threadIdx.x >> 3);
   const int64_t k0 = (int64_t)blockIdx.y * kColBlockK + (threadIdx.x & 7) * 8;
   if (col >= N || k0 >= ldp) return;
-  residue_col_piece(B, ldb, K, col, eb[col], bb[col], T, planes + col * ldp, plane_stride, k0);
+  residue_col_piece<NMOD>(B, ldb, K, col, eb[col], bb[col], T, planes + col * ldp, plane_stride, k0);
 }
 
 // C[i][j] += C_int * 2^(ea[i] - ba[i] + eb[j] - bb[j]), C_int recovered from the residues.
@@ -207,8 +209,10 @@ int ozaki2_prepare_a_rows(int m, int r0, int rows, int k, int n, const double* d
   const double* a = dA + (int64_t)r0 * lda;
   scan_rows_grid_kernel<<<ceil_div(rows, 8), 256, 0, stream>>>(a, lda, rows, k, V.ea + r0, V.ba + r0, T.logT,
                                                                device_status_ptr());
-  residue_rows_kernel<<<dim3(rows, ceil_div(L.ldp / 8, 128)), 128, 0, stream>>>(
-      a, lda, rows, k, V.ea + r0, V.ba + r0, T, V.pa + (int64_t)r0 * L.ldp, L.ldp, (int64_t)m * L.ldp);
+  with_crt_moduli(T.n, [&](auto nm) {
+    residue_rows_kernel<decltype(nm)::value><<<dim3(rows, ceil_div(L.ldp / 8, 128)), 128, 0, stream>>>(
+        a, lda, rows, k, V.ea + r0, V.ba + r0, T, V.pa + (int64_t)r0 * L.ldp, L.ldp, (int64_t)m * L.ldp);
+  });
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
 }
@@ -230,8 +234,11 @@ int ozaki2_prepare_b_cols(int m, int k, int n, int c0, int cols, const double* d
       b, ldb, k, cols, L.ldpart, V.pe + c0, V.ps + c0, device_status_ptr());
   scan_cols_merge_kernel<<<ceil_div(cols, 256), 256, 0, stream>>>(k, cols, L.ldpart, V.pe + c0, V.ps + c0, eb, bb,
                                                                  T.logT);
-  residue_cols_kernel<<<dim3(ceil_div(cols, kColBlockJ), ceil_div(L.ldp, kColBlockK)), 256, 0, stream>>>(
-      b, ldb, k, cols, eb, bb, T, V.pb + (int64_t)c0 * L.ldp, L.ldp, (int64_t)n * L.ldp);
+  with_crt_moduli(T.n, [&](auto nm) {
+    residue_cols_kernel<decltype(nm)::value>
+        <<<dim3(ceil_div(cols, kColBlockJ), ceil_div(L.ldp, kColBlockK)), 256, 0, stream>>>(
+            b, ldb, k, cols, eb, bb, T, V.pb + (int64_t)c0 * L.ldp, L.ldp, (int64_t)n * L.ldp);
+  });
   PHPC_CUDA_TRY(cudaGetLastError());
   return PHPC_OK;
 }

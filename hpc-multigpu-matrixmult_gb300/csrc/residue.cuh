@@ -294,10 +294,14 @@ __device__ __forceinline__ void limb_pairs(const double (&v)[8], int e, int bits
 }
 
 // Residue planes of 8 consecutive values (limb pairs P): plane i gets one
-// 16-byte vector at out + i * plane_stride.
+// 16-byte vector at out + i * plane_stride. NMOD = T.n (the split kernels
+// are instantiated per modulus count, so the loop is unrolled with constant
+// indices into the table).
+template <int NMOD>
 __device__ __forceinline__ void store_residues8(const float2 (&P)[4][kLimbs], const ModTable& T,
                                                 uint16_t* __restrict__ out, int64_t plane_stride) {
-  for (int i = 0; i < T.n; ++i) {
+#pragma unroll
+  for (int i = 0; i < NMOD; ++i) {
     uint32_t w[4];
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
@@ -310,6 +314,7 @@ __device__ __forceinline__ void store_residues8(const float2 (&P)[4][kLimbs], co
 
 // Residue planes of row piece [k0, k0 + 8) of one operand row a (K long,
 // grid exponent e, grid width bits): plane i at out + i * plane_stride.
+template <int NMOD>
 __device__ __forceinline__ void residue_row_piece(const double* __restrict__ a, int K, int e, int bits,
                                                   const ModTable& T, uint16_t* __restrict__ out,
                                                   int64_t plane_stride, int64_t k0) {
@@ -318,12 +323,13 @@ __device__ __forceinline__ void residue_row_piece(const double* __restrict__ a, 
   for (int j = 0; j < 8; ++j) v[j] = k0 + j < K ? a[k0 + j] : 0.0;
   float2 P[4][kLimbs];
   limb_pairs(v, e, bits, P);
-  store_residues8(P, T, out + k0, plane_stride);
+  store_residues8<NMOD>(P, T, out + k0, plane_stride);
 }
 
 // Residue planes of column piece [k0, k0 + 8) of column col of B (K x N, row
 // stride ldb, column exponent e), written transposed: plane i holds the
 // column as a row of [N][ldp] (out = row col of plane 0).
+template <int NMOD>
 __device__ __forceinline__ void residue_col_piece(const double* __restrict__ B, int64_t ldb, int K, int64_t col, int e,
                                                   int bits, const ModTable& T, uint16_t* __restrict__ out,
                                                   int64_t plane_stride, int64_t k0) {
@@ -332,7 +338,7 @@ __device__ __forceinline__ void residue_col_piece(const double* __restrict__ B, 
   for (int u = 0; u < 8; ++u) v[u] = k0 + u < K ? B[(k0 + u) * ldb + col] : 0.0;
   float2 P[4][kLimbs];
   limb_pairs(v, e, bits, P);
-  store_residues8(P, T, out + k0, plane_stride);
+  store_residues8<NMOD>(P, T, out + k0, plane_stride);
 }
 
 // Column blocks of the transposed split: 64 rows of B (k) x 32 columns (j)
