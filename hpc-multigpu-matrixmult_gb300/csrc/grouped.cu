@@ -236,11 +236,9 @@ __global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb
   const GSplitProb& p = P[locate(P, count, b, [](const GSplitProb& q) { return q.rblock_start; })];
   const int lb = b - p.rblock_start;
   const int nblk_j = (p.n + kColBlockJ - 1) / kColBlockJ;
-  const int64_t col = (int64_t)(lb % nblk_j) * kColBlockJ + (threadIdx.x >> 3);
-  const int64_t k0 = (int64_t)(lb / nblk_j) * kColBlockK + (threadIdx.x & 7) * 8;
-  if (col >= p.n || k0 >= p.ldp) return;
-  residue_col_piece<NMOD>(p.B, p.ldb, p.k, col, p.eb[col], p.bb[col], T, p.pb + col * p.ldp, (int64_t)p.n * p.ldp,
-                          k0);
+  __shared__ double tile[kColBlockK][kColBlockJ];
+  residue_col_block<NMOD>(p.B, p.ldb, p.k, p.n, (int64_t)(lb % nblk_j) * kColBlockJ, (int64_t)(lb / nblk_j) * kColBlockK,
+                          p.eb, p.bb, T, p.pb, p.ldp, (int64_t)p.n * p.ldp, tile);
 }
 
 constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one warp)

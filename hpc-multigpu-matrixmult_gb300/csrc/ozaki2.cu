@@ -111,10 +111,9 @@ __global__ void __launch_bounds__(256) residue_cols_kernel(const double* __restr
                                                            const __grid_constant__ ModTable T,
                                                            uint16_t* __restrict__ planes, int64_t ldp,
                                                            int64_t plane_stride) {
-  const int64_t col = (int64_t)blockIdx.x * kColBlockJ + (threadIdx.x >> 3);
-  const int64_t k0 = (int64_t)blockIdx.y * kColBlockK + (threadIdx.x & 7) * 8;
-  if (col >= N || k0 >= ldp) return;
-  residue_col_piece<NMOD>(B, ldb, K, col, eb[col], bb[col], T, planes + col * ldp, plane_stride, k0);
+  __shared__ double tile[kColBlockK][kColBlockJ];
+  residue_col_block<NMOD>(B, ldb, K, N, (int64_t)blockIdx.x * kColBlockJ, (int64_t)blockIdx.y * kColBlockK, eb, bb,
+                          T, planes, ldp, plane_stride, tile);
 }
 
 // C[i][j] += C_int * 2^(ea[i] - ba[i] + eb[j] - bb[j]), C_int recovered from the residues.

@@ -326,19 +326,38 @@ __device__ __forceinline__ void residue_row_piece(const double* __restrict__ a, 
   store_residues8<NMOD>(P, T, out + k0, plane_stride);
 }
 
-// Residue planes of column piece [k0, k0 + 8) of column col of B (K x N, row
-// stride ldb, column exponent e), written transposed: plane i holds the
-// column as a row of [N][ldp] (out = row col of plane 0).
+// The column block [k0, k0 + 64) x [j0, j0 + 32) of B (K x N, row stride
+// ldb) split into transposed residue planes by a 256-thread CTA (the caller
+// has checked that the block starts inside B). The block is staged in
+// shared memory (tile, 64 x 32 doubles): warp w reads rows w, w + 8, ... as
+// whole 256-byte row segments; then thread t takes column j0 + t / 8 and
+// rows 8 (t % 8) .. + 7, so that the 8 threads of one column write one
+// contiguous 128-byte run of each plane row. Element (k, j) sits at
+// tile[k][j ^ 4 ((k / 8) % 4)], which keeps both the row writes and the
+// column reads at two shared-memory wavefronts per warp access.
 template <int NMOD>
-__device__ __forceinline__ void residue_col_piece(const double* __restrict__ B, int64_t ldb, int K, int64_t col, int e,
-                                                  int bits, const ModTable& T, uint16_t* __restrict__ out,
-                                                  int64_t plane_stride, int64_t k0) {
+__device__ __forceinline__ void residue_col_block(const double* __restrict__ B, int64_t ldb, int K, int N,
+                                                  int64_t j0, int64_t k0, const int* __restrict__ eb,
+                                                  const int* __restrict__ bb, const ModTable& T,
+                                                  uint16_t* __restrict__ planes, int64_t ldp, int64_t plane_stride,
+                                                  double (&tile)[64][32]) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int64_t jl = j0 + l;
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int k = w + 8 * u;
+    tile[k][l ^ (4 * (u & 3))] = (k0 + k < K && jl < N) ? B[(k0 + k) * ldb + jl] : 0.0;
+  }
+  __syncthreads();
+  const int jj = threadIdx.x >> 3, p = threadIdx.x & 7;
+  const int64_t col = j0 + jj, kp = k0 + 8 * p;
+  if (col >= N || kp >= ldp) return;
   double v[8];
 #pragma unroll
-  for (int u = 0; u < 8; ++u) v[u] = k0 + u < K ? B[(k0 + u) * ldb + col] : 0.0;
+  for (int u = 0; u < 8; ++u) v[u] = tile[8 * p + u][jj ^ (4 * (p & 3))];
   float2 P[4][kLimbs];
-  limb_pairs(v, e, bits, P);
-  store_residues8<NMOD>(P, T, out + k0, plane_stride);
+  limb_pairs(v, eb[col], bb[col], P);
+  store_residues8<NMOD>(P, T, planes + col * ldp + kp, plane_stride);
 }
 
 // Column blocks of the transposed split: 64 rows of B (k) x 32 columns (j)
