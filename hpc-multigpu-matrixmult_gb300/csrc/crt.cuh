@@ -21,8 +21,10 @@ __host__ __device__ constexpr int crt_digits(int n) {
 
 // What the residue GEMMs store per element and modulus (a 16-bit value): not
 // the residue r_i of the product but t_i = r_i ((M / m_i)^-1 mod m_i) mod m_i,
-// symmetric (|t_i| <= 181), plus kCrtTBias. Then sum_i t_i (M / m_i) = y
-// (mod M), so the reconstruction needs no per-modulus multiplication.
+// symmetric (|t_i| <= 182), plus kCrtTBias. (A's residue planes carry the
+// factor (M / m_i)^-1 mod m_i, so the GEMM's sums are t_i mod m_i.) Then
+// sum_i t_i (M / m_i) = y (mod M), so the reconstruction needs no
+// per-modulus multiplication.
 constexpr int kCrtTBias = 256;
 
 // Constants of the reconstruction on FP32 limbs (crt_limbs_quad), each value
@@ -281,7 +283,7 @@ __device__ __forceinline__ double crt_add_i128(double c, uint64_t lo, uint64_t h
 //     exponent of 2^23), less 2^23 + kCrtTBias: one exact add;
 //     sum_i t_i (M / m_i) = y (mod M);
 //  2. S_j = sum_i t_i P_ij over the balanced 13-bit digits P_ij of M / m_i
-//     (|P_ij| <= 2^12, |S_j| <= 15 181 2^12 < 2^24);
+//     (|P_ij| <= 2^12, |S_j| <= 15 182 2^12 < 2^24);
 //  3. q = round(sum_i t_i / m_i) from the top three limb sums,
 //     est = sum_j S_j fl(2^(13 j) / M) (|est| <= 7.5, error below 2^-19; the
 //     lower limbs weigh below 2^-27); exact under the fast path's margin;

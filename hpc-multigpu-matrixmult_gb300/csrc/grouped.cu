@@ -338,7 +338,6 @@ PairList residue_pairs(const ModTable& T) {
     pl.a[i] = pl.b[i] = pl.g[i] = static_cast<uint8_t>(i);
     pl.mod[i] = static_cast<uint16_t>(T.m[i]);
     pl.invm[i] = T.invm[i].x;
-    pl.winv[i] = T.winv[i];
   }
   return pl;
 }

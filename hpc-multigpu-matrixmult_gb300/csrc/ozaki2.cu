@@ -287,7 +287,6 @@ int ozaki2_multiply_block(int m, int r0, int rows, int c0, int cols, int k, int 
     pl.g[i] = static_cast<uint8_t>(i);
     pl.mod[i] = static_cast<uint16_t>(T.m[i]);
     pl.invm[i] = T.invm[i].x;
-    pl.winv[i] = T.winv[i];
   }
   const int64_t rplane = (int64_t)m * L.ldr;
   const uint16_t* pa = V.pa + (int64_t)r0 * L.ldp;

@@ -33,9 +33,11 @@ struct ModTable {
   uint32_t m[kMaxModuli];
   // Per modulus, each value twice (both lanes of a packed f32x2 FMA):
   float2 cf[kMaxModuli][4];  // symmetric residues of 2^13, 2^26, 2^39, 2^52 mod m (|c| <= 181)
+  float2 cfa[kMaxModuli][5];  // A operand: symmetric residues of winv 2^(13 j) mod m, j = 0..4 (|c| <= 181)
   float2 invm[kMaxModuli];   // 1 / m rounded to float
   float2 negm[kMaxModuli];   // -m
-  float winv[kMaxModuli];    // (M / m)^-1 mod m: the residue GEMM stores t = r winv mod m (crt.cuh)
+  float winv[kMaxModuli];    // (M / m)^-1 mod m: A's residues are scaled by it, so that the residue
+                             // GEMM's sums are t = r winv mod m (crt.cuh)
   CrtTable crt;                // the reconstruction's constants
 };
 
@@ -89,6 +91,11 @@ inline ModTable make_table(int nmod, int k) {
     for (uint32_t v = 1; v < m; ++v)
       if ((static_cast<uint64_t>(mi_mod) * v) % m == 1) { inv = v; break; }
     T.winv[i] = static_cast<float>(inv);
+    for (int j = 0; j < 5; ++j) {
+      const int64_t c = static_cast<int64_t>((static_cast<unsigned __int128>(inv) << (13 * j)) % m);
+      const float cs = static_cast<float>(2 * c > static_cast<int64_t>(m) ? c - m : c);
+      T.cfa[i][j] = make_float2(cs, cs);
+    }
     T.crt.m[i] = m;
     for (int l = 0; l < 4; ++l) T.crt.W[i][l] = static_cast<uint32_t>(Mi >> (32 * l));
   }
@@ -269,13 +276,28 @@ __device__ __forceinline__ uint32_t bf16x2_of_float_ints(float lo, float hi) {
 // through the 1.5 * 2^23 rounding constant is round(t / m) except within
 // 0.001 of a tie, so r = t - q m (one exact FMA) has |r| <= 0.501 m, i.e.
 // |r| <= 181 for m <= 363.
+// With SCALED (the A operand) every limb is weighted by winv 2^(13 j) mod m
+// instead (|t| <= 5 2^12 181 < 2^22, |r| <= 0.5008 m, still |r| <= 181): the
+// residue of the operand times winv = (M / m)^-1 mod m, so that the residue
+// GEMM's sums are the t_i the CRT combines (crt.cuh) without a further
+// multiplication.
+template <bool SCALED>
 __device__ __forceinline__ float2 residue_pair(const float2 (&L)[kLimbs], const ModTable& T, int i) {
   const float2 kRound = make_float2(12582912.0f, 12582912.0f);
   const float2 kUnround = make_float2(-12582912.0f, -12582912.0f);
-  float2 t = __ffma2_rn(L[1], T.cf[i][0], L[0]);
-  t = __ffma2_rn(L[2], T.cf[i][1], t);
-  t = __ffma2_rn(L[3], T.cf[i][2], t);
-  t = __ffma2_rn(L[4], T.cf[i][3], t);
+  float2 t;
+  if (SCALED) {
+    t = __fmul2_rn(L[0], T.cfa[i][0]);
+    t = __ffma2_rn(L[1], T.cfa[i][1], t);
+    t = __ffma2_rn(L[2], T.cfa[i][2], t);
+    t = __ffma2_rn(L[3], T.cfa[i][3], t);
+    t = __ffma2_rn(L[4], T.cfa[i][4], t);
+  } else {
+    t = __ffma2_rn(L[1], T.cf[i][0], L[0]);
+    t = __ffma2_rn(L[2], T.cf[i][1], t);
+    t = __ffma2_rn(L[3], T.cf[i][2], t);
+    t = __ffma2_rn(L[4], T.cf[i][3], t);
+  }
   const float2 q = __fadd2_rn(__ffma2_rn(t, T.invm[i], kRound), kUnround);
   return __ffma2_rn(q, T.negm[i], t);
 }
@@ -296,8 +318,8 @@ __device__ __forceinline__ void limb_pairs(const double (&v)[8], int e, int bits
 // Residue planes of 8 consecutive values (limb pairs P): plane i gets one
 // 16-byte vector at out + i * plane_stride. NMOD = T.n (the split kernels
 // are instantiated per modulus count, so the loop is unrolled with constant
-// indices into the table).
-template <int NMOD>
+// indices into the table); SCALED for the A operand (residue_pair).
+template <int NMOD, bool SCALED>
 __device__ __forceinline__ void store_residues8(const float2 (&P)[4][kLimbs], const ModTable& T,
                                                 uint16_t* __restrict__ out, int64_t plane_stride) {
 #pragma unroll
@@ -305,7 +327,7 @@ __device__ __forceinline__ void store_residues8(const float2 (&P)[4][kLimbs], co
     uint32_t w[4];
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
-      const float2 r = residue_pair(P[p], T, i);
+      const float2 r = residue_pair<SCALED>(P[p], T, i);
       w[p] = bf16x2_of_float_ints(r.x, r.y);
     }
     *reinterpret_cast<uint4*>(out + i * plane_stride) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -323,7 +345,7 @@ __device__ __forceinline__ void residue_row_piece(const double* __restrict__ a, 
   for (int j = 0; j < 8; ++j) v[j] = k0 + j < K ? a[k0 + j] : 0.0;
   float2 P[4][kLimbs];
   limb_pairs(v, e, bits, P);
-  store_residues8<NMOD>(P, T, out + k0, plane_stride);
+  store_residues8<NMOD, true>(P, T, out + k0, plane_stride);
 }
 
 // The column block [k0, k0 + 64) x [j0, j0 + 32) of B (K x N, row stride
@@ -357,7 +379,7 @@ __device__ __forceinline__ void residue_col_block(const double* __restrict__ B, 
   for (int u = 0; u < 8; ++u) v[u] = tile[8 * p + u][jj ^ (4 * (p & 3))];
   float2 P[4][kLimbs];
   limb_pairs(v, eb[col], bb[col], P);
-  store_residues8<NMOD>(P, T, planes + col * ldp + kp, plane_stride);
+  store_residues8<NMOD, false>(P, T, planes + col * ldp + kp, plane_stride);
 }
 
 // Column blocks of the transposed split: 64 rows of B (k) x 32 columns (j)

@@ -71,7 +71,6 @@ struct PairList {
   uint8_t g[kTcMaxPairs];     // group id (Ozaki: diagonal p + q, 1-based digits); pairs of a group are contiguous
   uint16_t mod[kTcMaxPairs];  // kResidue: modulus of the group
   float invm[kTcMaxPairs];      // kResidue: 1 / modulus rounded to float
-  float winv[kTcMaxPairs];      // kResidue: (M / modulus)^-1 mod modulus (the stored value is r winv mod m)
 };
 
 // x - m round(x / m) for two integer-valued floats |x| < 2^24, m <= 363: the
@@ -84,15 +83,13 @@ __device__ __forceinline__ float2 reduce_pair_f32(float2 x, float m, float invm)
   return __ffma2_rn(q, make_float2(-m, -m), x);
 }
 
-// What the residue GEMM stores for two integer-valued floats |x| < 2^24 (the
-// products' sums mod m): t = (x mod m) winv mod m, symmetric, plus
-// kCrtTBias (crt.cuh), as two 16-bit values (lo in the low half) read from
-// the mantissas of 2^23 + kCrtTBias + t. |x mod m| <= 0.51 m after the
-// first reduction, so (x mod m) winv < 2^17 is exact, and the second
-// reduction leaves |t| <= 181.
-__device__ __forceinline__ uint32_t crt_t_pair_u16(float x0, float x1, float m, float invm, float winv) {
-  const float2 r = reduce_pair_f32(make_float2(x0, x1), m, invm);
-  const float2 t = reduce_pair_f32(__fmul2_rn(r, make_float2(winv, winv)), m, invm);
+// What the residue GEMM stores for two integer-valued floats |x| < 2^24, the
+// products' sums (A's residues carry the factor (M / m)^-1 mod m, so x = t
+// mod m for the t the CRT combines): t = x mod m, symmetric (|t| <= 0.51 m,
+// at most 182), plus kCrtTBias (crt.cuh), as two 16-bit values (lo in the low
+// half) read from the mantissas of 2^23 + kCrtTBias + t.
+__device__ __forceinline__ uint32_t crt_t_pair_u16(float x0, float x1, float m, float invm) {
+  const float2 t = reduce_pair_f32(make_float2(x0, x1), m, invm);
   const float bias = 8388608.0f + static_cast<float>(kCrtTBias);
   const float2 b = __fadd2_rn(t, make_float2(bias, bias));
   return __byte_perm(__float_as_uint(b.x), __float_as_uint(b.y), 0x5410);
@@ -664,7 +661,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             // with one 16-byte load. (acc holds exact f32 integers: the chunk
             // itself, or the sum of the reduced chunks.)
             uint16_t* rplane = job.R + static_cast<int64_t>(pairs.g[gstart]) * job.rplane;
-            const float winv = pairs.winv[gstart];
             uint4* tq = reinterpret_cast<uint4*>(tr);  // [32 rows][8 chunks], 4 KB of the warp's scratch
 #pragma unroll
             for (int h = 0; h < HALF; h += 64) {
@@ -674,7 +670,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                 for (int e = 0; e < 4; ++e)
                   w[e] = crt_t_pair_u16(__int_as_float(acc[h + 8 * c + 2 * e]), __int_as_float(acc[h + 8 * c + 2 * e + 1]),
-                                        mf, invm, winv);
+                                        mf, invm);
                 tq[lane * 8 + (c ^ (lane & 7))] = make_uint4(w[0], w[1], w[2], w[3]);
               }
               __syncwarp();

@@ -7,15 +7,15 @@ symmetric representative of sum_i r_i W_i mod M.
 
 The reconstruction, for residues r_i in [0, m_i) of the q moduli:
 
-1. (GEMM epilogue) the product's sum x (|x| < 2^24, x = r_i mod m_i) is
-   reduced mod m_i in FP32: r = x - m_i round(x / m_i) with the quotient
-   through the 1.5 2^23 rounding constant and fl(1 / m_i), |r| <= 0.51 m_i;
-   then t_i = p - m_i round(p / m_i) for p = r inv_i (< 2^17, exact), inv_i =
-   (M / m_i)^-1 mod m_i; |t_i| <= 181. Stored as t_i + 256 in 16 bits, and
+1. (split and GEMM epilogue) A's residues are scaled by inv_i = (M / m_i)^-1
+   mod m_i in the split, so the residue GEMM's sum x (|x| < 2^24) is
+   r_i inv_i mod m_i; the epilogue reduces it in FP32: t_i = x - m_i round(x
+   / m_i) with the quotient through the 1.5 2^23 rounding constant and
+   fl(1 / m_i), |t_i| <= 0.51 m_i <= 182. Stored as t_i + 256 in 16 bits, and
    sum_i t_i (M / m_i) = sum_i r_i W_i (mod M) with W_i = (M / m_i) inv_i.
 2. (CRT) t_i read back as (2^23 + 256 + t_i) - (2^23 + 256), exact;
    S_j = sum_i t_i P_ij over the balanced 13-bit digits P_ij of
-   P_i = M / m_i (|P_ij| <= 2^12): |S_j| <= 15 * 181 * 2^12 < 2^24, so every
+   P_i = M / m_i (|P_ij| <= 2^12): |S_j| <= 15 * 182 * 2^12 < 2^24, so every
    partial sum is an integer FP32 holds exactly.
 3. est = S_(NP-1) c_(NP-1) + S_(NP-2) c_(NP-2) + S_(NP-3) c_(NP-3) in FP32,
    c_j = fl(2^(13 j) / M): the top three limb sums give acc / M (|acc / M| =
@@ -92,7 +92,7 @@ def reconstruct(T: Table, r: list[int], checks: dict | None = None) -> int:
     S = [f32(0)] * T.NP
     tmax = 0
     for i, m in enumerate(T.m):
-        stored = gemm_t(r[i], m, T.inv[i]) + 256  # the 16-bit value the residue GEMM writes
+        stored = gemm_t(r[i] * T.inv[i], m) + 256  # the 16-bit value the residue GEMM writes
         assert 0 <= stored < 1 << 16
         tb = (np.uint32(0x4B000000) | np.uint32(stored)).view(np.float32)
         t = f32(np.float32(tb) + np.float32(-(8388608.0 + 256.0)))
@@ -138,16 +138,13 @@ def reduce_f32(x, m: int) -> np.float32:
     return rem
 
 
-def gemm_t(x: int, m: int, inv: int) -> int:
-    """The residue GEMM epilogue's t for an exact product sum x (|x| < 2^24):
-    (x mod m) inv mod m, symmetric (crt_t_pair_u16)."""
+def gemm_t(x: int, m: int) -> int:
+    """The residue GEMM epilogue's stored t for an exact product sum x
+    (|x| < 2^24, which A's scaled residues make congruent to the t the CRT
+    combines): x mod m, symmetric (crt_t_pair_u16)."""
     assert abs(x) < 1 << 24
-    r = reduce_f32(x, m)
-    assert abs(float(r)) <= 0.51 * m
-    p = np.float32(r) * np.float32(inv)
-    assert float(p) == float(r) * inv and abs(float(p)) < 1 << 17
-    t = reduce_f32(p, m)
-    assert abs(float(t)) <= 181 and (int(t) - int(x) * inv) % m == 0
+    t = reduce_f32(x, m)
+    assert abs(float(t)) <= 0.51 * m and abs(float(t)) <= 182 and (int(t) - x) % m == 0
     return int(t)
 
 

@@ -49,16 +49,37 @@ def test_limb_crt_extreme_residues(q):
 @pytest.mark.parametrize("q", [8, 13, 15])
 def test_gemm_epilogue_t_on_chunk_sums(q):
     """The residue GEMM's stored value for product sums across the exact f32
-    range (|x| < 2^24, both signs, the range ends): t = (x mod m) inv mod m,
-    |t| <= 181, exact at every step (crt_limb_model.gemm_t asserts each)."""
+    range (|x| < 2^24, both signs, the range ends): t = x mod m, symmetric,
+    |t| <= 182, exact (crt_limb_model.gemm_t asserts each step)."""
     T = CL.Table(q)
     rng = np.random.default_rng(300 + q)
     xs = [0, 1, -1, (1 << 24) - 1, -((1 << 24) - 1), 512 * 181 * 181, -512 * 181 * 181]
     xs += [int(v) for v in rng.integers(-(1 << 24) + 1, 1 << 24, 3000)]
-    for i, m in enumerate(T.m):
+    for m in T.m:
         for x in xs:
-            t = CL.gemm_t(x, m, T.inv[i])
-            assert abs(t) <= 181 and (t - x * T.inv[i]) % m == 0
+            t = CL.gemm_t(x, m)
+            assert abs(t) <= 182 and (t - x) % m == 0
+
+
+@pytest.mark.parametrize("q", [8, 13, 15])
+def test_scaled_a_residues(q):
+    """A's residue planes carry the factor inv_i = (M / m_i)^-1 mod m_i: the
+    split's limb weights winv 2^(13 j) mod m (symmetric) keep every partial
+    sum below 2^22 and the residue within 181, and sum_j L_j c_j = X inv_i
+    (mod m_i) for the operand integer X = sum_j L_j 2^(13 j)."""
+    T = CL.Table(q)
+    rng = np.random.default_rng(500 + q)
+    for i, m in enumerate(T.m):
+        c = [((T.inv[i] << (13 * j)) % m) for j in range(5)]
+        c = [v - m if 2 * v > m else v for v in c]
+        assert max(abs(v) for v in c) <= 181
+        for _ in range(300):
+            L = [int(v) for v in rng.integers(-4096, 4097, 4)] + [int(rng.integers(-1025, 1026))]
+            t = sum(l * v for l, v in zip(L, c))
+            assert abs(t) < 1 << 22
+            X = sum(l << (13 * j) for j, l in enumerate(L))
+            r = float(CL.reduce_f32(t, m))
+            assert abs(r) <= 181 and (int(r) - X * T.inv[i]) % m == 0
 
 
 def test_kernel_digit_table_matches_the_moduli():
