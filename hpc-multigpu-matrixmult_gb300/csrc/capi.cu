@@ -266,16 +266,18 @@ int b_panels(int rows, int n, int bn, int cl, int sms) {
 }
 
 // phpc_gemm_cublas on the modular scheme, pipelined over row panels of A and
-// C and, for the first row panel, column panels of B: B's column panels
-// travel on stream sB and are split on sS as each arrives, A's row panels
-// travel and are split on sA and C's on sC; the first row panel's residue
-// GEMMs run block by block on sG as soon as A_0 and the block's B panel are
-// ready, later panels' GEMMs once all of B is, each panel's CRT once its
-// GEMMs and C_p are done, and C_p returns on sO while later panels compute.
-// Only the first blocks' copies and splits and the last panel's copy-out are
-// not overlapped. Inputs with inf/NaN are detected after the scans, before
-// any of C is copied back, and the call is redone in IEEE FP64 (DMMA) from
-// the original C.
+// C and column panels of B. The host-to-device copies go in the order A_0,
+// B_0, A_1, B_1, ... (each A panel after the B panel before it) until B is on
+// the device, then C's panels and the remaining A panels; B's panels are
+// split on sS as each arrives, A's on sA. While B is incomplete the residue
+// GEMMs run as (row panel, B column panel) blocks on sG, issued in the order
+// their operands arrive; the row panels after that run whole once all of B
+// is there. Each panel's CRT follows its last GEMM on sG (once C_p is on the
+// device), and C_p returns on sO while later panels compute: only the first
+// block's copies and splits and the last panel's copy-out are not
+// overlapped. Inputs with inf/NaN are detected after the scans, before any
+// of C is copied back, and the call is redone in IEEE FP64 (DMMA) from the
+// original C.
 int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double* c, int ldc, int m, int k, int n,
                       int nmod, float* seconds) {
   t_phase_ms[0] = t_phase_ms[1] = t_phase_ms[2] = 0.f;
@@ -305,22 +307,38 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       evs.push_back(e);
     };
     const int64_t dlda = (k + 1) & ~1, dldb = (n + 1) & ~1, dldc = (n + 1) & ~1;
-    for (auto& x : r.st)
-      if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
-    for (auto& x : sx)
-      if (rc == PHPC_OK && cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) rc = PHPC_ERR_CUDA;
+    // The split streams (A's: st[1], B's: sx[2]) get the highest priority:
+    // the GEMMs hold every SM until a launch ends, and a split whose panel
+    // has arrived should take the SMs before the next GEMM launch does.
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    for (int i = 0; i < kStreams; ++i)
+      if (rc == PHPC_OK && cudaStreamCreateWithPriority(&r.st[i], cudaStreamNonBlocking,
+                                                       i == 1 ? prio_high : prio_low) != cudaSuccess)
+        rc = PHPC_ERR_CUDA;
+    for (int i = 0; i < 3; ++i)
+      if (rc == PHPC_OK && cudaStreamCreateWithPriority(&sx[i], cudaStreamNonBlocking,
+                                                       i == 2 ? prio_high : prio_low) != cudaSuccess)
+        rc = PHPC_ERR_CUDA;
     cudaStream_t sB = r.st[0], sA = r.st[1], sG = r.st[2], sC = sx[0], sO = sx[1], sS = sx[2];
-    cudaEvent_t ev_alloc{}, ev_bcopy{}, ev_b1{}, ev_g0{}, ev_g1{}, ev_crt0{};
-    // per row panel: A copied, A split; C copied; GEMM started (panels > 0) and
-    // done; CRT started and done
-    std::vector<cudaEvent_t> ev_a0(np), ev_a1(np), ev_c(np), ev_gs(np), ev_m(np), ev_cs(np), ev_g(np);
-    // per B column panel: copied; split started, done; first row panel's block GEMM started, done
-    std::vector<cudaEvent_t> ev_bc(nbpanels), ev_bs0(nbpanels), ev_bs1(nbpanels), ev_gb0(nbpanels), ev_gb1(nbpanels);
-    for (cudaEvent_t* e : {&ev_alloc, &ev_bcopy, &ev_b1, &ev_g0, &ev_g1, &ev_crt0}) new_event(*e);
+    // Row panels 0 .. np_blk - 1 run as blocks over B's column panels (their A
+    // panels travel between B's); with one B panel only panel 0 does.
+    const int np_blk = nbpanels > 1 ? std::min(np, nbpanels) : 1;
+    cudaEvent_t ev_alloc{}, ev_bcopy{}, ev_b1{}, ev_g1{}, ev_first{};
+    // per row panel: A copied, A split; C copied; GEMM started and done
+    // (whole panels); CRT started and done
+    std::vector<cudaEvent_t> ev_acp(np), ev_a0(np), ev_a1(np), ev_c(np), ev_gs(np), ev_m(np), ev_cs(np), ev_g(np);
+    // per B column panel: copied; split started, done
+    std::vector<cudaEvent_t> ev_bc(nbpanels), ev_bs0(nbpanels), ev_bs1(nbpanels);
+    // per block (row panel < np_blk, B column panel): GEMM started, done
+    std::vector<cudaEvent_t> ev_gb0(np_blk * nbpanels), ev_gb1(np_blk * nbpanels);
+    for (cudaEvent_t* e : {&ev_alloc, &ev_bcopy, &ev_b1, &ev_g1, &ev_first}) new_event(*e);
     for (int p = 0; p < np; ++p)
-      for (auto* v : {&ev_a0, &ev_a1, &ev_c, &ev_gs, &ev_m, &ev_cs, &ev_g}) new_event((*v)[p]);
+      for (auto* v : {&ev_acp, &ev_a0, &ev_a1, &ev_c, &ev_gs, &ev_m, &ev_cs, &ev_g}) new_event((*v)[p]);
     for (int j = 0; j < nbpanels; ++j)
-      for (auto* v : {&ev_bc, &ev_bs0, &ev_bs1, &ev_gb0, &ev_gb1}) new_event((*v)[j]);
+      for (auto* v : {&ev_bc, &ev_bs0, &ev_bs1}) new_event((*v)[j]);
+    for (int i = 0; i < np_blk * nbpanels; ++i)
+      for (auto* v : {&ev_gb0, &ev_gb1}) new_event((*v)[i]);
     if (rc == PHPC_OK &&
         (cudaMallocFromPoolAsync(reinterpret_cast<void**>(&r.dA), sizeof(double) * m * dlda, pool, sB) !=
              cudaSuccess ||
@@ -342,17 +360,19 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
           rc = PHPC_ERR_CUDA;
           return;
         }
+        cudaEventRecord(ev_acp[p], sA);
         cudaEventRecord(ev_a0[p], sA);
         rc = ozaki2_prepare_a_rows(m, r0, rows, k, n, r.dA, dlda, nmod, r.ws, ws_bytes, sA);
         cudaEventRecord(ev_a1[p], sA);
       };
-      // The host-to-device copies run in the order they are issued: A's first
-      // panel, then B's column panels (each split on sS as it arrives), so
-      // that the first block GEMM waits for A_0 and B_0 only; then C's and
-      // A's remaining panels.
+      // The link carries one copy at a time in this order: A_0, B_0, A_1,
+      // B_1, ... (each copy waits for the one before it), so that the first
+      // block GEMM waits for A_0 and B_0 only and each later block for the
+      // panels it needs; then C's panels and A's remaining panels.
       issue_a(0);
       for (int j = 0; j < nbpanels && rc == PHPC_OK; ++j) {
         const int c0 = j * bcols, cols = std::min(bcols, n - c0);
+        cudaStreamWaitEvent(sB, ev_acp[std::min(j, np_blk - 1)], 0);
         if (cudaMemcpy2DAsync(r.dB + c0, dldb * 8, b + c0, (size_t)ldb * 8, (size_t)cols * 8, k,
                               cudaMemcpyHostToDevice, sB) != cudaSuccess) {
           rc = PHPC_ERR_CUDA;
@@ -363,6 +383,10 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
         cudaEventRecord(ev_bs0[j], sS);
         rc = ozaki2_prepare_b_cols(m, k, n, c0, cols, r.dB, dldb, nmod, r.ws, ws_bytes, sS);
         cudaEventRecord(ev_bs1[j], sS);
+        if (rc == PHPC_OK && j + 1 < np_blk) {
+          cudaStreamWaitEvent(sA, ev_bc[j], 0);
+          issue_a(j + 1);
+        }
       }
       cudaEventRecord(ev_bcopy, sB);
       cudaEventRecord(ev_b1, sS);
@@ -376,31 +400,45 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
           break;
         }
         cudaEventRecord(ev_c[p], sC);
-        if (p > 0) issue_a(p);
+        if (p >= np_blk) issue_a(p);
       }
-      // residue GEMMs and CRT per panel (the first panel's GEMMs per B column panel)
-      for (int p = 0; p < np && rc == PHPC_OK; ++p) {
+      // Residue GEMMs and CRTs on sG. The blocks of the first np_blk row
+      // panels in the order their operands arrive (A_p is the 2p-th copy, B_j
+      // the (2j+1)-th); a panel's CRT right after its last block.
+      auto crt = [&](int p) {
         const int r0 = p * pr, rows = std::min(pr, m - r0);
-        cudaStreamWaitEvent(sG, ev_a1[p], 0);
-        if (p == 0) {
-          cudaEventRecord(ev_g0, sG);
-          for (int j = 0; j < nbpanels && rc == PHPC_OK; ++j) {
-            const int c0 = j * bcols, cols = std::min(bcols, n - c0);
-            cudaStreamWaitEvent(sG, ev_bs1[j], 0);
-            cudaEventRecord(ev_gb0[j], sG);
-            rc = ozaki2_multiply_block(m, r0, rows, c0, cols, k, n, nmod, r.ws, ws_bytes, sG, bn);
-            cudaEventRecord(ev_gb1[j], sG);
-          }
-        } else {
-          cudaEventRecord(ev_gs[p], sG);
-          rc = ozaki2_multiply_rows(m, r0, rows, k, n, nmod, r.ws, ws_bytes, sG, bn);
-        }
         cudaEventRecord(ev_m[p], sG);
         cudaStreamWaitEvent(sG, ev_c[p], 0);
-        if (p == 0) cudaEventRecord(ev_crt0, sG);
         cudaEventRecord(ev_cs[p], sG);
         if (rc == PHPC_OK) rc = ozaki2_reconstruct_rows(m, r0, rows, k, n, r.dC, dldc, nmod, r.ws, ws_bytes, sG);
         cudaEventRecord(ev_g[p], sG);
+      };
+      std::vector<std::pair<int, int>> blocks;
+      for (int p = 0; p < np_blk; ++p)
+        for (int j = 0; j < nbpanels; ++j) blocks.emplace_back(p, j);
+      std::stable_sort(blocks.begin(), blocks.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+        return std::max(2 * x.first, 2 * x.second + 1) < std::max(2 * y.first, 2 * y.second + 1);
+      });
+      std::vector<int> left(np_blk, nbpanels);
+      for (const auto& bl : blocks) {
+        if (rc != PHPC_OK) break;
+        const int p = bl.first, j = bl.second;
+        const int r0 = p * pr, rows = std::min(pr, m - r0), c0 = j * bcols, cols = std::min(bcols, n - c0);
+        cudaStreamWaitEvent(sG, ev_a1[p], 0);
+        cudaStreamWaitEvent(sG, ev_bs1[j], 0);
+        cudaEventRecord(ev_gb0[p * nbpanels + j], sG);
+        if (&bl == &blocks.front()) cudaEventRecord(ev_first, sG);
+        rc = ozaki2_multiply_block(m, r0, rows, c0, cols, k, n, nmod, r.ws, ws_bytes, sG, bn);
+        cudaEventRecord(ev_gb1[p * nbpanels + j], sG);
+        if (--left[p] == 0) crt(p);
+      }
+      for (int p = np_blk; p < np && rc == PHPC_OK; ++p) {
+        const int r0 = p * pr, rows = std::min(pr, m - r0);
+        cudaStreamWaitEvent(sG, ev_a1[p], 0);
+        cudaStreamWaitEvent(sG, ev_b1, 0);
+        cudaEventRecord(ev_gs[p], sG);
+        rc = ozaki2_multiply_rows(m, r0, rows, k, n, nmod, r.ws, ws_bytes, sG, bn);
+        crt(p);
       }
       cudaEventRecord(ev_g1, sG);
     }
@@ -430,16 +468,16 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       if (cudaStreamSynchronize(st) != cudaSuccess && rc == PHPC_OK) rc = PHPC_ERR_CUDA;
     if (rc == PHPC_OK && getenv("PHPC_VERBOSE")) {
       // timeline of the call (ms after the allocations): B's panels copied /
-      // split, the first row panel's block GEMMs, per panel A split, C
-      // copied, GEMM + CRT done, and the last copy-out
-      fprintf(stderr, "phpc: modular pipeline %d row panels of %d rows, %d B panels of %d columns:", np, pr, nbpanels,
-              bcols);
+      // split, per panel A copied / split, C copied, GEMM (block or whole) and
+      // CRT done, and the last copy-out
+      fprintf(stderr, "phpc: modular pipeline %d row panels of %d rows (%d as blocks), %d B panels of %d columns:",
+              np, pr, np_blk, nbpanels, bcols);
       for (int j = 0; j < nbpanels; ++j)
-        fprintf(stderr, " b%d copied %.2f split %.2f gemm %.2f-%.2f", j, elapsed_ms(ev_alloc, ev_bc[j]),
-                elapsed_ms(ev_alloc, ev_bs1[j]), elapsed_ms(ev_alloc, ev_gb0[j]), elapsed_ms(ev_alloc, ev_gb1[j]));
+        fprintf(stderr, " b%d copied %.2f split %.2f", j, elapsed_ms(ev_alloc, ev_bc[j]), elapsed_ms(ev_alloc, ev_bs1[j]));
       fprintf(stderr, " |");
       for (int p = 0; p < np; ++p)
-        fprintf(stderr, " p%d A %.2f C %.2f G %.2f", p, elapsed_ms(ev_alloc, ev_a1[p]), elapsed_ms(ev_alloc, ev_c[p]),
+        fprintf(stderr, " p%d A %.2f/%.2f C %.2f G %.2f CRT %.2f", p, elapsed_ms(ev_alloc, ev_acp[p]),
+                elapsed_ms(ev_alloc, ev_a1[p]), elapsed_ms(ev_alloc, ev_c[p]), elapsed_ms(ev_alloc, ev_m[p]),
                 elapsed_ms(ev_alloc, ev_g[p]));
       fprintf(stderr, " | out %.2f\n", elapsed_ms(ev_alloc, ev_out));
     }
@@ -447,26 +485,18 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
       rc = PHPC_ERR_CUDA;
     float kernel_ms = 0.f;
     if (rc == PHPC_OK) {
-      // device compute time: A's first panel split and B's panel splits (they
-      // run while B travels), the first row panel's block GEMMs, then its CRT
-      // through the last panel's CRT, a span in which the kernels follow one
-      // another without gaps (later A splits run between the panel GEMMs);
-      // spans that only wait for copies are not added
-      kernel_ms = elapsed_ms(ev_a0[0], ev_a1[0]) + elapsed_ms(ev_crt0, ev_g1);
-      for (int j = 0; j < nbpanels; ++j)
-        kernel_ms += elapsed_ms(ev_bs0[j], ev_bs1[j]) + elapsed_ms(ev_gb0[j], ev_gb1[j]);
-      // per phase: the spans of its kernels (later A splits run while GEMMs
-      // of earlier panels do, so the three can add up to more than kernel_ms)
+      // device compute time: the kernels on sG (GEMM blocks and panels, CRTs)
+      // and the splits that the first block waited for (A_0's and B_0's);
+      // later splits run on other streams while GEMMs do and are not added
       float prep = 0.f, gemm = 0.f, crt = 0.f;
-      for (int j = 0; j < nbpanels; ++j) {
-        prep += elapsed_ms(ev_bs0[j], ev_bs1[j]);
-        gemm += elapsed_ms(ev_gb0[j], ev_gb1[j]);
-      }
+      for (int j = 0; j < nbpanels; ++j) prep += elapsed_ms(ev_bs0[j], ev_bs1[j]);
       for (int p = 0; p < np; ++p) {
         prep += elapsed_ms(ev_a0[p], ev_a1[p]);
-        if (p > 0) gemm += elapsed_ms(ev_gs[p], ev_m[p]);
+        if (p >= np_blk) gemm += elapsed_ms(ev_gs[p], ev_m[p]);
         crt += elapsed_ms(ev_cs[p], ev_g[p]);
       }
+      for (int i = 0; i < np_blk * nbpanels; ++i) gemm += elapsed_ms(ev_gb0[i], ev_gb1[i]);
+      kernel_ms = elapsed_ms(ev_a0[0], ev_a1[0]) + elapsed_ms(ev_bs0[0], ev_bs1[0]) + gemm + crt;
       t_phase_ms[0] = prep;
       t_phase_ms[1] = gemm;
       t_phase_ms[2] = crt;
@@ -479,7 +509,7 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
           cudaMemcpy2DAsync(r.dC, dldc * 8, c, (size_t)ldc * 8, (size_t)n * 8, m, cudaMemcpyHostToDevice, sB) !=
               cudaSuccess)
         rc = PHPC_ERR_CUDA;
-      cudaEventRecord(ev_g0, sB);
+      cudaEventRecord(ev_first, sB);
       if (rc == PHPC_OK) rc = dgemm_dmma(m, k, n, r.dA, dlda, r.dB, dldb, r.dC, dldc, 1, 1, 256, sB);
       cudaEventRecord(ev_g1, sB);
       if (rc == PHPC_OK &&
@@ -489,7 +519,7 @@ int host_gemm_modular(const double* a, int lda, const double* b, int ldb, double
            cudaMemcpy(&dstatus, status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess))
         rc = PHPC_ERR_CUDA;
       if (rc == PHPC_OK) {
-        kernel_ms = elapsed_ms(ev_g0, ev_g1);
+        kernel_ms = elapsed_ms(ev_first, ev_g1);
         t_phase_ms[0] = t_phase_ms[2] = 0.f;
         t_phase_ms[1] = kernel_ms;
       }
