@@ -209,7 +209,9 @@ __device__ __forceinline__ NormAcc norm_warp(NormAcc a) {
 }
 
 // One lane's share of a row's scan: elements lane, lane + 32, ... in that
-// order, four loads issued before they are accumulated.
+// order, four loads issued before they are accumulated. (Eight measured
+// 3 % faster on 16384-element rows and 20 % slower on the batch's short
+// rows.)
 __device__ __forceinline__ void norm_row_lane(const double* __restrict__ a, int K, int lane, NormAcc& acc,
                                               bool& nonfinite) {
   int k = lane;
@@ -223,17 +225,16 @@ __device__ __forceinline__ void norm_row_lane(const double* __restrict__ a, int 
   for (; k < K; k += 32) norm_add(acc, a[k], nonfinite);
 }
 
-// Rows k0 .. k1 - 1 of column col of B, in order, four loads at a time.
+// Rows k0 .. k1 - 1 of column col of B, in order, eight loads at a time.
 __device__ __forceinline__ void norm_col_chunk(const double* __restrict__ B, int64_t ldb, int64_t col, int k0, int k1,
                                                NormAcc& acc, bool& nonfinite) {
   int k = k0;
-  for (; k + 3 < k1; k += 4) {
-    const double x0 = B[(int64_t)k * ldb + col], x1 = B[(int64_t)(k + 1) * ldb + col];
-    const double x2 = B[(int64_t)(k + 2) * ldb + col], x3 = B[(int64_t)(k + 3) * ldb + col];
-    norm_add(acc, x0, nonfinite);
-    norm_add(acc, x1, nonfinite);
-    norm_add(acc, x2, nonfinite);
-    norm_add(acc, x3, nonfinite);
+  for (; k + 7 < k1; k += 8) {
+    double x[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) x[u] = B[(int64_t)(k + u) * ldb + col];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) norm_add(acc, x[u], nonfinite);
   }
   for (; k < k1; ++k) norm_add(acc, B[(int64_t)k * ldb + col], nonfinite);
 }
