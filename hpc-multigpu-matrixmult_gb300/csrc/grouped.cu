@@ -307,7 +307,7 @@ TableLayout table_layout(int count, int64_t tiles) {
   T.tprob = align_up(sizeof(GSplitProb) * (size_t)count, 256);
   T.maps = align_up(T.tprob + sizeof(TcGroupProblem) * (size_t)count, 256);
   T.tiles = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
-  T.sched = align_up(T.tiles + sizeof(int2) * (size_t)tiles, 256);  // the GEMM's unit counter
+  T.sched = align_up(T.tiles + sizeof(int4) * (size_t)tiles, 256);  // the GEMM's unit counter
   T.end = align_up(T.sched + sizeof(int), 256);
   return T;
 }
@@ -587,7 +587,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->table.group_rows = 8;
   pl->table.probs = reinterpret_cast<const TcGroupProblem*>(base + T.tprob);
   pl->table.maps = reinterpret_cast<const CUtensorMap*>(base + T.maps);
-  pl->table.tiles = reinterpret_cast<const int2*>(base + T.tiles);
+  pl->table.tiles = reinterpret_cast<const int4*>(base + T.tiles);
   // units handed out in order by a counter (PHPC_GROUPED_SCHED=static: CTA c
   // takes units c, c + grid, ...)
   {
@@ -595,9 +595,13 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     const bool stat = env && std::strcmp(env, "static") == 0;
     pl->table.next_unit = stat ? nullptr : reinterpret_cast<int*>(base + T.sched);
   }
-  std::vector<int2> htiles(tiles);
+  std::vector<int4> htiles(tiles);
   for (int i = 0; i < count && rc == PHPC_OK; ++i)
-    for (int u = 0; u < ht[i].tm * ht[i].tn; ++u) htiles[ht[i].tile_start + u] = make_int2(i, u);
+    for (int u = 0; u < ht[i].tm * ht[i].tn; ++u) {
+      int rm = 0, rn = 0;
+      tc_tile_coords(ht[i].tm, ht[i].tn, pl->table.group_rows, u, rm, rn);
+      htiles[ht[i].tile_start + u] = make_int4(i, rm, rn, ceil_div(ht[i].K, kTcBK));
+    }
   if (rc == PHPC_OK) {
     if (modular)
       rc = pl->bn == 128 ? prepare_grouped_gemm<128, kResidue>() : prepare_grouped_gemm<256, kResidue>();
@@ -612,7 +616,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
            cudaSuccess ||
        cudaMemcpyAsync(base + T.maps, hm.data(), sizeof(CUtensorMap) * 2 * count, cudaMemcpyHostToDevice, st) !=
            cudaSuccess ||
-       (tiles > 0 && cudaMemcpyAsync(base + T.tiles, htiles.data(), sizeof(int2) * tiles, cudaMemcpyHostToDevice,
+       (tiles > 0 && cudaMemcpyAsync(base + T.tiles, htiles.data(), sizeof(int4) * tiles, cudaMemcpyHostToDevice,
                                      st) != cudaSuccess) ||
        cudaStreamSynchronize(st) != cudaSuccess))
     rc = PHPC_ERR_CUDA;

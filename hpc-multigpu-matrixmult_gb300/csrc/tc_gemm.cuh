@@ -135,7 +135,7 @@ struct TcGroupTable {
   int group_rows;
   const TcGroupProblem* probs;  // [count]
   const CUtensorMap* maps;      // [2 * count], 64-byte aligned
-  const int2* tiles;            // [ntiles]: (problem, tile index within the problem), one load per tile
+  const int4* tiles;            // [ntiles]: (problem, tile row, tile column, K-steps), one load per tile
   int* next_unit;               // non-null: units handed out in order by this counter (zeroed before
                                 // each launch), else CTA c takes units c, c + grid, ...
 };
@@ -182,7 +182,7 @@ struct TcCfg {
 
 // Tile t of a tm x tn tile grid in L2 raster order: groups of group_rows tile
 // rows, column-major inside a group, so consecutive tiles share a B panel.
-__device__ __forceinline__ void tc_tile_coords(int tm, int tn, int group_rows, int t, int& rm, int& rn) {
+__host__ __device__ __forceinline__ void tc_tile_coords(int tm, int tn, int group_rows, int t, int& rm, int& rn) {
   const int per_group = group_rows * tn;
   const int grp = t / per_group;
   const int r0 = grp * group_rows;
@@ -220,13 +220,16 @@ __device__ __forceinline__ void tc_job(int t, const TcArgs& a, const CUtensorMap
     j.ldr = a.ldr;
     j.rplane = a.rplane;
   } else {
-    const int2 e = g.tiles[t];
+    // the tile's coordinates and K-steps come with its table entry: the TMA
+    // producer needs nothing else (no second, dependent load)
+    const int4 e = g.tiles[t];
     const int lo = e.x;
     const TcGroupProblem& p = g.probs[lo];
     j.M = p.M;
     j.N = p.N;
-    j.nk = (p.K + kTcBK - 1) / kTcBK;
-    tc_tile_coords(p.tm, p.tn, g.group_rows, e.y, j.rm, j.rn);
+    j.nk = e.w;
+    j.rm = e.y;
+    j.rn = e.z;
     j.tmA = g.maps + 2 * lo;
     j.tmB = g.maps + 2 * lo + 1;
     j.C = p.C;
