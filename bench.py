@@ -76,8 +76,12 @@ METRIC = "FP64-accurate GEMM TFLOP/s @N=16384: split-TC vs plain DMMA, rel errâ‰
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
 # dominant kernel, from a one-pass ncu capture of this workload on a GB300;
-# keyed by (N, "slices" | "moduli", count).
+# keyed by (N, "slices" | "moduli", count). The capture predates the odd
+# rounds of residue units walking K backwards, which read 6-20 % less DRAM at
+# N = 6144-8192 (smaller captures of the current kernel).
 NCU_TRAFFIC_BYTES = {(16384, "moduli", 13): 112.12e9 + 7.31e9}
+NCU_TRAFFIC_NOTE = ("one-pass ncu capture of this launch before odd rounds of units walked K backwards "
+                    "(the current kernel reads 6-20 % less DRAM at N = 6144-8192)")
 UNIT = "TFLOP/s"
 
 
@@ -491,6 +495,7 @@ def run_ours(args, world, rank, local):
                      "achieved": round(achieved, 1), "peak": peak, "unit": "TFLOP/s",
                      "frac": round(achieved / peak, 4), "traffic": NCU_TRAFFIC_BYTES.get(key),
                      "traffic_unit": "DRAM bytes per launch (ncu)",
+                     "traffic_note": NCU_TRAFFIC_NOTE if key in NCU_TRAFFIC_BYTES else None,
                      "peak_source": peak_src,
                      "work_per_launch": f"{unit_desc} x 2 N^3 = {sch.gemms * flops:.4e} bf16 flop"},
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": 3 * n * n * 8,
