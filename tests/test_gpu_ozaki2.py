@@ -239,12 +239,16 @@ def test_host_entry_uses_modular_scheme(phpc, torch_cuda, monkeypatch):
 
 
 
-@pytest.mark.parametrize("m,k,n", [(2500, 300, 200), (4096, 64, 256), (5000, 48, 8200), (10000, 32, 16400)])
+@pytest.mark.parametrize("m,k,n", [(2500, 300, 200), (4096, 64, 256), (5000, 48, 8200), (10000, 32, 16400),
+                                   (4864, 40, 8192), (12160, 40, 8192)])
 def test_host_pipeline_panels_equal_device_call(phpc, torch_cuda, monkeypatch, m, k, n):
     """phpc_gemm_cublas runs the modular scheme over row panels of A and C
-    (ragged last panel here) and, for the two larger shapes, the first row
-    panel's GEMMs over four column panels of B (ragged last one); the result
-    equals the one-call device path."""
+    (ragged last panel in most shapes) and, with four column panels of B,
+    the first row panels' GEMMs as (row panel, B panel) blocks: all four row
+    panels at 10000 x 16400 (ragged last B panel), two row panels with four B
+    panels at 4864 x 8192, four row panels as blocks and the fifth whole at
+    12160 x 8192 (five row panels of 2432 rows); the result equals the
+    one-call device path."""
     monkeypatch.setenv("PHPC_MODULI", "15")
     rng = np.random.default_rng(m + k + n)
     a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-20, 21, (m, k)))
