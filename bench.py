@@ -109,6 +109,7 @@ def parse_args():
     p.add_argument("--m", type=int, default=0)
     p.add_argument("--k", type=int, default=0)
     p.add_argument("--reps", type=int, default=2)
+    p.add_argument("--count", type=int, default=512, help="--case batched: number of problems")
     p.add_argument("--check-rows", type=int, default=0)
     p.add_argument("--grid", default="1x1", help="--case dmma: logical SUMMA block grid (width x height)")
     p.add_argument("--summa-rank", default=None, metavar="RxC",
@@ -623,7 +624,8 @@ def run_case(args) -> None:
     import workloads
 
     if args.case == "batched":
-        r = workloads.batched(torch, phpc, moduli=args.moduli if args.moduli > 0 else 13, reps=args.reps)
+        r = workloads.batched(torch, phpc, count=args.count, moduli=args.moduli if args.moduli > 0 else 13,
+                              reps=args.reps)
         print(json.dumps(r), flush=True)
         if r["status"] != 0:
             raise SystemExit(1)

@@ -241,25 +241,28 @@ __global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb
                           p.eb, p.bb, T, p.pb, p.ldp, (int64_t)p.n * p.ldp, tile);
 }
 
-constexpr int kCrtUnitCols = 32 * kCrtCols;  // columns of one CRT unit (one warp)
+// CRT units: 32 groups of kCrtCols consecutive columns of one row (a
+// group never spans two rows; a row's last group may be short), numbered
+// row-major through each problem and across the problems, so that a warp's
+// lanes stay busy whatever the problem's width: a problem of m rows and n
+// columns has ceil(m * ceil(n / kCrtCols) / 32) units.
+inline int64_t crt_units_of(int m, int n) { return ((int64_t)m * ceil_div(n, kCrtCols) + 31) / 32; }
 
-// Modular scheme: C += the CRT of the residues. One warp per unit of one row
-// and 128 columns, units numbered across the problems (no idle blocks for
-// narrow problems), four columns per thread.
+// Modular scheme: C += the CRT of the residues. One warp per unit, one group
+// of kCrtCols columns per lane.
 template <int NMOD>
 __global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict__ P, int count, int total_units,
                                                     const __grid_constant__ ModTable T) {
   const int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (u >= total_units) return;
   const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.crt_unit_start; })];
-  const int w = u - p.crt_unit_start;
-  const int chunks = (p.n + kCrtUnitCols - 1) / kCrtUnitCols;
-  const int64_t row = w / chunks;
-  const int64_t c0 = (int64_t)(w % chunks) * kCrtUnitCols + (threadIdx.x & 31) * kCrtCols;
-  if (c0 >= p.n) return;
+  const int64_t gpr = (p.n + kCrtCols - 1) / kCrtCols;  // groups per row
+  const int64_t g = (int64_t)(u - p.crt_unit_start) * 32 + (threadIdx.x & 31);
+  if (g >= p.m * gpr) return;
+  const int64_t row = g / gpr, c0 = (g - row * gpr) * kCrtCols;
   crt_cols<NMOD>(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
-           static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - p.ba[row],
-           p.eb + c0, p.bb + c0, p.C + row * p.ldc + c0);
+                 static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - p.ba[row],
+                 p.eb + c0, p.bb + c0, p.C + row * p.ldc + c0);
 }
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -539,7 +542,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     rblocks += ceil_div(q.n, kColBlockJ) * ceil_div((int)L.ldp, kColBlockK);
     pieces += (int64_t)q.m * (L.ldp / 8);
     cunits += (int64_t)q.n * ceil_div(q.k, kScanKChunk);
-    if (modular) crt_units += (int64_t)q.m * ceil_div(q.n, kCrtUnitCols);
+    if (modular) crt_units += crt_units_of(q.m, q.n);
 
     TcGroupProblem& t = ht[i];
     t = TcGroupProblem{};

@@ -249,19 +249,18 @@ __device__ __forceinline__ int grid_bits(float s, int K, float logT) {
 constexpr int kLimbs = 5;  // balanced 13-bit limbs of an operand integer
 
 // The operand integer V = sign * X (X <= 2^62) as five balanced 13-bit limbs
-// held in floats: V = sum L_j 2^(13 j), |L_j| <= 2^12 (|L_4| <= 2^10 + 1).
-__device__ __forceinline__ void balanced_limbs(uint64_t X, bool neg, float (&L)[kLimbs]) {
-  uint64_t x = X;
-#pragma unroll
-  for (int j = 0; j < kLimbs - 1; ++j) {
-    const int d = static_cast<int>(x & 0x1FFFu);
-    const int c = d >= 0x1000;
-    const int l = d - (c << 13);
-    L[j] = float_of_small_int(neg ? -l : l);
-    x = (x >> 13) + static_cast<uint64_t>(c);
-  }
-  const int top = static_cast<int>(x);
-  L[kLimbs - 1] = float_of_small_int(neg ? -top : top);
+// held in floats: V = sum L_j 2^(13 j), |L_j| <= 2^12 (|L_4| <= 2^10 + 1),
+// L_j in [-2^12, 2^12) for j < 4. Adding 2^12 to each of the four low 13-bit
+// fields (X' = X + kLimbBias, no overflow for X <= 2^62) turns these limbs
+// into plain bit fields of X': L_j = field_j(X') - 2^12 for j < 4 and
+// L_4 = X' >> 52 (the carries of the balancing are those of the addition;
+// the limbs are unique, so they equal the ones of a digit-by-digit
+// balancing). A field f becomes the float 1.5 * 2^23 + f through its bits,
+// and one exact FMA removes the offset and applies the sign.
+constexpr uint64_t kLimbBias = 0x1000ull * (1ull + (1ull << 13) + (1ull << 26) + (1ull << 39));
+
+__device__ __forceinline__ float limb_field(uint64_t xb, int shift) {
+  return __uint_as_float(0x4B400000u | (static_cast<uint32_t>(xb >> shift) & 0x1FFFu));
 }
 
 // Two residues as a packed BF16 pair (lo in the low half): integer-valued
@@ -305,14 +304,21 @@ __device__ __forceinline__ float2 residue_pair(const float2 (&L)[kLimbs], const 
 
 // Limbs of the 8 values v[0..7] as 4 lane pairs (v[2p], v[2p + 1]).
 __device__ __forceinline__ void limb_pairs(const double (&v)[8], int e, int bits, float2 (&P)[4][kLimbs]) {
+  constexpr float kOff = 12582912.0f + 4096.0f;  // 1.5 * 2^23 + 2^12
+  constexpr float kOffTop = 12582912.0f;
 #pragma unroll
   for (int p = 0; p < 4; ++p) {
-    float L0[kLimbs], L1[kLimbs];
     bool n0, n1;
-    balanced_limbs(fixed_point(v[2 * p], e, bits, n0), n0, L0);
-    balanced_limbs(fixed_point(v[2 * p + 1], e, bits, n1), n1, L1);
+    const uint64_t x0 = fixed_point(v[2 * p], e, bits, n0) + kLimbBias;
+    const uint64_t x1 = fixed_point(v[2 * p + 1], e, bits, n1) + kLimbBias;
+    const float2 sg = make_float2(n0 ? -1.0f : 1.0f, n1 ? -1.0f : 1.0f);
+    const float2 off = make_float2(n0 ? kOff : -kOff, n1 ? kOff : -kOff);
 #pragma unroll
-    for (int j = 0; j < kLimbs; ++j) P[p][j] = make_float2(L0[j], L1[j]);
+    for (int j = 0; j < kLimbs - 1; ++j)
+      P[p][j] = __ffma2_rn(make_float2(limb_field(x0, 13 * j), limb_field(x1, 13 * j)), sg, off);
+    const float2 top = make_float2(__uint_as_float(0x4B400000u | static_cast<uint32_t>(x0 >> 52)),
+                                   __uint_as_float(0x4B400000u | static_cast<uint32_t>(x1 >> 52)));
+    P[p][kLimbs - 1] = __ffma2_rn(top, sg, make_float2(n0 ? kOffTop : -kOffTop, n1 ? kOffTop : -kOffTop));
   }
 }
 
