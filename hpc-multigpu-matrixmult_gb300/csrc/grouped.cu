@@ -258,8 +258,14 @@ __global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict
   const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.crt_unit_start; })];
   const int64_t gpr = (p.n + kCrtCols - 1) / kCrtCols;  // groups per row
   const int64_t g = (int64_t)(u - p.crt_unit_start) * 32 + (threadIdx.x & 31);
-  if (g >= p.m * gpr) return;
-  const int64_t row = g / gpr, c0 = (g - row * gpr) * kCrtCols;
+  const int64_t groups = p.m * gpr;
+  if (g >= groups) return;
+  int64_t row;
+  if (groups <= INT32_MAX)  // the usual case: a 32-bit division
+    row = static_cast<uint32_t>(g) / static_cast<uint32_t>(gpr);
+  else
+    row = g / gpr;
+  const int64_t c0 = (g - row * gpr) * kCrtCols;
   crt_cols<NMOD>(p.R + row * p.ldr + c0, (int64_t)p.m * p.ldr, T.crt, p.fast,
                  static_cast<int>(min(static_cast<int64_t>(kCrtCols), p.n - c0)), max(p.ea[row], -20000) - p.ba[row],
                  p.eb + c0, p.bb + c0, p.C + row * p.ldc + c0);
