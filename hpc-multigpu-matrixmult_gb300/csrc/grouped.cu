@@ -248,14 +248,25 @@ __global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb
 // columns has ceil(m * ceil(n / kCrtCols) / 32) units.
 inline int64_t crt_units_of(int m, int n) { return ((int64_t)m * ceil_div(n, kCrtCols) + 31) / 32; }
 
+constexpr int kCrtBlockUnits = 4;  // CRT units (warps) per 128-thread block
+
+// CRT blocks of a batch: one first-problem entry per block.
+inline int64_t crt_blocks_of(int64_t crt_units) { return (crt_units + kCrtBlockUnits - 1) / kCrtBlockUnits; }
+
 // Modular scheme: C += the CRT of the residues. One warp per unit, one group
-// of kCrtCols columns per lane.
+// of kCrtCols columns per lane. first[b] is the problem of block b's first
+// unit (written with the plan); a warp walks on from it (a block's units
+// span at most kCrtBlockUnits problems).
 template <int NMOD>
-__global__ void __launch_bounds__(128) g_crt_kernel(const GSplitProb* __restrict__ P, int count, int total_units,
-                                                    const __grid_constant__ ModTable T) {
-  const int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+__global__ void __launch_bounds__(32 * kCrtBlockUnits) g_crt_kernel(const GSplitProb* __restrict__ P,
+                                                                   const int* __restrict__ first, int count,
+                                                                   int total_units,
+                                                                   const __grid_constant__ ModTable T) {
+  const int u = blockIdx.x * kCrtBlockUnits + (threadIdx.x >> 5);
   if (u >= total_units) return;
-  const GSplitProb& p = P[locate(P, count, u, [](const GSplitProb& q) { return q.crt_unit_start; })];
+  int pi = first[blockIdx.x];
+  while (pi + 1 < count && P[pi + 1].crt_unit_start <= u) ++pi;
+  const GSplitProb& p = P[pi];
   const int64_t gpr = (p.n + kCrtCols - 1) / kCrtCols;  // groups per row
   const int64_t g = (int64_t)(u - p.crt_unit_start) * 32 + (threadIdx.x & 31);
   const int64_t groups = p.m * gpr;
@@ -299,7 +310,7 @@ ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
 }
 
 struct TableLayout {
-  size_t split, tprob, maps, tiles, sched, end;
+  size_t split, tprob, maps, tiles, sched, crt_first, end;
 };
 
 // Output tiles of the batch at the narrowest tile width (an upper bound for
@@ -310,14 +321,23 @@ int64_t max_tiles(const phpc_gemm_problem* problems, int count) {
   return t;
 }
 
-TableLayout table_layout(int count, int64_t tiles) {
+// CRT blocks of the batch (0 if a problem is invalid: the callers check).
+int64_t max_crt_blocks(const phpc_gemm_problem* problems, int count) {
+  int64_t u = 0;
+  for (int i = 0; i < count; ++i)
+    if (problems[i].m > 0 && problems[i].n > 0) u += crt_units_of(problems[i].m, problems[i].n);
+  return crt_blocks_of(u);
+}
+
+TableLayout table_layout(int count, int64_t tiles, int64_t crt_blocks) {
   TableLayout T;
   T.split = 0;
   T.tprob = align_up(sizeof(GSplitProb) * (size_t)count, 256);
   T.maps = align_up(T.tprob + sizeof(TcGroupProblem) * (size_t)count, 256);
   T.tiles = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
   T.sched = align_up(T.tiles + sizeof(int4) * (size_t)tiles, 256);  // the GEMM's unit counter
-  T.end = align_up(T.sched + sizeof(int), 256);
+  T.crt_first = align_up(T.sched + sizeof(int), 256);  // modular scheme: the CRT blocks' first problems
+  T.end = align_up(T.crt_first + sizeof(int) * (size_t)crt_blocks, 256);
   return T;
 }
 
@@ -361,6 +381,7 @@ struct phpc_grouped_plan {
   int total_rows, total_cols, total_sblocks, total_rblocks, total_tiles, total_pieces, total_cunits,
       total_crt_units;
   phpc::GSplitProb* d_split;
+  const int* d_crt_first;  // modular scheme: first problem of each CRT block
   phpc::TcGroupTable table;
   phpc::PairList pairs;
   phpc::ModTable mods;  // modular scheme: moduli constants (grid widths are per problem)
@@ -448,8 +469,9 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
   if (rc == PHPC_OK && modular) {
     if (pl->mods.crt.L.np != crt_digits(pl->mods.n)) return PHPC_ERR_UNSUPPORTED;
     with_crt_moduli(pl->mods.n, [&](auto nm) {
-      g_crt_kernel<decltype(nm)::value><<<ceil_div(pl->total_crt_units, 4), 128, 0, stream>>>(
-          pl->d_split, pl->count, pl->total_crt_units, pl->mods);
+      g_crt_kernel<decltype(nm)::value>
+          <<<ceil_div(pl->total_crt_units, kCrtBlockUnits), 32 * kCrtBlockUnits, 0, stream>>>(
+              pl->d_split, pl->d_crt_first, pl->count, pl->total_crt_units, pl->mods);
     });
     if (cudaGetLastError() != cudaSuccess) rc = PHPC_ERR_CUDA;
   }
@@ -457,7 +479,7 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
 }
 
 size_t grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int planes, bool modular) {
-  size_t total = table_layout(count, max_tiles(problems, count)).end;
+  size_t total = table_layout(count, max_tiles(problems, count), modular ? max_crt_blocks(problems, count) : 0).end;
   for (int i = 0; i < count; ++i) {
     if (!valid_problem(problems[i])) return 0;
     total += prob_layout(problems[i], planes, modular).end;
@@ -497,7 +519,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     pl->pairs = grouped_pairs(planes);
   }
 
-  const TableLayout T = table_layout(count, max_tiles(problems, count));
+  const TableLayout T =
+      table_layout(count, max_tiles(problems, count), modular ? max_crt_blocks(problems, count) : 0);
   uint8_t* base = static_cast<uint8_t*>(workspace);
   std::vector<GSplitProb> hs(count);
   std::vector<TcGroupProblem> ht(count);
@@ -591,6 +614,14 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->total_cunits = static_cast<int>(cunits);
   pl->total_crt_units = static_cast<int>(crt_units);
   pl->d_split = reinterpret_cast<GSplitProb*>(base + T.split);
+  pl->d_crt_first = reinterpret_cast<const int*>(base + T.crt_first);
+  // the problem of each CRT block's first unit
+  std::vector<int> hfirst(modular && rc == PHPC_OK ? crt_blocks_of(crt_units) : 0);
+  for (size_t b = 0, i = 0; b < hfirst.size(); ++b) {
+    const int64_t u = (int64_t)b * kCrtBlockUnits;
+    while (i + 1 < (size_t)count && hs[i + 1].crt_unit_start <= u) ++i;
+    hfirst[b] = static_cast<int>(i);
+  }
   pl->table.count = count;
   pl->table.ntiles = tiles;
   pl->table.group_rows = 8;
@@ -627,6 +658,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
            cudaSuccess ||
        (tiles > 0 && cudaMemcpyAsync(base + T.tiles, htiles.data(), sizeof(int4) * tiles, cudaMemcpyHostToDevice,
                                      st) != cudaSuccess) ||
+       (!hfirst.empty() && cudaMemcpyAsync(base + T.crt_first, hfirst.data(), sizeof(int) * hfirst.size(),
+                                           cudaMemcpyHostToDevice, st) != cudaSuccess) ||
        cudaStreamSynchronize(st) != cudaSuccess))
     rc = PHPC_ERR_CUDA;
   if (rc != PHPC_OK) {

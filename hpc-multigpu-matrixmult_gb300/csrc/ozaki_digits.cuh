@@ -53,7 +53,8 @@ __device__ __forceinline__ uint64_t fixed_point(double x, int e, int P, bool& ne
   const int sh = elsb + P - e;
   if (m == 0) return 0;
   if (sh >= 0) return m << sh;  // |x| < 2^e  =>  X < 2^P <= 2^63
-  if (sh > -64) return (m >> (-sh)) + ((m >> (-sh - 1)) & 1ull);
+  // round half up: (m + 2^(s-1)) >> s, s = -sh (m < 2^53, no overflow)
+  if (sh > -64) return (m + (1ull << (-sh - 1))) >> (-sh);
   return 0;
 }
 
