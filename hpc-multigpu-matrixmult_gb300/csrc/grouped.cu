@@ -217,23 +217,37 @@ __global__ void __launch_bounds__(256) g_split_cols_kernel(const GSplitProb* __r
 // splits are held to 64 registers, four CTAs per SM: 4 % faster than at 79
 // registers and three CTAs; instantiated per modulus count, they fit without
 // spills.)
-template <int NMOD>
-__global__ void __launch_bounds__(256, 4) g_residue_rows_kernel(const GSplitProb* __restrict__ P, int count,
-                                                             int total_pieces, const __grid_constant__ ModTable T) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= total_pieces) return;
-  const RowPiece rp = row_piece(P, count, t);
-  const GSplitProb& p = *rp.p;
-  residue_row_piece<NMOD>(p.A + rp.row * p.lda, p.k, p.ea[rp.row], p.ba[rp.row], T, p.pa + rp.row * p.ldp,
-                    (int64_t)p.m * p.ldp, rp.k0);
-}
+// Row pieces per block of the modular row split; first[b] (written with the
+// plan) is the problem of block b's first piece, and each thread walks on
+// from it (a block's 256 pieces span few problems: a problem has at least
+// one piece per row).
+constexpr int kResRowBlock = 256;
 
 template <int NMOD>
-__global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb* __restrict__ P, int count,
-                                                             int total_blocks, const __grid_constant__ ModTable T) {
+__global__ void __launch_bounds__(kResRowBlock, 4) g_residue_rows_kernel(const GSplitProb* __restrict__ P,
+                                                                      const int* __restrict__ first, int count,
+                                                                      int total_pieces,
+                                                                      const __grid_constant__ ModTable T) {
+  const int t = blockIdx.x * kResRowBlock + threadIdx.x;
+  if (t >= total_pieces) return;
+  int pi = first[blockIdx.x];
+  while (pi + 1 < count && P[pi + 1].piece_start <= t) ++pi;
+  const GSplitProb& p = P[pi];
+  const int per_row = static_cast<int>(p.ldp >> 3);
+  const int local = t - p.piece_start;
+  const int64_t row = local / per_row, k0 = static_cast<int64_t>(local % per_row) * 8;
+  residue_row_piece<NMOD>(p.A + row * p.lda, p.k, p.ea[row], p.ba[row], T, p.pa + row * p.ldp, (int64_t)p.m * p.ldp,
+                          k0);
+}
+
+// Column blocks: prob[b] (written with the plan) is block b's problem.
+template <int NMOD>
+__global__ void __launch_bounds__(256, 4) g_residue_cols_kernel(const GSplitProb* __restrict__ P,
+                                                             const int* __restrict__ prob, int total_blocks,
+                                                             const __grid_constant__ ModTable T) {
   const int b = blockIdx.x;
   if (b >= total_blocks) return;  // uniform over the CTA
-  const GSplitProb& p = P[locate(P, count, b, [](const GSplitProb& q) { return q.rblock_start; })];
+  const GSplitProb& p = P[prob[b]];
   const int lb = b - p.rblock_start;
   const int nblk_j = (p.n + kColBlockJ - 1) / kColBlockJ;
   __shared__ double tile[kColBlockK][kColBlockJ];
@@ -310,8 +324,20 @@ ProbLayout prob_layout(const phpc_gemm_problem& q, int planes, bool modular) {
 }
 
 struct TableLayout {
-  size_t split, tprob, maps, tiles, sched, crt_first, end;
+  size_t split, tprob, maps, tiles, sched, crt_first, rows_first, cols_prob, end;
 };
+
+// Modular scheme: the lookup tables the plan writes for the CRT and the
+// residue splits (their kernels find a block's problem with one load).
+struct LookupSizes {
+  int64_t crt_blocks = 0, row_blocks = 0, col_blocks = 0;
+};
+
+int64_t row_pieces_of(const phpc_gemm_problem& q) { return (int64_t)q.m * ((q.k + 7) / 8); }
+
+int64_t residue_blocks_of(const phpc_gemm_problem& q) {
+  return (int64_t)ceil_div(q.n, kColBlockJ) * ceil_div((q.k + 7) / 8 * 8, kColBlockK);
+}
 
 // Output tiles of the batch at the narrowest tile width (an upper bound for
 // the plan's).
@@ -321,23 +347,35 @@ int64_t max_tiles(const phpc_gemm_problem* problems, int count) {
   return t;
 }
 
-// CRT blocks of the batch (0 if a problem is invalid: the callers check).
-int64_t max_crt_blocks(const phpc_gemm_problem* problems, int count) {
-  int64_t u = 0;
-  for (int i = 0; i < count; ++i)
-    if (problems[i].m > 0 && problems[i].n > 0) u += crt_units_of(problems[i].m, problems[i].n);
-  return crt_blocks_of(u);
+// Sizes of the modular plan's lookup tables (problems with a zero or
+// negative size add nothing: the callers refuse them).
+LookupSizes lookup_sizes(const phpc_gemm_problem* problems, int count, bool modular) {
+  LookupSizes z;
+  if (!modular) return z;
+  int64_t units = 0, pieces = 0;
+  for (int i = 0; i < count; ++i) {
+    const phpc_gemm_problem& q = problems[i];
+    if (q.m <= 0 || q.n <= 0 || q.k <= 0) continue;
+    units += crt_units_of(q.m, q.n);
+    pieces += row_pieces_of(q);
+    z.col_blocks += residue_blocks_of(q);
+  }
+  z.crt_blocks = crt_blocks_of(units);
+  z.row_blocks = (pieces + kResRowBlock - 1) / kResRowBlock;
+  return z;
 }
 
-TableLayout table_layout(int count, int64_t tiles, int64_t crt_blocks) {
+TableLayout table_layout(int count, int64_t tiles, const LookupSizes& look) {
   TableLayout T;
   T.split = 0;
   T.tprob = align_up(sizeof(GSplitProb) * (size_t)count, 256);
   T.maps = align_up(T.tprob + sizeof(TcGroupProblem) * (size_t)count, 256);
   T.tiles = align_up(T.maps + sizeof(CUtensorMap) * 2 * (size_t)count, 256);
   T.sched = align_up(T.tiles + sizeof(int4) * (size_t)tiles, 256);  // the GEMM's unit counter
-  T.crt_first = align_up(T.sched + sizeof(int), 256);  // modular scheme: the CRT blocks' first problems
-  T.end = align_up(T.crt_first + sizeof(int) * (size_t)crt_blocks, 256);
+  T.crt_first = align_up(T.sched + sizeof(int), 256);  // modular scheme: the CRT blocks' first problems,
+  T.rows_first = align_up(T.crt_first + sizeof(int) * (size_t)look.crt_blocks, 256);  // row blocks' first ones,
+  T.cols_prob = align_up(T.rows_first + sizeof(int) * (size_t)look.row_blocks, 256);  // column blocks' problems
+  T.end = align_up(T.cols_prob + sizeof(int) * (size_t)look.col_blocks, 256);
   return T;
 }
 
@@ -381,7 +419,9 @@ struct phpc_grouped_plan {
   int total_rows, total_cols, total_sblocks, total_rblocks, total_tiles, total_pieces, total_cunits,
       total_crt_units;
   phpc::GSplitProb* d_split;
-  const int* d_crt_first;  // modular scheme: first problem of each CRT block
+  const int* d_crt_first;  // modular scheme: first problem of each CRT block,
+  const int* d_rows_first;  // of each row-split block,
+  const int* d_cols_prob;   // the problem of each column-split block
   phpc::TcGroupTable table;
   phpc::PairList pairs;
   phpc::ModTable mods;  // modular scheme: moduli constants (grid widths are per problem)
@@ -439,10 +479,11 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
       g_scan_cols_merge_kernel<<<ceil_div(pl->total_cols, 256), 256, 0, side>>>(pl->d_split, pl->count,
                                                                                 pl->total_cols, pl->mods);
       with_crt_moduli(pl->mods.n, [&](auto nm) {
-        g_residue_rows_kernel<decltype(nm)::value><<<ceil_div(pl->total_pieces, 256), 256, 0, stream>>>(
-            pl->d_split, pl->count, pl->total_pieces, pl->mods);
+        g_residue_rows_kernel<decltype(nm)::value><<<ceil_div(pl->total_pieces, kResRowBlock), kResRowBlock, 0,
+                                                     stream>>>(pl->d_split, pl->d_rows_first, pl->count,
+                                                               pl->total_pieces, pl->mods);
         g_residue_cols_kernel<decltype(nm)::value><<<pl->total_rblocks, 256, 0, side>>>(
-            pl->d_split, pl->count, pl->total_rblocks, pl->mods);
+            pl->d_split, pl->d_cols_prob, pl->total_rblocks, pl->mods);
       });
       if (cudaGetLastError() != cudaSuccess || (side != stream && !stream_fork(side, stream))) return PHPC_ERR_CUDA;
     } else {
@@ -479,7 +520,7 @@ int run_grouped(const phpc_grouped_plan* pl, cudaStream_t stream) {
 }
 
 size_t grouped_workspace_bytes(const phpc_gemm_problem* problems, int count, int planes, bool modular) {
-  size_t total = table_layout(count, max_tiles(problems, count), modular ? max_crt_blocks(problems, count) : 0).end;
+  size_t total = table_layout(count, max_tiles(problems, count), lookup_sizes(problems, count, modular)).end;
   for (int i = 0; i < count; ++i) {
     if (!valid_problem(problems[i])) return 0;
     total += prob_layout(problems[i], planes, modular).end;
@@ -519,8 +560,7 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     pl->pairs = grouped_pairs(planes);
   }
 
-  const TableLayout T =
-      table_layout(count, max_tiles(problems, count), modular ? max_crt_blocks(problems, count) : 0);
+  const TableLayout T = table_layout(count, max_tiles(problems, count), lookup_sizes(problems, count, modular));
   uint8_t* base = static_cast<uint8_t*>(workspace);
   std::vector<GSplitProb> hs(count);
   std::vector<TcGroupProblem> ht(count);
@@ -568,8 +608,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     rows += q.m;
     cols += q.n;
     sblocks += g.nblk_j * ceil_div(q.k, 32);
-    rblocks += ceil_div(q.n, kColBlockJ) * ceil_div((int)L.ldp, kColBlockK);
-    pieces += (int64_t)q.m * (L.ldp / 8);
+    rblocks += static_cast<int>(residue_blocks_of(q));
+    pieces += row_pieces_of(q);
     cunits += (int64_t)q.n * ceil_div(q.k, kScanKChunk);
     if (modular) crt_units += crt_units_of(q.m, q.n);
 
@@ -615,6 +655,8 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
   pl->total_crt_units = static_cast<int>(crt_units);
   pl->d_split = reinterpret_cast<GSplitProb*>(base + T.split);
   pl->d_crt_first = reinterpret_cast<const int*>(base + T.crt_first);
+  pl->d_rows_first = reinterpret_cast<const int*>(base + T.rows_first);
+  pl->d_cols_prob = reinterpret_cast<const int*>(base + T.cols_prob);
   // the problem of each CRT block's first unit
   std::vector<int> hfirst(modular && rc == PHPC_OK ? crt_blocks_of(crt_units) : 0);
   for (size_t b = 0, i = 0; b < hfirst.size(); ++b) {
@@ -622,6 +664,15 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
     while (i + 1 < (size_t)count && hs[i + 1].crt_unit_start <= u) ++i;
     hfirst[b] = static_cast<int>(i);
   }
+  std::vector<int> hrows(modular && rc == PHPC_OK ? (pieces + kResRowBlock - 1) / kResRowBlock : 0);
+  for (size_t b = 0, i = 0; b < hrows.size(); ++b) {
+    const int64_t t = (int64_t)b * kResRowBlock;
+    while (i + 1 < (size_t)count && hs[i + 1].piece_start <= t) ++i;
+    hrows[b] = static_cast<int>(i);
+  }
+  std::vector<int> hcols(modular && rc == PHPC_OK ? rblocks : 0);
+  for (int i = 0; i < count && !hcols.empty(); ++i)
+    for (int64_t j = 0, nb = residue_blocks_of(problems[i]); j < nb; ++j) hcols[hs[i].rblock_start + j] = i;
   pl->table.count = count;
   pl->table.ntiles = tiles;
   pl->table.group_rows = 8;
@@ -660,6 +711,10 @@ int grouped_plan_create(phpc_grouped_plan** out, const phpc_gemm_problem* proble
                                      st) != cudaSuccess) ||
        (!hfirst.empty() && cudaMemcpyAsync(base + T.crt_first, hfirst.data(), sizeof(int) * hfirst.size(),
                                            cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+       (!hrows.empty() && cudaMemcpyAsync(base + T.rows_first, hrows.data(), sizeof(int) * hrows.size(),
+                                          cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+       (!hcols.empty() && cudaMemcpyAsync(base + T.cols_prob, hcols.data(), sizeof(int) * hcols.size(),
+                                          cudaMemcpyHostToDevice, st) != cudaSuccess) ||
        cudaStreamSynchronize(st) != cudaSuccess))
     rc = PHPC_ERR_CUDA;
   if (rc != PHPC_OK) {
