@@ -7,20 +7,23 @@
 // whole batch once:
 //  - a device table with one record per problem and the prefix sums of its
 //    rows, columns, split blocks and output tiles, plus two TMA descriptors
-//    per problem (A digit planes, B digit planes), written into the head of
+//    per problem (A digit planes, B digit planes) and a table of the output
+//    tiles (problem, tile row and column, K-steps), written into the head of
 //    the caller's workspace;
 //  - five kernels cover the batch (six launches: the column scan's reset):
 //    exponent scans of all rows, of all columns, digit splits of all rows,
 //    of all column blocks, and the
 //    persistent tcgen05 slice GEMM over the union of all output tiles
-//    (tc_gemm.cuh, grouped mode: a tile finds its problem by binary search);
+//    (tc_gemm.cuh, grouped mode: a work unit's tile comes from the tile
+//    table);
 //  - phpc_grouped_graph_launch captures those five launches once into a CUDA
 //    graph and replays it.
 // A modular-scheme plan (phpc_grouped_modular_plan_create) has six kernels:
 // the two scans, residue splits of all rows and of all column blocks, the
 // persistent residue GEMM over all tiles (each tile's residues go to its
 // problem's planes), and the CRT of all rows; every problem uses the plan's
-// moduli and the grid width of its own K.
+// moduli and the grid width of its own K. Its residue splits and CRT find a
+// block's problem in lookup tables the plan also writes.
 #include <cuda.h>
 
 #include <algorithm>
